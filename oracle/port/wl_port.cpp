@@ -888,6 +888,25 @@ int orc_huffman_decode(const uint32_t *words, int n_words, const int *table,
   auto bit = [&](long p) -> unsigned {
     return p < total ? (words[p >> 5] >> (p & 31)) & 1u : 0u;
   };
+  // A one-node tree gives its only symbol a zero-length code
+  // (computeEncodedBits, huffman.cc:147-160).  The reference's table walk
+  // indexes past such a table (undefined behaviour); decode it as what the
+  // encoder wrote: every token is that symbol, and a zero-run token still
+  // carries its 3 length bits.
+  if (n_table == 2 && table[0] == 0) {
+    int v = table[1];
+    if (v != dup_key) {
+      for (; i < n; i++) out[i] = v;
+      return i;
+    }
+    while (i < n && pos + 3 <= total) {
+      unsigned e = bit(pos) | (bit(pos + 1) << 1) | (bit(pos + 2) << 2);
+      pos += 3;
+      int L = 1 << (e + 3);
+      while (L-- > 0 && i < n) out[i++] = dup_value;
+    }
+    return i;
+  }
   while (i < n) {
     if (pos >= total) return i;
     int node = 0;

@@ -1,0 +1,131 @@
+"""Generate the golden fixtures in this directory from the REFERENCE ITSELF.
+
+Runs only where the reference checkout is present: it builds the reference's
+CPU path from its own sources (oracle/ref/Makefile, protobuf shim) and runs
+its ``test_compress_cpu`` and the ``ref_dump`` glue on seeded inputs.  The
+outputs committed here pin the oracle and the GPU library on machines without
+the reference.
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+Writes, per case: ``<case>.in.cube`` (input), ``<case>.<p>.cube`` (reference
+compressed output), ``<case>.<p>.d.cube`` (reference decompression of it),
+``<case>.<p>.coeffs.f32`` (reference transform output, rotated Z-X-Y order)
+and ``manifest.json`` (flags, sizes, threshold statistics, hashes).
+"""
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import build_oracle  # noqa: E402
+from wavelets_gb300 import cubefile, synth  # noqa: E402
+
+PARAMS = {
+    "p1": ["-steps", "-1", "-thresh", "0.5", "-qalg", "log", "-qcount", "256"],
+    "p2": ["-steps", "3,3,3", "-thresh", "0.95", "-qalg", "uniform", "-qcount", "1024"],
+    "p3": ["-wave", "haar", "-steps", "2,2,2", "-thresh", "0.9", "-qalg", "lloyd", "-qcount", "256"],
+    "p4": ["-steps", "2,1", "-thresh", "0.7", "-qalg", "log", "-qcount", "255", "-noz"],
+    "p5": ["-wave", "haar", "-thresh", "0.8", "-qalg", "uniform", "-qcount", "7"],
+    "p6": ["-steps", "0,0,0", "-thresh", "0.6", "-qalg", "log", "-qcount", "64"],
+    "p7": ["-steps", "4,4,4", "-thresh", "0.9", "-qalg", "lloyd", "-qcount", "255"],
+}
+
+# (case name, array, parameter sets)
+def cases():
+    out = []
+    small = synth.small_cases()
+    plans = [["p1", "p2", "p3"], ["p1", "p4", "p7"], ["p2", "p5", "p6"],
+             ["p1", "p5"], ["p2", "p3", "p7"], ["p1", "p4"], ["p3", "p6"],
+             ["p1", "p2", "p4"]]
+    for (name, arr), plan in zip(small, plans):
+        out.append((name, arr, plan))
+    rng = np.random.default_rng(11)
+    img = synth.scaled_blob_cubelet(rng, (1, 256, 256), np.uint8)
+    out.append(("uint8_1x256x256", img, ["p1", "p4"]))
+    # all-zero and constant cubes: threshold 0 -> 1e-16, single Huffman symbol
+    out.append(("float32_4x4x4_zero", np.zeros((4, 4, 4), np.float32), ["p1"]))
+    out.append(("uint8_1x8x8_const", np.full((1, 8, 8), 7, np.uint8), ["p2"]))
+    return out
+
+
+def sha(path):
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
+def kat_cdf97(ref_dump, tmp):
+    """cdf97 one step on the vector of dwt_cpu.cc:657 (x axis only)."""
+    v = np.array([7, 2, 3, 4, 5, 3, 1, 5, 7, 1, 9, 2, 4, 8, 2, 6], np.float32)
+    path = os.path.join(tmp, "kat.cube")
+    cubefile.write_file(path, [cubefile.from_array(v.reshape(1, 1, 16))])
+    d = os.path.join(tmp, "katdump")
+    os.makedirs(d, exist_ok=True)
+    subprocess.check_call([ref_dump, "-steps", "1,0,0", path,
+                           os.path.join(tmp, "kat.out.cube"), d])
+    return np.fromfile(os.path.join(d, "coeffs.f32"), np.float32)
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not os.path.isdir(ref):
+        sys.exit("reference checkout not found: " + ref)
+    build_oracle.build_reference(ref)
+    cli = os.path.join(ROOT, "oracle", "_ref", "test_compress_cpu")
+    dump = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+    manifest = {"generator": "tests/golden/make_golden.py",
+                "params": PARAMS, "cases": []}
+    with tempfile.TemporaryDirectory() as tmp:
+        kat = kat_cdf97(dump, tmp)
+        manifest["kat_cdf97_1step"] = {
+            "input": [7, 2, 3, 4, 5, 3, 1, 5, 7, 1, 9, 2, 4, 8, 2, 6],
+            "output_hex": [float(x).hex() for x in kat],
+            # printed in the reference's comment dwt_cpu.cc:680
+            "published": [7.00224, 3.52709, 6.82547, 2.87912, 7.34827, 7.39307,
+                          6.14146, 6.57857, 2.33178, -0.122068, -0.136087,
+                          -1.33848, 5.86312, 3.64358, -4.18374, -2.92383]}
+        for name, arr, plan in cases():
+            inp = os.path.join(HERE, name + ".in.cube")
+            cubefile.write_file(inp, [cubefile.from_array(arr)])
+            for p in plan:
+                out = os.path.join(HERE, f"{name}.{p}.cube")
+                dec = os.path.join(HERE, f"{name}.{p}.d.cube")
+                subprocess.check_call([cli, "-q", *PARAMS[p], inp, out])
+                subprocess.check_call([cli, "-q", "-d", out, dec])
+                d = os.path.join(tmp, name + p)
+                os.makedirs(d)
+                subprocess.check_call([dump, *PARAMS[p], inp,
+                                       os.path.join(tmp, "x.cube"), d])
+                shutil.copy(os.path.join(d, "coeffs.f32"),
+                            os.path.join(HERE, f"{name}.{p}.coeffs.f32"))
+                stats = {}
+                with open(os.path.join(d, "stats.txt")) as f:
+                    lines = f.read().split("\n")
+                for ln in lines[:8]:
+                    parts = ln.split()
+                    if parts:
+                        stats[parts[0]] = parts[1:]
+                manifest["cases"].append({
+                    "case": name, "params": p, "shape_zyx": list(arr.shape),
+                    "dtype": str(arr.dtype), "input": os.path.basename(inp),
+                    "output": os.path.basename(out),
+                    "decompressed": os.path.basename(dec),
+                    "coeffs": f"{name}.{p}.coeffs.f32",
+                    "stats": stats,
+                    "sha256": {"output": sha(out), "decompressed": sha(dec)}})
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    print("wrote", len(manifest["cases"]), "cases")
+
+
+if __name__ == "__main__":
+    main()
