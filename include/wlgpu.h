@@ -1,0 +1,177 @@
+/* libwlgpu: GB300 (sm_103a) cubelet compression behind a C ABI.
+ *
+ * Drop-in for the reference's cubelet compression path
+ * (transform -> threshold -> quantize -> count -> Huffman, and its inverse).
+ * The entry points replace these reference interfaces:
+ *
+ *   wl_compress_file / wl_decompress_file
+ *       test_compress_cpu / test_compress_gpu command line
+ *       (compressFile test_compress_cpu.cc:68-184, test_compress_gpu.cu:150-436;
+ *        decompressFile test_compress_cpu.cc:187-241): first uncompressed
+ *       cubelet of a .cube file in, one compressed cubelet out, same bytes.
+ *   wl_compress_cubelet
+ *       readData .. writeQuantData for one in-memory cubelet
+ *       (test_compress_common.h:173-248; waveletTransform :492,
+ *        thresh_cpu thresh_cpu.cc:80, quantize test_compress_cpu.cc:244,
+ *        writeQuantData test_compress_common.cc:198).
+ *   wl_decompress_cubelet
+ *       readQuantData + dequantize + inverse waveletTransform +
+ *       translateCubeDataToOriginal (test_compress_common.cc:850, :567, :492, :699).
+ *   wl_compress_batch
+ *       no reference counterpart: many cubelets per launch (the reference
+ *       compresses one cubelet per process, test_compress_common.cc:296-302).
+ *
+ * Conventions: every call returns a wl_status and never exits the process
+ * (the reference prints and exit(1)s on CUDA errors, cucheck.h:9-21);
+ * wl_last_error() describes the last failure on a context.  One context per
+ * host thread; a context owns one CUDA stream and its device workspace.
+ */
+#ifndef WLGPU_H
+#define WLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  WL_OK = 0,
+  WL_EINVAL = 1,    /* bad argument or unsupported parameter */
+  WL_ENOMEM = 2,    /* device or host allocation failed / budget exceeded */
+  WL_ETIMEOUT = 3,  /* a bounded wait ran out */
+  WL_EFORMAT = 4,   /* malformed .cube file or compressed stream */
+  WL_ECUDA = 5,     /* CUDA runtime error */
+  WL_EIO = 6        /* file open/read/write failed */
+} wl_status;
+
+/* element types; U8, I32 and F32 are the reference's (wavelet.h:41-46) */
+typedef enum { WL_U8 = 1, WL_I32 = 2, WL_F32 = 3, WL_U16 = 4 } wl_dtype;
+typedef enum { WL_HAAR = 1, WL_CDF97 = 2 } wl_wavelet;            /* wavelet.h:33-38 */
+typedef enum { WL_UNIFORM = 1, WL_LOG = 2, WL_LLOYD = 3 } wl_quant; /* wavelet.h:25-30 */
+
+/* Compression parameters (WaveletCompressionParam, wavelet.h:221-295, with the
+ * command-line defaults of wavelet.h:48-53). */
+typedef struct {
+  int steps[3];             /* x, y, z; -1 = ceil(log2(axis length)) */
+  int wavelet;              /* wl_wavelet */
+  float threshold_fraction; /* fraction of coefficients set to the zero bin */
+  int bin_count;            /* 2..4096 */
+  int quant_alg;            /* wl_quant */
+  int compress_zeros;       /* 1 = zero-run Huffman tokens (reference default) */
+  int lloyd_iters;          /* Lloyd iterations on the |coefficient| histogram */
+  int exact_transform;      /* 1 = reference float operation order (filter bank);
+                               0 = lifting (default) */
+} wl_params;
+
+/* Fill p with the reference's defaults. */
+void wl_params_default(wl_params *p);
+
+/* One compressed cubelet: metadata of the CubeletBuffer /
+ * CompressionParametersBuffer messages (wavelet_compress.proto) plus the
+ * Huffman words.  Arrays are owned by the library; release with wl_result_free. */
+typedef struct {
+  int size[3];              /* stored (rotated Z-X-Y) size: width, height, depth */
+  int original_size[3];
+  int original_dtype;       /* wl_dtype of the input */
+  int steps[3];             /* after clamping */
+  int wavelet, quant_alg, bin_count;
+  float threshold_fraction;
+  float threshold_value;
+  float max_value;          /* largest |coefficient| (quant_max_value) */
+  float min_coef, max_coef; /* signed extremes as the reference tracks them */
+  int zero_bin;
+  int dup_key, dup_value;   /* -1 when zero-run tokens are off */
+  int longest_code;         /* bits */
+  int n_words;              /* Huffman stream length, 32-bit words */
+  uint32_t *words;
+  int n_decode;             /* Huffman decode table length (ints) */
+  int32_t *decode;
+  int n_boundaries, n_values; /* codebook (Lloyd only) */
+  float *boundaries, *values;
+} wl_result;
+
+void wl_result_free(wl_result *r);
+
+typedef struct wl_ctx wl_ctx;
+
+/* Create a context on CUDA device `device`. */
+wl_status wl_init(int device, wl_ctx **ctx);
+void wl_destroy(wl_ctx *ctx);
+const char *wl_last_error(const wl_ctx *ctx);
+
+/* Compress one cubelet.  data points to X*Y*Z elements (x fastest) of dtype;
+ * it may be host or device memory (data_on_device).  out is filled and owns
+ * its arrays. */
+wl_status wl_compress_cubelet(wl_ctx *ctx, const void *data, int dtype,
+                              const int size[3], int data_on_device,
+                              const wl_params *params, wl_result *out);
+
+/* A batch entry for wl_compress_batch. */
+typedef struct {
+  const void *data;         /* X*Y*Z elements, x fastest */
+  int dtype;
+  int size[3];
+  wl_params params;
+} wl_cubelet;
+
+/* Compress n cubelets of any sizes/dtypes/parameters in one pass of batched
+ * launches.  data_on_device: all inputs are device pointers. */
+wl_status wl_compress_batch(wl_ctx *ctx, const wl_cubelet *items, int n,
+                            int data_on_device, wl_result *outs);
+
+/* Decompress: inverse of wl_compress_cubelet.  out receives
+ * original_size elements of out_dtype (WL_U8 clamps and truncates like the
+ * reference's floatToByte; WL_I32 rounds (int)(f+0.5f); WL_U16 rounds and
+ * clamps to 0..65535; WL_F32 as is). */
+wl_status wl_decompress_cubelet(wl_ctx *ctx, const wl_result *in, int out_dtype,
+                                void *out, int out_on_device);
+
+/* The transform alone (waveletTransform, test_compress_common.cc:492-564).
+ * Forward: data (X*Y*Z elements of dtype, x fastest) is padded by repeating
+ * edge values to a multiple of 2^steps per axis and transformed; coeffs
+ * receives the padded element count of floats in the stored Z-X-Y order and
+ * stored_size the stored (rotated) width, height, depth.  Inverse: coeffs in
+ * that order back to original_size elements of out_dtype. */
+wl_status wl_forward_transform(wl_ctx *ctx, const void *data, int dtype,
+                               const int size[3], const wl_params *params,
+                               float *coeffs, size_t coeffs_cap,
+                               int stored_size[3]);
+wl_status wl_inverse_transform(wl_ctx *ctx, const float *coeffs,
+                               const int stored_size[3], const int steps[3],
+                               int wavelet, const int original_size[3],
+                               int out_dtype, void *out);
+
+/* Command-line equivalents: read the first uncompressed cubelet of in_path,
+ * write a .cube with one compressed cubelet (no footer, like the reference);
+ * decompress writes the restored cubelet with a footer. */
+wl_status wl_compress_file(wl_ctx *ctx, const char *in_path,
+                           const char *out_path, const wl_params *params);
+wl_status wl_decompress_file(wl_ctx *ctx, const char *in_path,
+                             const char *out_path);
+
+/* Serialize one compressed cubelet as a complete .cube file image
+ * (header + length + CubeletBuffer + words), as the reference writes it.
+ * *buf is malloc'ed; free with wl_free. */
+wl_status wl_encode_cube(const wl_result *r, int footer, uint8_t **buf,
+                         size_t *len);
+void wl_free(void *p);
+
+/* Per-stage device timings (milliseconds, CUDA events on the context's
+ * stream) of the last compress call: transform, select, quantize+count,
+ * Huffman build, encode, total device time. */
+wl_status wl_last_timings(const wl_ctx *ctx, float out[6]);
+
+/* Synchronize the context's stream. */
+wl_status wl_sync(wl_ctx *ctx);
+
+/* Page-locked host memory for inputs and outputs of the host-pointer entry
+ * points (copies from it overlap with device work). */
+void *wl_host_alloc(size_t bytes);
+void wl_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

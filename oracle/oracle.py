@@ -91,6 +91,23 @@ def encode(coeffs: np.ndarray, frac: float, bin_count: int, quant_alg: int,
             "values": vals[:res.n_values].copy()}
 
 
+def huffman_encode(bins, bin_count, zero_bin):
+    """Reference Huffman coding of given bins (zero_bin < 0: no zero runs)."""
+    b = np.ascontiguousarray(bins, np.int32).ravel()
+    res = Result()
+    cap = b.size * 2 + 1024
+    words = np.empty(cap, np.uint32)
+    dec = np.empty(8 * (bin_count + 2), np.int32)
+    hist = np.empty(bin_count + 1, np.int64)
+    rc = lib().orc_huffman_encode(_ptr(b), b.size, bin_count, zero_bin, ctypes.byref(res),
+                                  _ptr(words), cap, _ptr(dec), dec.size, _ptr(hist))
+    if rc != 0:
+        raise RuntimeError("oracle huffman buffer too small")
+    return {"words": words[:res.n_words].copy(), "decode": dec[:res.n_decode].copy(),
+            "hist": hist, "longest": res.longest_code, "dup_key": res.dup_key,
+            "dup_value": res.dup_value}
+
+
 def quantize(coeffs, quant_alg, bin_count, threshold, max_abs, boundaries=None):
     c = np.ascontiguousarray(coeffs, np.float32).ravel()
     out = np.empty(c.size, np.int32)

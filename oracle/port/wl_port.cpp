@@ -527,6 +527,8 @@ struct Encoded {
   std::vector<float> bnd, vals;
 };
 
+void huffman_part(Encoded &e, int n, int binCount, int zeroBin);
+
 // Threshold + quantize + Huffman (test_compress_cpu.cc:97-172).
 void encode_coeffs(const float *c, int n, float frac, int binCount, int qalg,
                    int compressZeros, Encoded &e) {
@@ -542,6 +544,7 @@ void encode_coeffs(const float *c, int n, float frac, int binCount, int qalg,
   }
   std::sort(a.begin(), a.end());
   int k = (int)(frac * n);
+  if (k >= n) k = n - 1;  // frac == 1 reads past the array in the reference
   float thr = a[k];
   if (thr == 0) thr = 1e-16;
   int nonzero = n - k - 1;
@@ -570,7 +573,11 @@ void encode_coeffs(const float *c, int n, float frac, int binCount, int qalg,
   e.r.zero_bin = zeroBin;
   e.r.n_boundaries = (int)e.bnd.size();
   e.r.n_values = (int)e.vals.size();
+  huffman_part(e, n, binCount, zeroBin);
+}
 
+// huffScan + tree + encodeToStream on e.bins (test_compress_common.cc:953-1022)
+void huffman_part(Encoded &e, int n, int binCount, int zeroBin) {
   // huffScan (test_compress_common.cc:901-921) with the dup value set when
   // zero runs are on (initHuffman :960-994)
   int dupValue = (zeroBin >= 0 && zeroBin < binCount) ? zeroBin : -1;
@@ -835,6 +842,28 @@ int orc_encode(const float *coeffs, int n, float frac, int binCount, int qalg,
   if (hist_out) memcpy(hist_out, e.hist.data(), sizeof(int64_t) * e.hist.size());
   if (bnd_out && !e.bnd.empty()) memcpy(bnd_out, e.bnd.data(), sizeof(float) * e.bnd.size());
   if (vals_out && !e.vals.empty()) memcpy(vals_out, e.vals.data(), sizeof(float) * e.vals.size());
+  if (words_out) {
+    if ((int)e.words.size() > words_cap) return 1;
+    memcpy(words_out, e.words.data(), 4 * e.words.size());
+  }
+  if (decode_out) {
+    if ((int)e.decode.size() > decode_cap) return 1;
+    memcpy(decode_out, e.decode.data(), sizeof(int) * e.decode.size());
+  }
+  return 0;
+}
+
+int orc_huffman_encode(const int *bins, int n, int binCount, int zeroBin,
+                       orc_result *res, uint32_t *words_out, int words_cap,
+                       int *decode_out, int decode_cap, int64_t *hist_out) {
+  Encoded e;
+  memset(&e.r, 0, sizeof e.r);
+  e.bins.assign(bins, bins + n);
+  e.r.bin_count = binCount;
+  e.r.zero_bin = zeroBin;
+  huffman_part(e, n, binCount, zeroBin);
+  if (res) *res = e.r;
+  if (hist_out) memcpy(hist_out, e.hist.data(), sizeof(int64_t) * e.hist.size());
   if (words_out) {
     if ((int)e.words.size() > words_cap) return 1;
     memcpy(words_out, e.words.data(), 4 * e.words.size());

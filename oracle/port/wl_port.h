@@ -71,6 +71,14 @@ int orc_quantize(const float *coeffs, int n, int quant_alg, int bin_count,
                  float threshold, float max_abs, const float *boundaries,
                  const float *values, int *bins_out);
 
+/* Huffman-encode given bins exactly as the reference does after quantizing
+ * (initHuffman + huffScan + computeHuffmanCoding + encodeToStream,
+ * test_compress_common.cc:953-1022, huffman.cc:42-97, huffman.h:242-296).
+ * zero_bin < 0 disables zero-run tokens.  hist_out: bin_count+1 counts. */
+int orc_huffman_encode(const int *bins, int n, int bin_count, int zero_bin,
+                       orc_result *res, uint32_t *words_out, int words_cap,
+                       int *decode_out, int decode_cap, int64_t *hist_out);
+
 /* Dequantize bins (dequantize, test_compress_common.cc:567-584). */
 int orc_dequantize(const int *bins, int n, int quant_alg, int bin_count,
                    float threshold, float max_abs, const float *values,

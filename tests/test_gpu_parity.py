@@ -1,0 +1,237 @@
+"""GPU parity: libwlgpu (through its C ABI) against the reference's outputs
+and the oracle.
+
+* exact mode (reference float order): the .cube files the GPU writes are
+  byte-identical to the reference's own output files in tests/golden;
+* lifting mode: coefficients within 1e-5 of the reference's (relative to the
+  largest coefficient), and threshold / bins / histogram / Huffman stream
+  bit-exact against the oracle fed the GPU's coefficients;
+* decompression within tolerance of the oracle's; batch == single.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle
+from wavelets_gb300 import cubefile, lib, params as P, synth
+
+pytestmark = pytest.mark.gpu
+
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+TRANSFORM_RTOL = 1e-5  # max|gpu - ref| / max|ref| for the lifting transform
+QALG = {cubefile.PB_UNIFORM: oracle.UNIFORM, cubefile.PB_LOG: oracle.LOG,
+        cubefile.PB_LLOYD: oracle.LLOYD}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from wavelets_gb300 import build
+    build.build()
+    c = lib.Context(0)
+    yield c
+    c.close()
+
+
+def _params(case, exact=False):
+    p, _, _ = P.parse_flags(MANIFEST["params"][case["params"]])
+    p.exact_transform = exact
+    return p
+
+
+def _ids(cases):
+    return [f"{c['case']}.{c['params']}" for c in cases]
+
+
+def _input(case):
+    c = cubefile.read_file(os.path.join(GOLDEN, case["input"]))[0]
+    a = c.array()
+    return a
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_exact_mode_file_identical_to_reference(ctx, case, tmp_path):
+    out = str(tmp_path / "o.cube")
+    ctx.compress_file(os.path.join(GOLDEN, case["input"]), out, _params(case, exact=True))
+    assert open(out, "rb").read() == open(os.path.join(GOLDEN, case["output"]), "rb").read()
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_decompress_reference_files(ctx, case, tmp_path):
+    """Decompress the reference's compressed file; compare with the
+    reference's own decompression (lifting synthesis vs the reference filter
+    bank: float tolerance, +-1 for integer outputs that round or truncate)."""
+    out = str(tmp_path / "d.cube")
+    ctx.decompress_file(os.path.join(GOLDEN, case["output"]), out)
+    got = cubefile.read_file(out)[0]
+    want = cubefile.read_file(os.path.join(GOLDEN, case["decompressed"]))[0]
+    assert (got.width, got.height, got.depth, got.data_type) == \
+        (want.width, want.height, want.depth, want.data_type)
+    g = got.array().astype(np.float64)
+    w = want.array().astype(np.float64)
+    if want.data_type == cubefile.FLOAT32:
+        scale = max(1.0, float(np.abs(w).max()))
+        assert np.abs(g - w).max() <= 1e-4 * scale
+    else:
+        diff = np.abs(g - w)
+        assert diff.max() <= 1
+        assert (diff > 0).mean() < 0.01
+
+
+CDF = [c for c in MANIFEST["cases"] if "haar" not in MANIFEST["params"][c["params"]]]
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_transform_matches_reference(ctx, case):
+    p = _params(case)
+    coeffs, stored = ctx.forward_transform(_input(case), p)
+    ref = np.fromfile(os.path.join(GOLDEN, case["coeffs"]), np.float32)
+    assert coeffs.shape == ref.shape
+    scale = float(np.abs(ref).max())
+    if scale == 0:
+        assert np.abs(coeffs).max() == 0
+        return
+    err = float(np.abs(coeffs.astype(np.float64) - ref).max()) / scale
+    assert err <= TRANSFORM_RTOL, err
+    if p.wavelet == P.HAAR or p.exact_transform:
+        assert np.array_equal(coeffs, ref)
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_exact_transform_bit_identical(ctx, case):
+    coeffs, _ = ctx.forward_transform(_input(case), _params(case, exact=True))
+    ref = np.fromfile(os.path.join(GOLDEN, case["coeffs"]), np.float32)
+    assert np.array_equal(coeffs, ref)
+
+
+def _check_integer_stages(ctx, arr, p):
+    """GPU result vs the oracle fed the GPU's own coefficients."""
+    comp = ctx.compress(arr, p)
+    coeffs, stored = ctx.forward_transform(arr, p)
+    assert tuple(stored) == tuple(comp.size)
+    if p.quant_alg == P.LLOYD:
+        # codebook: trained differently (histogram Lloyd); bins exact given it
+        bins = oracle.quantize(coeffs, oracle.LLOYD, p.bin_count, comp.threshold_value,
+                               comp.max_value, comp.boundaries)
+        zb = comp.zero_bin if p.compress_zeros else -1
+        enc = oracle.huffman_encode(bins, p.bin_count, zb)
+        ref_thr = oracle.encode(coeffs, p.threshold_fraction, p.bin_count, oracle.UNIFORM,
+                                p.compress_zeros)["threshold"]
+        assert np.float32(comp.threshold_value) == np.float32(ref_thr)
+    else:
+        enc = oracle.encode(coeffs, p.threshold_fraction, p.bin_count, p.quant_alg,
+                            p.compress_zeros)
+        assert np.float32(comp.threshold_value) == np.float32(enc["threshold"])
+        assert np.float32(comp.max_value) == np.float32(enc["max_abs"])
+        assert comp.zero_bin == (enc["zero_bin"] if p.compress_zeros else comp.zero_bin)
+    assert comp.dup_key == enc["dup_key"]
+    assert comp.dup_value == enc["dup_value"]
+    assert list(comp.decode) == list(enc["decode"])
+    assert comp.longest_code == enc["longest"]
+    assert np.array_equal(comp.words, enc["words"])
+    return comp, coeffs
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_integer_stages_bit_exact(ctx, case):
+    _check_integer_stages(ctx, _input(case), _params(case))
+
+
+EDGE = [
+    ("zeros", np.zeros((4, 4, 4), np.float32), P.Params()),
+    ("const", np.full((1, 8, 8), 7, np.uint8), P.Params(quant_alg=P.UNIFORM)),
+    ("tiny", np.arange(2, dtype=np.float32).reshape(1, 1, 2), P.Params()),
+    ("one", np.ones((1, 1, 1), np.float32), P.Params()),
+    ("bins2", synth.volume_f32(3, (8, 8, 8), 4), P.Params(bin_count=2, quant_alg=P.UNIFORM)),
+    ("bins3log", synth.volume_f32(4, (8, 8, 8), 4), P.Params(bin_count=3)),
+    ("bins4096", synth.volume_f32(5, (16, 16, 16), 8), P.Params(bin_count=4096, quant_alg=P.UNIFORM,
+                                                                 threshold_fraction=0.2)),
+    ("noz", synth.volume_f32(6, (9, 10, 11), 8), P.Params(compress_zeros=False)),
+    ("thresh0", synth.volume_f32(7, (8, 8, 8), 8), P.Params(threshold_fraction=0.0)),
+    ("thresh1", synth.volume_f32(8, (8, 8, 8), 8), P.Params(threshold_fraction=1.0)),
+    ("steps0", synth.volume_f32(9, (5, 6, 7), 4), P.Params(steps=(0, 0, 0))),
+    ("steps_mixed", synth.volume_f32(10, (12, 20, 24), 8), P.Params(steps=(1, 0, 2))),
+    ("haar_u16", synth.scaled_blob_cubelet(np.random.default_rng(3), (16, 16, 16), np.uint16),
+     P.Params(wavelet=P.HAAR, quant_alg=P.UNIFORM, bin_count=1024)),
+    ("lloyd_even", synth.volume_f32(11, (16, 24, 32), 10), P.Params(quant_alg=P.LLOYD, bin_count=256,
+                                                                     threshold_fraction=0.9)),
+    ("lloyd_odd", synth.volume_f32(12, (16, 16, 16), 10), P.Params(quant_alg=P.LLOYD, bin_count=255,
+                                                                    threshold_fraction=0.8)),
+    ("long_runs", np.pad(np.ones((2, 2, 2), np.float32), ((0, 30), (0, 30), (0, 62))),
+     P.Params(threshold_fraction=0.99)),
+]
+
+
+@pytest.mark.parametrize("name,arr,p", EDGE, ids=[e[0] for e in EDGE])
+def test_edge_cases(ctx, name, arr, p):
+    comp, coeffs = _check_integer_stages(ctx, arr, p)
+    # decoding the GPU stream with the reference's table walk gives bins of
+    # the right count
+    bins = oracle.huffman_decode(comp.words, comp.decode, comp.dup_key, comp.dup_value,
+                                 coeffs.size)
+    assert bins.size == coeffs.size
+
+
+def test_batch_equals_single(ctx):
+    rng = np.random.default_rng(5)
+    items = []
+    for i in range(12):
+        shape = tuple(int(rng.choice([4, 8, 12, 16, 32])) for _ in range(3))
+        dt = [np.uint8, np.uint16, np.float32][i % 3]
+        p = P.Params(wavelet=P.HAAR if i % 2 else P.CDF97,
+                     quant_alg=[P.UNIFORM, P.LOG, P.LLOYD][i % 3],
+                     bin_count=[256, 1024, 255][i % 3], threshold_fraction=0.9)
+        items.append((synth.scaled_blob_cubelet(rng, shape, dt), p))
+    batch = ctx.compress_batch(items)
+    for (a, p), b in zip(items, batch):
+        s = ctx.compress(a, p)
+        assert np.array_equal(s.words, b.words)
+        assert np.array_equal(s.decode, b.decode)
+        assert s.threshold_value == b.threshold_value
+        assert np.array_equal(s.boundaries, b.boundaries)
+
+
+def test_roundtrip_against_oracle(ctx):
+    """GPU decompression vs the oracle's dequantize + inverse transform of
+    the same stream."""
+    arr = synth.volume_f32(13, (32, 48, 64), 30)
+    p = P.Params(steps=(3, 3, 3), threshold_fraction=0.95, quant_alg=P.UNIFORM, bin_count=1024)
+    comp = ctx.compress(arr, p)
+    got = ctx.decompress(comp)
+    n = int(np.prod(comp.size))
+    bins = oracle.huffman_decode(comp.words, comp.decode, comp.dup_key, comp.dup_value, n)
+    deq = oracle.dequantize(bins, oracle.UNIFORM, p.bin_count, comp.threshold_value,
+                            comp.max_value)
+    Zp, Xp, Yp = comp.size
+    ref = oracle.inverse(deq, (Zp, Yp, Xp), comp.steps, p.wavelet)
+    ref = ref[:arr.shape[0], :arr.shape[1], :arr.shape[2]]
+    assert got.shape == arr.shape
+    scale = float(np.abs(ref).max())
+    assert float(np.abs(got.astype(np.float64) - ref).max()) <= 1e-4 * scale
+
+
+def test_round_trip_psnr_full_volume_f32(ctx):
+    """256^3 float32 volume, CDF9/7 3,3,3, keep 5%, uniform 1024 bins:
+    decompressed PSNR (peak = max - min of the original) and the Huffman
+    stream identical to the oracle's coding of the GPU coefficients."""
+    arr = synth.volume_f32()
+    p = P.Params(steps=(3, 3, 3), threshold_fraction=0.95, quant_alg=P.UNIFORM, bin_count=1024)
+    comp, coeffs = _check_integer_stages(ctx, arr, p)
+    back = ctx.decompress(comp)
+    peak = float(arr.max() - arr.min())
+    mse = float(np.mean((back.astype(np.float64) - arr) ** 2))
+    psnr = 10 * np.log10(peak * peak / mse)
+    assert psnr > 30, psnr
+
+
+def test_plain_2d_u8_full_size(ctx):
+    """2048x2048 uint8, CDF9/7 11,11,0, keep 10%, log 256 bins."""
+    arr = synth.plain_2d()
+    p = P.Params(steps=(11, 11, 0), threshold_fraction=0.9, quant_alg=P.LOG, bin_count=256)
+    comp, coeffs = _check_integer_stages(ctx, arr, p)
+    back = ctx.decompress(comp)
+    mse = float(np.mean((back.astype(np.float64) - arr) ** 2))
+    psnr = 10 * np.log10(255.0 ** 2 / mse)
+    assert psnr > 25, psnr

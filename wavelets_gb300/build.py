@@ -1,0 +1,93 @@
+"""Build libwlgpu (CUDA for sm_103a + C++ host code) in-tree.
+
+Outputs ``wavelets_gb300/_lib/libwlgpu.so`` and the command-line tool
+``wavelets_gb300/_lib/wl_compress``.  Translation units compile in parallel;
+objects are rebuilt only when a source or header is newer.
+"""
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+OBJ = os.path.join(OUT, "obj")
+INCLUDE = os.path.join(ROOT, "include")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _cuda_home():
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    return "/usr/local/cuda"
+
+
+def _nvcc():
+    return shutil.which("nvcc") or os.path.join(_cuda_home(), "bin", "nvcc")
+
+
+def _headers():
+    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src, verbose=False):
+    base = os.path.splitext(os.path.basename(src))[0]
+    obj = os.path.join(OBJ, base + ".o")
+    if not _stale(obj, [src] + _headers()):
+        return obj
+    if src.endswith(".cu"):
+        cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+               "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+    else:
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+               "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(_cuda_home(), "include"),
+               "-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and r.stderr:
+        print(r.stderr)
+    return obj
+
+
+def build(verbose=False):
+    """Compile every translation unit and link; returns the library path."""
+    os.makedirs(OBJ, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    lib_srcs = [s for s in srcs if os.path.basename(s) != "cli.cpp"]
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), lib_srcs))
+    lib = os.path.join(OUT, "libwlgpu.so")
+    if _stale(lib, objs):
+        cmd = [_nvcc(), *ARCH, "-shared", *objs, "-o", lib, "-lcudart_static", "-lrt", "-ldl",
+               "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    cli = os.path.join(OUT, "wl_compress")
+    if os.path.exists(cli_src) and _stale(cli, [cli_src, lib]):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", cli, "-L", OUT,
+               "-lwlgpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return lib
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(verbose="-v" in sys.argv))

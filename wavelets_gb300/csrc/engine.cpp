@@ -1,0 +1,991 @@
+// libwlgpu engine: context, device workspace, batch planning and the C ABI.
+//
+// One call compresses a batch of cubelets of any sizes, dtypes and
+// parameters with a fixed sequence of batched launches on the context's
+// stream: transform (one launch per axis; the x pass once per input dtype),
+// radix select, quantizer set-up, Lloyd (if any cubelet uses it), quantize +
+// count, zero-run join, Huffman build, encode.  Cubelets that use the log
+// quantizer need one host round trip after the select (their bin boundaries
+// are computed with the host's logf, quant_host.cpp).  Device memory is a set
+// of grow-only buffers owned by the context and reused across calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cubelet_io.h"
+#include "wl_internal.h"
+
+using namespace wl;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+// Per-cubelet plan computed on the host.
+struct Plan {
+  const void *data;
+  int dtype;
+  int X, Y, Z;
+  wl_params p;
+  int sx, sy, sz;
+  int Xp, Yp, Zp;
+  long long n;
+  long long inOff;     // bytes into the input staging buffer (host inputs)
+  long long coefOff;   // elements
+  long long chunkBase;
+  int nChunks;
+  long long wordsCap;
+  int tableOff;
+  bool identity;       // all steps zero: no transform, no axis rotation
+};
+
+int dtype_size(int dt) {
+  switch (dt) {
+    case WL_U8: return 1;
+    case WL_U16: return 2;
+    case WL_I32: return 4;
+    case WL_F32: return 4;
+    default: return 0;
+  }
+}
+
+int ceil_log2(unsigned x) {  // ceilLog2 (dwt_cpu.cc:75-78)
+  if (x == 0) return 0;
+  int n = 0;
+  unsigned v = x - 1;
+  while (v) { n++; v >>= 1; }
+  return n;
+}
+
+int padded_length(int len, int steps) {  // dwt_padded_length (dwt_cpu.cc:212-219)
+  int mod = 1 << steps;
+  return mod * ((len - 1) / mod + 1);
+}
+
+}  // namespace
+
+struct wl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  DevBuf input, coef, coef2, bins, state, cub, selHist, lloydHist, qtable, dqtable,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, codes, codeLen, decode,
+      words, passes, logHdr, outbuf;
+  HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals;
+  cudaEvent_t ev[7] = {};
+  float timings[6] = {0, 0, 0, 0, 0, 0};
+};
+
+namespace {
+
+wl_status fail(wl_ctx *c, wl_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return s;
+}
+
+#define CU(expr)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return fail(ctx, WL_ECUDA, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+wl_status ensure(wl_ctx *ctx, DevBuf &b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.cap >= bytes) return WL_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t want = bytes + bytes / 4;
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ENOMEM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+  }
+  b.cap = want;
+  return WL_OK;
+}
+
+wl_status ensure_host(wl_ctx *ctx, HostBuf &b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.cap >= bytes) return WL_OK;
+  if (b.p) cudaFreeHost(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t want = bytes + bytes / 4;
+  cudaError_t e = cudaMallocHost(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ENOMEM, "cudaMallocHost(%zu) failed: %s", want, cudaGetErrorString(e));
+  }
+  b.cap = want;
+  return WL_OK;
+}
+
+#define TRY(expr)                          \
+  do {                                     \
+    wl_status s_ = (expr);                 \
+    if (s_ != WL_OK) return s_;            \
+  } while (0)
+
+template <class T> T *P(DevBuf &b) { return static_cast<T *>(b.p); }
+template <class T> T *H(HostBuf &b) { return static_cast<T *>(b.p); }
+
+wl_status check_params(wl_ctx *ctx, const wl_params &p) {
+  if (p.wavelet != WL_HAAR && p.wavelet != WL_CDF97)
+    return fail(ctx, WL_EINVAL, "unknown wavelet %d", p.wavelet);
+  if (p.quant_alg != WL_UNIFORM && p.quant_alg != WL_LOG && p.quant_alg != WL_LLOYD)
+    return fail(ctx, WL_EINVAL, "unknown quantization algorithm %d", p.quant_alg);
+  if (p.bin_count < 2 || p.bin_count > kMaxBins)
+    return fail(ctx, WL_EINVAL, "bin count %d outside 2..%d", p.bin_count, kMaxBins);
+  if (!(p.threshold_fraction >= 0.f && p.threshold_fraction <= 1.f))
+    return fail(ctx, WL_EINVAL, "threshold fraction %g outside [0,1]", p.threshold_fraction);
+  if (p.quant_alg == WL_LLOYD && p.bin_count < 3)
+    return fail(ctx, WL_EINVAL, "Lloyd quantization needs at least 3 bins");
+  return WL_OK;
+}
+
+// Build PassDescs for one cubelet's forward transform.
+void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
+                    std::vector<PassDesc> *xs, std::vector<PassDesc> &ys,
+                    std::vector<PassDesc> &zs) {
+  const int big = 0x7fffffff;
+  const float *c = coef + pl.coefOff;
+  float *o = coef + pl.coefOff;
+  float *o2 = coef2 + pl.coefOff;
+  const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
+  PassDesc d;
+  memset(&d, 0, sizeof d);
+  d.cropL = d.cropB = d.cropA = big;
+  // x pass: rows (z, y) of the source, REPEAT padding by clamping
+  d.in = in;
+  d.inSA = (long long)pl.X * pl.Y;
+  d.inSB = pl.X;
+  d.clampL = pl.X; d.clampB = pl.Y; d.clampA = pl.Z;
+  d.L = pl.Xp; d.B = pl.Yp; d.rows = (int)(Yp * Zp);
+  d.wavelet = pl.p.wavelet; d.exact = pl.p.exact_transform;
+  if (pl.identity) {
+    d.out = o;
+    d.outSA = Xp * Yp; d.outSB = Xp; d.outSC = 1;
+    d.steps = 0;
+  } else {
+    d.out = o2;                       // x-y-z -> y-z-x
+    d.outSA = Yp; d.outSB = 1; d.outSC = Yp * Zp;
+    d.steps = pl.sx;
+  }
+  d.T = dwt_tile_rows(d.L, d.exact && d.wavelet == WL_CDF97);
+  d.tiles = (d.rows + d.T - 1) / d.T;
+  xs[pl.dtype].push_back(d);
+  if (pl.identity) return;
+  // y pass: rows (x, z) of the y-z-x cube -> z-x-y
+  PassDesc e;
+  memset(&e, 0, sizeof e);
+  e.cropL = e.cropB = e.cropA = big;
+  e.clampL = e.clampB = e.clampA = big;
+  e.in = o2;
+  e.inSA = Zp * Yp; e.inSB = Yp;
+  e.L = pl.Yp; e.B = pl.Zp; e.rows = (int)(Zp * Xp);
+  e.out = o;
+  e.outSA = Zp; e.outSB = 1; e.outSC = Zp * Xp;
+  e.steps = pl.sy; e.wavelet = pl.p.wavelet; e.exact = pl.p.exact_transform;
+  e.T = dwt_tile_rows(e.L, e.exact && e.wavelet == WL_CDF97);
+  e.tiles = (e.rows + e.T - 1) / e.T;
+  ys.push_back(e);
+  if (pl.sz == 0) return;
+  // z pass: rows (y, x) of the z-x-y cube, in place
+  PassDesc f = e;
+  f.in = c;
+  f.inSA = Xp * Zp; f.inSB = Zp;
+  f.L = pl.Zp; f.B = pl.Xp; f.rows = (int)(Xp * Yp);
+  f.out = o;
+  f.outSA = Xp * Zp; f.outSB = Zp; f.outSC = 1;
+  f.steps = pl.sz;
+  f.T = dwt_tile_rows(f.L, f.exact && f.wavelet == WL_CDF97);
+  f.tiles = (f.rows + f.T - 1) / f.T;
+  zs.push_back(f);
+}
+
+// Upload a group of passes (descriptor + tile prefix) and launch it.
+wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
+                    int inType, int outType, bool inverse) {
+  if (g.empty()) return WL_OK;
+  const size_t n = g.size();
+  const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int) + 64;
+  if (hoff + bytes > ctx->hPasses.cap || hoff + bytes > ctx->passes.cap)
+    return fail(ctx, WL_ENOMEM, "pass staging too small");
+  char *h = H<char>(ctx->hPasses) + hoff;
+  char *d = P<char>(ctx->passes) + hoff;
+  memcpy(h, g.data(), n * sizeof(PassDesc));
+  int *tp = reinterpret_cast<int *>(h + n * sizeof(PassDesc));
+  int tiles = 0, smem = 0;
+  for (size_t i = 0; i < n; i++) {
+    tp[i] = tiles;
+    tiles += g[i].tiles;
+    smem = std::max(smem, dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
+  }
+  tp[n] = tiles;
+  CU(cudaMemcpyAsync(d, h, bytes - 64, cudaMemcpyHostToDevice, ctx->stream));
+  launch_dwt_pass(reinterpret_cast<const PassDesc *>(d),
+                  reinterpret_cast<const int *>(d + n * sizeof(PassDesc)), (int)n, tiles, smem,
+                  inType, outType, inverse, ctx->stream);
+  CU(cudaGetLastError());
+  hoff += (bytes + 255) & ~(size_t)255;
+  return WL_OK;
+}
+
+int pb_dtype(int dt) {  // data type as the reference stores it
+  if (dt == WL_U8) return kPbUint8;
+  if (dt == WL_F32) return kPbFloat32;
+  return kPbInt32;  // I32 and U16 (16-bit data travels as INT32)
+}
+
+wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevice,
+                        wl_result *outs, float *coefOut = nullptr, size_t coefCap = 0,
+                        int *storedSize = nullptr) {
+  if (n <= 0) return fail(ctx, WL_EINVAL, "empty batch");
+  CU(cudaSetDevice(ctx->device));
+  std::vector<Plan> plans(n);
+  long long coefTotal = 0, chunkTotal = 0, inBytes = 0, wordsTotal = 0;
+  int tableTotal = 0, maxS = 2;
+  bool anyLog = false, anyLloyd = false;
+  for (int i = 0; i < n; i++) {
+    const wl_cubelet &it = items[i];
+    Plan &pl = plans[i];
+    TRY(check_params(ctx, it.params));
+    if (!it.data) return fail(ctx, WL_EINVAL, "cubelet %d: null data", i);
+    if (dtype_size(it.dtype) == 0) return fail(ctx, WL_EINVAL, "cubelet %d: bad dtype %d", i, it.dtype);
+    pl.data = it.data;
+    pl.dtype = it.dtype;
+    pl.X = it.size[0]; pl.Y = it.size[1]; pl.Z = it.size[2];
+    if (pl.X < 1 || pl.Y < 1 || pl.Z < 1)
+      return fail(ctx, WL_EINVAL, "cubelet %d: empty size %dx%dx%d", i, pl.X, pl.Y, pl.Z);
+    pl.p = it.params;
+    // setWaveletSteps (test_compress_common.cc:362-374)
+    int m;
+    m = ceil_log2(pl.X); pl.sx = (pl.p.steps[0] < 0 || pl.p.steps[0] > m) ? m : pl.p.steps[0];
+    m = ceil_log2(pl.Y); pl.sy = (pl.p.steps[1] < 0 || pl.p.steps[1] > m) ? m : pl.p.steps[1];
+    m = ceil_log2(pl.Z); pl.sz = (pl.p.steps[2] < 0 || pl.p.steps[2] > m) ? m : pl.p.steps[2];
+    pl.Xp = padded_length(pl.X, pl.sx);
+    pl.Yp = padded_length(pl.Y, pl.sy);
+    pl.Zp = padded_length(pl.Z, pl.sz);
+    pl.identity = pl.sx == 0 && pl.sy == 0 && pl.sz == 0;
+    if (pl.Xp > kMaxAxis || pl.Yp > kMaxAxis || pl.Zp > kMaxAxis)
+      return fail(ctx, WL_EINVAL, "cubelet %d: padded axis length above %d", i, kMaxAxis);
+    pl.n = (long long)pl.Xp * pl.Yp * pl.Zp;
+    if (pl.n > 0x7fffffffLL) return fail(ctx, WL_EINVAL, "cubelet %d too large", i);
+    pl.inOff = inBytes;
+    inBytes += ((long long)pl.X * pl.Y * pl.Z * dtype_size(pl.dtype) + 255) & ~255LL;
+    pl.coefOff = coefTotal;
+    coefTotal += (pl.n + 63) & ~63LL;
+    pl.chunkBase = chunkTotal;
+    pl.nChunks = (int)((pl.n + kChunk - 1) / kChunk);
+    chunkTotal += pl.nChunks;
+    // Huffman output bound: < log2(symbols)+1 bits per token plus 3 per dup token
+    pl.wordsCap = pl.n / 2 + 64;
+    wordsTotal += pl.wordsCap;
+    pl.tableOff = tableTotal;
+    tableTotal += ((2 * pl.p.bin_count + 2) + 63) & ~63;
+    maxS = std::max(maxS, pl.p.bin_count + 1);
+    if (pl.p.quant_alg == WL_LOG) anyLog = true;
+    if (pl.p.quant_alg == WL_LLOYD) anyLloyd = true;
+  }
+
+  // ---- workspace ----
+  TRY(ensure(ctx, ctx->coef, coefTotal * 4));
+  TRY(ensure(ctx, ctx->coef2, coefTotal * 4));
+  TRY(ensure(ctx, ctx->bins, coefTotal * 2));
+  TRY(ensure(ctx, ctx->state, n * sizeof(CubeletState)));
+  TRY(ensure(ctx, ctx->cub, n * sizeof(CubeletDev)));
+  TRY(ensure(ctx, ctx->chunkPrefix, n * sizeof(long long)));
+  TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
+  if (anyLloyd) TRY(ensure(ctx, ctx->lloydHist, (size_t)n * kLloydBins * 4));
+  TRY(ensure(ctx, ctx->qtable, (size_t)tableTotal * 4));
+  TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
+  TRY(ensure(ctx, ctx->hist, (size_t)n * kMaxSymbols * 8));
+  TRY(ensure(ctx, ctx->chunkRun, chunkTotal * sizeof(int4)));
+  TRY(ensure(ctx, ctx->chunkRunCtx, chunkTotal * 2 * sizeof(long long)));
+  TRY(ensure(ctx, ctx->chunkBits, chunkTotal * 8));
+  TRY(ensure(ctx, ctx->codes, (size_t)n * kMaxSymbols * 8));
+  TRY(ensure(ctx, ctx->codeLen, (size_t)n * kMaxSymbols));
+  TRY(ensure(ctx, ctx->decode, (size_t)n * 4 * kMaxSymbols * 4));
+  TRY(ensure(ctx, ctx->words, wordsTotal * 4));
+  TRY(ensure(ctx, ctx->logHdr, n * sizeof(int4)));
+  const size_t passBytes = (size_t)3 * n * (sizeof(PassDesc) + sizeof(int)) + 8 * 4096;
+  TRY(ensure(ctx, ctx->passes, passBytes));
+  TRY(ensure_host(ctx, ctx->hPasses, passBytes));
+  TRY(ensure_host(ctx, ctx->hCub, n * sizeof(CubeletDev) + n * sizeof(long long)));
+  TRY(ensure_host(ctx, ctx->hState, n * sizeof(CubeletState)));
+  TRY(ensure_host(ctx, ctx->hLogHdr, n * sizeof(int4)));
+  if (anyLog) TRY(ensure_host(ctx, ctx->hTab, (size_t)tableTotal * 4));
+
+  cudaStream_t s = ctx->stream;
+  CU(cudaEventRecord(ctx->ev[0], s));
+
+  // ---- inputs ----
+  std::vector<const void *> dIn(n);
+  if (onDevice) {
+    for (int i = 0; i < n; i++) dIn[i] = plans[i].data;
+  } else {
+    TRY(ensure(ctx, ctx->input, inBytes));
+    for (int i = 0; i < n; i++) {
+      const Plan &pl = plans[i];
+      char *dst = P<char>(ctx->input) + pl.inOff;
+      CU(cudaMemcpyAsync(dst, pl.data, (size_t)pl.X * pl.Y * pl.Z * dtype_size(pl.dtype),
+                         cudaMemcpyHostToDevice, s));
+      dIn[i] = dst;
+    }
+  }
+
+  // ---- descriptors ----
+  CubeletDev *hc = H<CubeletDev>(ctx->hCub);
+  long long *hp = reinterpret_cast<long long *>(hc + n);
+  for (int i = 0; i < n; i++) {
+    const Plan &pl = plans[i];
+    CubeletDev &c = hc[i];
+    memset(&c, 0, sizeof c);
+    c.n = pl.n;
+    c.coefOff = pl.coefOff;
+    c.chunkBase = pl.chunkBase;
+    c.wordsOff = 0;
+    c.wordsCap = pl.wordsCap;
+    c.nChunks = pl.nChunks;
+    c.binCount = pl.p.bin_count;
+    c.quantAlg = pl.p.quant_alg;
+    c.compressZeros = pl.p.compress_zeros ? 1 : 0;
+    c.frac = pl.p.threshold_fraction;
+    c.lloydIters = pl.p.lloyd_iters > 0 ? pl.p.lloyd_iters : 20;
+    c.tableOff = pl.tableOff;
+    hp[i] = pl.chunkBase;
+  }
+  CU(cudaMemcpyAsync(ctx->cub.p, hc, n * sizeof(CubeletDev), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->chunkPrefix.p, hp, n * sizeof(long long), cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(ctx->state.p, 0, n * sizeof(CubeletState), s));
+  CU(cudaMemsetAsync(ctx->selHist.p, 0, (size_t)n * kSelectBins * 4, s));
+  CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)n * kMaxSymbols * 8, s));
+  if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
+
+  DevBatch b;
+  memset(&b, 0, sizeof b);
+  b.n = n;
+  b.cub = P<CubeletDev>(ctx->cub);
+  b.state = P<CubeletState>(ctx->state);
+  b.coef = P<float>(ctx->coef);
+  b.coef2 = P<float>(ctx->coef2);
+  b.bins = P<uint16_t>(ctx->bins);
+  b.selHist = P<unsigned>(ctx->selHist);
+  b.lloydHist = P<float>(ctx->lloydHist);
+  b.qtable = P<float>(ctx->qtable);
+  b.dqtable = P<float>(ctx->dqtable);
+  b.hist = P<unsigned long long>(ctx->hist);
+  b.chunkRun = P<int4>(ctx->chunkRun);
+  b.chunkRunCtx = P<long long>(ctx->chunkRunCtx);
+  b.chunkBits = P<unsigned long long>(ctx->chunkBits);
+  b.codes = P<unsigned long long>(ctx->codes);
+  b.codeLen = P<uint8_t>(ctx->codeLen);
+  b.decode = P<int>(ctx->decode);
+  b.words = P<uint32_t>(ctx->words);
+  b.chunkPrefix = P<long long>(ctx->chunkPrefix);
+  b.logHdr = P<int4>(ctx->logHdr);
+  b.totalChunks = chunkTotal;
+
+  // ---- transform ----
+  std::vector<PassDesc> xs[5], ys, zs;
+  for (int i = 0; i < n; i++)
+    forward_passes(plans[i], dIn[i], b.coef, b.coef2, xs, ys, zs);
+  size_t hoff = 0;
+  for (int dt = 1; dt <= 4; dt++) TRY(run_group(ctx, xs[dt], hoff, dt, WL_F32, false));
+  TRY(run_group(ctx, ys, hoff, WL_F32, WL_F32, false));
+  TRY(run_group(ctx, zs, hoff, WL_F32, WL_F32, false));
+  CU(cudaEventRecord(ctx->ev[1], s));
+  if (coefOut) {  // transform only: hand back the coefficients of cubelet 0
+    const Plan &pl = plans[0];
+    if ((size_t)pl.n > coefCap) return fail(ctx, WL_EINVAL, "coefficient buffer too small");
+    CU(cudaMemcpyAsync(coefOut, b.coef + pl.coefOff, (size_t)pl.n * 4, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    if (pl.identity) { storedSize[0] = pl.Xp; storedSize[1] = pl.Yp; storedSize[2] = pl.Zp; }
+    else { storedSize[0] = pl.Zp; storedSize[1] = pl.Xp; storedSize[2] = pl.Yp; }
+    return WL_OK;
+  }
+
+  // ---- threshold ----
+  launch_select(b, b.coef, s);
+  CU(cudaGetLastError());
+
+  // ---- log quantizer tables (host logf) ----
+  if (anyLog) {
+    CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
+                       cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    const CubeletState *hs = H<CubeletState>(ctx->hState);
+    float *tab = H<float>(ctx->hTab);
+    int4 *lh = H<int4>(ctx->hLogHdr);
+    for (int i = 0; i < n; i++) {
+      lh[i] = make_int4(0, 0, 0, 0);
+      if (plans[i].p.quant_alg != WL_LOG) continue;
+      LogTable t;
+      log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
+      if (t.nPos + t.nNeg > kMaxBins)
+        return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)", i);
+      lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
+      std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
+    }
+    CU(cudaMemcpyAsync(ctx->qtable.p, tab, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(ctx->logHdr.p, lh, n * sizeof(int4), cudaMemcpyHostToDevice, s));
+  }
+  CU(cudaEventRecord(ctx->ev[2], s));
+
+  // ---- quantize + count ----
+  launch_quant_params(b, s);
+  if (anyLloyd) launch_lloyd(b, b.coef, s);
+  launch_quantize(b, b.coef, s);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(ctx->ev[3], s));
+
+  // ---- Huffman ----
+  launch_huffman_build(b, maxS, s);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(ctx->ev[4], s));
+  launch_encode(b, s);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(ctx->ev[5], s));
+
+  // ---- results ----
+  CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  const CubeletState *hs = H<CubeletState>(ctx->hState);
+  long long totalWords = 0;
+  size_t decodeInts = 0;
+  for (int i = 0; i < n; i++) {
+    if (hs[i].error)
+      return fail(ctx, WL_EINVAL, "cubelet %d: device error %d (code too long or output overflow)",
+                  i, hs[i].error);
+    totalWords += hs[i].nWords;
+    decodeInts += hs[i].nDecode;
+  }
+  TRY(ensure_host(ctx, ctx->hWords, (size_t)totalWords * 4));
+  TRY(ensure_host(ctx, ctx->hDecode, decodeInts * 4 + (size_t)n * 2 * kMaxBins * 4));
+  if (totalWords)
+    CU(cudaMemcpyAsync(ctx->hWords.p, b.words, (size_t)totalWords * 4, cudaMemcpyDeviceToHost, s));
+  int *hd = H<int>(ctx->hDecode);
+  size_t doff = 0;
+  std::vector<size_t> decOff(n), cbOff(n, 0);
+  for (int i = 0; i < n; i++) {
+    decOff[i] = doff;
+    if (hs[i].nDecode)
+      CU(cudaMemcpyAsync(hd + doff, b.decode + (size_t)i * 4 * kMaxSymbols,
+                         (size_t)hs[i].nDecode * 4, cudaMemcpyDeviceToHost, s));
+    doff += hs[i].nDecode;
+  }
+  for (int i = 0; i < n; i++) {
+    if (plans[i].p.quant_alg != WL_LLOYD) continue;
+    cbOff[i] = doff;
+    CU(cudaMemcpyAsync(hd + doff, b.qtable + plans[i].tableOff, (size_t)hs[i].nBounds * 4,
+                       cudaMemcpyDeviceToHost, s));
+    doff += hs[i].nBounds;
+    CU(cudaMemcpyAsync(hd + doff, b.dqtable + (size_t)i * kMaxBins, (size_t)hs[i].nValues * 4,
+                       cudaMemcpyDeviceToHost, s));
+    doff += hs[i].nValues;
+  }
+  CU(cudaEventRecord(ctx->ev[6], s));
+  CU(cudaStreamSynchronize(s));
+
+  float t[6];
+  cudaEventElapsedTime(&t[0], ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&t[1], ctx->ev[1], ctx->ev[2]);
+  cudaEventElapsedTime(&t[2], ctx->ev[2], ctx->ev[3]);
+  cudaEventElapsedTime(&t[3], ctx->ev[3], ctx->ev[4]);
+  cudaEventElapsedTime(&t[4], ctx->ev[4], ctx->ev[5]);
+  cudaEventElapsedTime(&t[5], ctx->ev[0], ctx->ev[6]);
+  memcpy(ctx->timings, t, sizeof t);
+
+  const uint32_t *hw = H<uint32_t>(ctx->hWords);
+  for (int i = 0; i < n; i++) {
+    const Plan &pl = plans[i];
+    const CubeletState &st = hs[i];
+    wl_result &r = outs[i];
+    memset(&r, 0, sizeof r);
+    if (pl.identity) { r.size[0] = pl.Xp; r.size[1] = pl.Yp; r.size[2] = pl.Zp; }
+    else { r.size[0] = pl.Zp; r.size[1] = pl.Xp; r.size[2] = pl.Yp; }
+    r.original_size[0] = pl.X; r.original_size[1] = pl.Y; r.original_size[2] = pl.Z;
+    r.original_dtype = pl.dtype;
+    r.steps[0] = pl.sx; r.steps[1] = pl.sy; r.steps[2] = pl.sz;
+    r.wavelet = pl.p.wavelet;
+    r.quant_alg = pl.p.quant_alg;
+    r.bin_count = pl.p.bin_count;
+    r.threshold_fraction = pl.p.threshold_fraction;
+    r.threshold_value = st.threshold;
+    r.max_value = st.maxAbs;
+    r.min_coef = st.minVal;
+    r.max_coef = st.maxVal;
+    r.zero_bin = st.zeroBin;
+    r.dup_value = st.dupValue;
+    r.dup_key = st.dupValue >= 0 ? pl.p.bin_count : -1;
+    r.longest_code = st.longest;
+    r.n_words = st.nWords;
+    r.words = (uint32_t *)malloc((size_t)std::max(1, st.nWords) * 4);
+    memcpy(r.words, hw + st.wordsBase, (size_t)st.nWords * 4);
+    r.n_decode = st.nDecode;
+    r.decode = (int32_t *)malloc((size_t)std::max(1, st.nDecode) * 4);
+    memcpy(r.decode, hd + decOff[i], (size_t)st.nDecode * 4);
+    if (pl.p.quant_alg == WL_LLOYD) {
+      r.n_boundaries = st.nBounds;
+      r.n_values = st.nValues;
+      r.boundaries = (float *)malloc((size_t)std::max(1, st.nBounds) * 4);
+      r.values = (float *)malloc((size_t)std::max(1, st.nValues) * 4);
+      memcpy(r.boundaries, hd + cbOff[i], (size_t)st.nBounds * 4);
+      memcpy(r.values, hd + cbOff[i] + st.nBounds, (size_t)st.nValues * 4);
+    }
+  }
+  return WL_OK;
+}
+
+// ---- decompression -----------------------------------------------------------
+// Table walk of HuffmanDecoder::decodeFromStream (huffman.h:96-131) on the
+// host.  A one-node table codes its symbol with zero bits.
+wl_status huffman_decode_host(wl_ctx *ctx, const wl_result *r, long long n, int *out) {
+  const uint32_t *w = r->words;
+  const long long total = (long long)r->n_words * 32;
+  const int *t = r->decode;
+  const int nt = r->n_decode;
+  if (nt < 2) return fail(ctx, WL_EFORMAT, "empty Huffman decode table");
+  if (r->dup_key >= 0 && (r->dup_value < 0 || r->dup_value >= r->bin_count))
+    return fail(ctx, WL_EFORMAT, "zero-run value out of range");
+  long long pos = 0, i = 0;
+  auto bit = [&](long long p) -> unsigned {
+    return p < total ? (w[p >> 5] >> (p & 31)) & 1u : 0u;
+  };
+  auto emit_run = [&](unsigned e) {
+    long long L = 1LL << (e + 3);
+    while (L-- > 0 && i < n) out[i++] = r->dup_value;
+  };
+  if (nt == 2 && t[0] == 0) {
+    if (t[1] != r->dup_key) { for (; i < n; i++) out[i] = t[1]; return WL_OK; }
+    while (i < n && pos + 3 <= total) {
+      unsigned e = bit(pos) | (bit(pos + 1) << 1) | (bit(pos + 2) << 2);
+      pos += 3;
+      emit_run(e);
+    }
+  } else {
+    while (i < n && pos < total) {
+      int node = 0;
+      while (true) {
+        const int nx = t[node + (int)bit(pos++)] * 2;
+        if (nx < 0 || nx + 1 >= nt) return fail(ctx, WL_EFORMAT, "corrupt Huffman stream");
+        node = nx;
+        if (t[node] == 0) break;
+      }
+      const int v = t[node + 1];
+      if (v == r->dup_key && r->dup_key >= 0) {
+        unsigned e = bit(pos) | (bit(pos + 1) << 1) | (bit(pos + 2) << 2);
+        pos += 3;
+        emit_run(e);
+      } else {
+        if (v < 0 || v >= r->bin_count) return fail(ctx, WL_EFORMAT, "symbol out of range");
+        out[i++] = v;
+      }
+    }
+  }
+  if (i != n) return fail(ctx, WL_EFORMAT, "stream holds %lld of %lld values", i, n);
+  return WL_OK;
+}
+
+}  // namespace
+
+// dequantize kernel launcher lives in dwt.cu
+namespace wl {
+void launch_dequant(const int *bins, const float *table, float *out, long long n, cudaStream_t s);
+}
+
+namespace {
+
+// Inverse transform of the coefficients already in ctx->coef (stored order)
+// into out (original size, outType), then synchronize.
+wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int wavelet,
+                       const int original_size[3], int outType, void *out, int outOnDevice) {
+  cudaStream_t s = ctx->stream;
+  const bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
+  const int Xp = identity ? size[0] : size[1];
+  const int Yp = identity ? size[1] : size[2];
+  const int Zp = identity ? size[2] : size[0];
+  const int X = original_size[0], Y = original_size[1], Z = original_size[2];
+  const size_t outBytes = (size_t)X * Y * Z * dtype_size(outType);
+  if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, outBytes));
+  TRY(ensure(ctx, ctx->passes, 8 * 4096));
+  TRY(ensure_host(ctx, ctx->hPasses, 8 * 4096));
+  void *dst = outOnDevice ? out : ctx->outbuf.p;
+  const int big = 0x7fffffff;
+  float *c1 = P<float>(ctx->coef), *c2 = P<float>(ctx->coef2);
+  size_t hoff = 0;
+  auto mk = [&]() { PassDesc d; memset(&d, 0, sizeof d); d.cropL = d.cropB = d.cropA = big;
+                    d.clampL = d.clampB = d.clampA = big; d.wavelet = wavelet; d.exact = 0; return d; };
+  const bool exactCdf = false;
+  if (!identity) {
+    // inverse z pass: z-x-y -> y-z-x
+    PassDesc a = mk();
+    a.in = c1; a.inSA = Zp; a.inSB = (long long)Xp * Zp;
+    a.L = Zp; a.B = Yp; a.rows = Xp * Yp;
+    a.out = c2; a.outSA = (long long)Yp * Zp; a.outSB = 1; a.outSC = Yp;
+    a.steps = steps[2];
+    a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
+    TRY(run_group(ctx, {a}, hoff, WL_F32, WL_F32, true));
+    // inverse y pass: y-z-x -> x-y-z
+    PassDesc bq = mk();
+    bq.in = c2; bq.inSA = Yp; bq.inSB = (long long)Zp * Yp;
+    bq.L = Yp; bq.B = Xp; bq.rows = Zp * Xp;
+    bq.out = c1; bq.outSA = (long long)Xp * Yp; bq.outSB = 1; bq.outSC = Xp;
+    bq.steps = steps[1];
+    bq.T = dwt_tile_rows(bq.L, exactCdf); bq.tiles = (bq.rows + bq.T - 1) / bq.T;
+    TRY(run_group(ctx, {bq}, hoff, WL_F32, WL_F32, true));
+  }
+  // inverse x pass + crop + dtype
+  PassDesc x = mk();
+  x.in = c1; x.inSA = (long long)Yp * Xp; x.inSB = Xp;
+  x.L = Xp; x.B = Yp; x.rows = Yp * Zp;
+  x.out = dst; x.outSA = (long long)X * Y; x.outSB = X; x.outSC = 1;
+  x.cropL = X; x.cropB = Y; x.cropA = Z;
+  x.steps = identity ? 0 : steps[0];
+  x.T = dwt_tile_rows(x.L, exactCdf); x.tiles = (x.rows + x.T - 1) / x.T;
+  TRY(run_group(ctx, {x}, hoff, WL_F32, outType, true));
+  if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return WL_OK;
+}
+
+wl_status check_sizes(wl_ctx *ctx, const int size[3], const int steps[3], const int orig[3],
+                      long long &n) {
+  const bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
+  const int Xp = identity ? size[0] : size[1];
+  const int Yp = identity ? size[1] : size[2];
+  const int Zp = identity ? size[2] : size[0];
+  for (int a = 0; a < 3; a++)
+    if (steps[a] < 0 || steps[a] > 30) return fail(ctx, WL_EFORMAT, "bad step count");
+  if (orig[0] < 1 || orig[1] < 1 || orig[2] < 1 || orig[0] > Xp || orig[1] > Yp || orig[2] > Zp)
+    return fail(ctx, WL_EFORMAT, "inconsistent sizes");
+  if (Xp % (1 << steps[0]) || Yp % (1 << steps[1]) || Zp % (1 << steps[2]))
+    return fail(ctx, WL_EFORMAT, "size not padded for the step counts");
+  n = (long long)Xp * Yp * Zp;
+  return WL_OK;
+}
+
+wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *out, int outOnDevice) {
+  CU(cudaSetDevice(ctx->device));
+  if (!r || !out) return fail(ctx, WL_EINVAL, "null argument");
+  if (dtype_size(outType) == 0) return fail(ctx, WL_EINVAL, "bad output dtype %d", outType);
+  long long n;
+  TRY(check_sizes(ctx, r->size, r->steps, r->original_size, n));
+  if (r->size[0] > kMaxAxis || r->size[1] > kMaxAxis || r->size[2] > kMaxAxis)
+    return fail(ctx, WL_EINVAL, "axis length above %d", kMaxAxis);
+  if (r->bin_count < 2 || r->bin_count > kMaxBins) return fail(ctx, WL_EFORMAT, "bad bin count");
+  std::vector<int> bins((size_t)n);
+  TRY(huffman_decode_host(ctx, r, n, bins.data()));
+  std::vector<float> dq(r->bin_count);
+  if (r->quant_alg == WL_LLOYD && (!r->values || r->n_values != r->bin_count))
+    return fail(ctx, WL_EFORMAT, "codebook values missing");
+  dequant_values(r->quant_alg, r->bin_count, r->threshold_value, r->max_value, r->values, dq.data());
+  const long long padded = (n + 63) & ~63LL;
+  TRY(ensure(ctx, ctx->coef, padded * 4));
+  TRY(ensure(ctx, ctx->coef2, padded * 4));
+  TRY(ensure(ctx, ctx->bins, padded * 4));  // int bins for the dequant kernel
+  TRY(ensure(ctx, ctx->dqtable, (size_t)kMaxBins * 4));
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemcpyAsync(ctx->bins.p, bins.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->dqtable.p, dq.data(), dq.size() * 4, cudaMemcpyHostToDevice, s));
+  launch_dequant(P<int>(ctx->bins), P<float>(ctx->dqtable), P<float>(ctx->coef), n, s);
+  CU(cudaGetLastError());
+  return inverse_impl(ctx, r->size, r->steps, r->wavelet, r->original_size, outType, out,
+                      outOnDevice);
+}
+
+wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
+  m.width = r->size[0]; m.height = r->size[1]; m.depth = r->size[2];
+  m.data_type = kPbInt32;
+  m.compressed = true;
+  m.steps[0] = r->steps[0]; m.steps[1] = r->steps[1]; m.steps[2] = r->steps[2];
+  m.wavelet = r->wavelet;
+  m.threshold_fraction = r->threshold_fraction;
+  m.threshold_value = r->threshold_value;
+  m.bin_count = r->bin_count;
+  m.pb_quant_alg = r->quant_alg == WL_UNIFORM ? kPbUniform : r->quant_alg == WL_LOG ? kPbLog : kPbLloyd;
+  m.quant_max_value = r->max_value;
+  if (r->quant_alg == WL_LLOYD) {
+    m.boundaries.assign(r->boundaries, r->boundaries + r->n_boundaries);
+    m.values.assign(r->values, r->values + r->n_values);
+  }
+  m.decode.assign(r->decode, r->decode + r->n_decode);
+  m.original_size[0] = r->original_size[0];
+  m.original_size[1] = r->original_size[1];
+  m.original_size[2] = r->original_size[2];
+  m.original_data_type = pb_dtype(r->original_dtype);
+  m.dup_key = r->dup_key;
+  m.dup_value = r->dup_value;
+  return WL_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+extern "C" {
+
+void wl_params_default(wl_params *p) {
+  p->steps[0] = p->steps[1] = p->steps[2] = -1;
+  p->wavelet = WL_CDF97;
+  p->threshold_fraction = 0.5f;
+  p->bin_count = 256;
+  p->quant_alg = WL_LOG;
+  p->compress_zeros = 1;
+  p->lloyd_iters = 20;
+  p->exact_transform = 0;
+}
+
+void wl_result_free(wl_result *r) {
+  if (!r) return;
+  free(r->words);
+  free(r->decode);
+  free(r->boundaries);
+  free(r->values);
+  memset(r, 0, sizeof *r);
+}
+
+wl_status wl_init(int device, wl_ctx **out) {
+  if (!out) return WL_EINVAL;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return WL_ECUDA;
+  }
+  if (device < 0 || device >= count) return WL_EINVAL;
+  wl_ctx *ctx = new wl_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return WL_ECUDA;
+  }
+  for (auto &e : ctx->ev) cudaEventCreate(&e);
+  *out = ctx;
+  return WL_OK;
+}
+
+void wl_destroy(wl_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->state, &ctx->cub,
+                   &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->hist,
+                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix,
+                   &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
+                   &ctx->logHdr, &ctx->outbuf};
+  for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
+  HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses, &ctx->hCub,
+                    &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals};
+  for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
+  for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *wl_last_error(const wl_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+wl_status wl_compress_cubelet(wl_ctx *ctx, const void *data, int dtype, const int size[3],
+                              int onDevice, const wl_params *params, wl_result *out) {
+  if (!ctx || !data || !size || !params || !out) return fail(ctx, WL_EINVAL, "null argument");
+  wl_cubelet it;
+  it.data = data;
+  it.dtype = dtype;
+  it.size[0] = size[0]; it.size[1] = size[1]; it.size[2] = size[2];
+  it.params = *params;
+  return compress_impl(ctx, &it, 1, onDevice, out);
+}
+
+wl_status wl_compress_batch(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevice,
+                            wl_result *outs) {
+  if (!ctx || !items || !outs) return fail(ctx, WL_EINVAL, "null argument");
+  return compress_impl(ctx, items, n, onDevice, outs);
+}
+
+wl_status wl_decompress_cubelet(wl_ctx *ctx, const wl_result *in, int outType, void *out,
+                                int outOnDevice) {
+  if (!ctx) return WL_EINVAL;
+  return decompress_impl(ctx, in, outType, out, outOnDevice);
+}
+
+wl_status wl_encode_cube(const wl_result *r, int footer, uint8_t **buf, size_t *len) {
+  if (!r || !buf || !len) return WL_EINVAL;
+  CubeMeta m;
+  result_to_meta(r, m);
+  std::string words((const char *)r->words, (size_t)r->n_words * 4);
+  std::string f = encode_file({m}, {&words}, footer != 0);
+  *buf = (uint8_t *)malloc(f.size());
+  if (!*buf) return WL_ENOMEM;
+  memcpy(*buf, f.data(), f.size());
+  *len = f.size();
+  return WL_OK;
+}
+
+void wl_free(void *p) { free(p); }
+
+wl_status wl_compress_file(wl_ctx *ctx, const char *inPath, const char *outPath,
+                           const wl_params *params) {
+  if (!ctx || !inPath || !outPath || !params) return fail(ctx, WL_EINVAL, "null argument");
+  std::string buf, err;
+  if (!read_whole_file(inPath, buf)) return fail(ctx, WL_EIO, "cannot read %s", inPath);
+  std::vector<CubeMeta> metas;
+  std::vector<std::string> datas;
+  if (!decode_file(buf, metas, datas, err)) return fail(ctx, WL_EFORMAT, "%s: %s", inPath, err.c_str());
+  // first uncompressed cubelet (readData, test_compress_common.cc:296-302)
+  for (size_t i = 0; i < metas.size(); i++) {
+    const CubeMeta &m = metas[i];
+    if (m.compressed) continue;
+    int dt = m.data_type == kPbUint8 ? WL_U8 : m.data_type == kPbInt32 ? WL_I32
+             : m.data_type == kPbFloat32 ? WL_F32 : 0;
+    if (!dt) return fail(ctx, WL_EFORMAT, "unknown data type %d", m.data_type);
+    const size_t need = (size_t)m.width * m.height * m.depth * dtype_size(dt);
+    if (datas[i].size() < need) return fail(ctx, WL_EFORMAT, "cubelet data truncated");
+    int size[3] = {m.width, m.height, m.depth};
+    wl_result r;
+    TRY(wl_compress_cubelet(ctx, datas[i].data(), dt, size, 0, params, &r));
+    CubeMeta om;
+    result_to_meta(&r, om);
+    std::string words((const char *)r.words, (size_t)r.n_words * 4);
+    wl_result_free(&r);
+    // the reference closes the compressed file without a footer
+    // (test_compress_cpu.cc:174-175)
+    if (!write_whole_file(outPath, encode_file({om}, {&words}, false)))
+      return fail(ctx, WL_EIO, "cannot write %s", outPath);
+    return WL_OK;
+  }
+  return fail(ctx, WL_EFORMAT, "No uncompressed cubelets in the input data.");
+}
+
+wl_status wl_decompress_file(wl_ctx *ctx, const char *inPath, const char *outPath) {
+  if (!ctx || !inPath || !outPath) return fail(ctx, WL_EINVAL, "null argument");
+  std::string buf, err;
+  if (!read_whole_file(inPath, buf)) return fail(ctx, WL_EIO, "cannot read %s", inPath);
+  std::vector<CubeMeta> metas;
+  std::vector<std::string> datas;
+  if (!decode_file(buf, metas, datas, err)) return fail(ctx, WL_EFORMAT, "%s: %s", inPath, err.c_str());
+  // first compressed INT32 cubelet (readQuantData, test_compress_common.cc:850-862)
+  for (size_t i = 0; i < metas.size(); i++) {
+    CubeMeta &m = metas[i];
+    if (!m.compressed || m.data_type != kPbInt32) continue;
+    wl_result r;
+    memset(&r, 0, sizeof r);
+    r.size[0] = m.width; r.size[1] = m.height; r.size[2] = m.depth;
+    r.original_size[0] = m.original_size[0];
+    r.original_size[1] = m.original_size[1];
+    r.original_size[2] = m.original_size[2];
+    int odt = m.original_data_type == kPbUint8 ? WL_U8
+              : m.original_data_type == kPbInt32 ? WL_I32 : WL_F32;
+    r.original_dtype = odt;
+    r.steps[0] = m.steps[0]; r.steps[1] = m.steps[1]; r.steps[2] = m.steps[2];
+    r.wavelet = m.wavelet;
+    r.quant_alg = m.pb_quant_alg == kPbUniform ? WL_UNIFORM : m.pb_quant_alg == kPbLog ? WL_LOG : WL_LLOYD;
+    r.bin_count = m.bin_count;
+    r.threshold_fraction = m.threshold_fraction;
+    r.threshold_value = m.threshold_value;
+    r.max_value = m.quant_max_value;
+    r.dup_key = m.dup_key;
+    r.dup_value = m.dup_value;
+    r.n_words = (int)(datas[i].size() / 4);
+    r.words = (uint32_t *)const_cast<char *>(datas[i].data());
+    r.n_decode = (int)m.decode.size();
+    r.decode = m.decode.data();
+    r.n_values = (int)m.values.size();
+    r.values = m.values.data();
+    if (r.original_size[0] == 0) {
+      return fail(ctx, WL_EFORMAT, "compressed cubelet lacks its original size");
+    }
+    const size_t n = (size_t)r.original_size[0] * r.original_size[1] * r.original_size[2];
+    std::string out(n * dtype_size(odt), '\0');
+    TRY(decompress_impl(ctx, &r, odt, &out[0], 0));
+    CubeMeta om;
+    om.width = r.original_size[0]; om.height = r.original_size[1]; om.depth = r.original_size[2];
+    om.data_type = pb_dtype(odt);
+    if (!write_whole_file(outPath, encode_file({om}, {&out}, true)))
+      return fail(ctx, WL_EIO, "cannot write %s", outPath);
+    return WL_OK;
+  }
+  return fail(ctx, WL_EFORMAT, "No compressed cubelet found");
+}
+
+wl_status wl_forward_transform(wl_ctx *ctx, const void *data, int dtype, const int size[3],
+                               const wl_params *params, float *coeffs, size_t cap,
+                               int stored[3]) {
+  if (!ctx || !data || !size || !params || !coeffs || !stored)
+    return fail(ctx, WL_EINVAL, "null argument");
+  wl_cubelet it;
+  it.data = data;
+  it.dtype = dtype;
+  it.size[0] = size[0]; it.size[1] = size[1]; it.size[2] = size[2];
+  it.params = *params;
+  wl_result dummy;
+  return compress_impl(ctx, &it, 1, 0, &dummy, coeffs, cap, stored);
+}
+
+wl_status wl_inverse_transform(wl_ctx *ctx, const float *coeffs, const int stored[3],
+                               const int steps[3], int wavelet, const int orig[3],
+                               int outType, void *out) {
+  if (!ctx || !coeffs || !stored || !steps || !orig || !out)
+    return fail(ctx, WL_EINVAL, "null argument");
+  CU(cudaSetDevice(ctx->device));
+  if (dtype_size(outType) == 0) return fail(ctx, WL_EINVAL, "bad output dtype %d", outType);
+  if (wavelet != WL_HAAR && wavelet != WL_CDF97) return fail(ctx, WL_EINVAL, "unknown wavelet");
+  long long n;
+  TRY(check_sizes(ctx, stored, steps, orig, n));
+  if (stored[0] > kMaxAxis || stored[1] > kMaxAxis || stored[2] > kMaxAxis)
+    return fail(ctx, WL_EINVAL, "axis length above %d", kMaxAxis);
+  TRY(ensure(ctx, ctx->coef, n * 4 + 256));
+  TRY(ensure(ctx, ctx->coef2, n * 4 + 256));
+  CU(cudaMemcpyAsync(ctx->coef.p, coeffs, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  return inverse_impl(ctx, stored, steps, wavelet, orig, outType, out, 0);
+}
+
+wl_status wl_last_timings(const wl_ctx *ctx, float out[6]) {
+  if (!ctx || !out) return WL_EINVAL;
+  memcpy(out, ctx->timings, sizeof ctx->timings);
+  return WL_OK;
+}
+
+void *wl_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void wl_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
+wl_status wl_sync(wl_ctx *ctx) {
+  if (!ctx) return WL_EINVAL;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, WL_ECUDA, "%s", cudaGetErrorString(e));
+  return WL_OK;
+}
+
+}  // extern "C"

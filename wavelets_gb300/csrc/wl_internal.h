@@ -1,0 +1,143 @@
+// Internal declarations shared by the libwlgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "wlgpu.h"
+
+namespace wl {
+
+constexpr int kMaxBins = 4096;          // bins per cubelet (kernel tables)
+constexpr int kMaxSymbols = kMaxBins + 1;
+constexpr int kChunk = 4096;            // elements per quantize/encode chunk
+constexpr int kChunkThreads = 256;
+constexpr int kSelectBins = 4096;       // radix-select digit histogram
+constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
+constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
+constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
+
+// One pass of the separable transform over one cubelet, as seen by the
+// row kernel.  Rows are flattened r = b + B*a; row (a,b) of the input starts
+// at in + a*inSA + b*inSB (contiguous along c); element (a,b,c) of the
+// output goes to out + a*outSA + b*outSB + c*outSC.
+struct PassDesc {
+  const void *in;
+  void *out;
+  long long inSA, inSB;
+  long long outSA, outSB, outSC;
+  int L;          // row length (padded)
+  int B;          // rows per 'a'
+  int rows;       // total rows (A*B)
+  int T;          // rows per tile (power of two)
+  int tiles;
+  int steps;
+  int wavelet;    // WL_HAAR / WL_CDF97
+  int exact;      // reference float order (filter bank) instead of lifting
+  int clampL, clampB, clampA;  // forward load: source sizes (REPEAT padding)
+  int cropL, cropB, cropA;     // inverse store: destination sizes (crop)
+};
+
+// Per-cubelet state written by the kernels and read back by the host.
+struct CubeletState {
+  // select
+  unsigned minOrd, maxOrd;       // order-preserving encodings of min/max
+  unsigned absMax, absMax2;      // bits of the two largest |c|
+  unsigned prefix;               // radix-select prefix of the threshold bits
+  unsigned long long rank;       // remaining rank inside the prefix bucket
+  float threshold;
+  float minVal, maxVal, maxAbs, maxAbs2;
+  // quantizer
+  int zeroBin;
+  int dupValue;                  // -1 when zero runs are off
+  float negScale, negOffset, posScale, posOffset;  // uniform
+  // quantizer tables: Lloyd boundary/value counts; log table layout
+  int nBounds, nValues;
+  int lowBin, highNeg, nPos, nNeg;
+  // Huffman
+  unsigned long long totalBits;
+  long long wordsBase;           // word offset of this cubelet in the packed output
+  int nWords;
+  int longest;
+  int nDecode;
+  int nLeaves;
+  int error;                     // nonzero: kernel-side failure code
+  int pad_;
+};
+
+// Everything a kernel needs about one cubelet of a batch.
+struct CubeletDev {
+  long long n;            // padded element count
+  long long coefOff;      // float offset of the coefficients
+  long long chunkBase;    // first global chunk index
+  long long wordsOff;     // word offset of the Huffman output
+  long long wordsCap;     // capacity in words
+  int nChunks;
+  int binCount;
+  int quantAlg;
+  int compressZeros;
+  float frac;
+  int lloydIters;
+  int tableOff;           // offset into per-cubelet quantizer tables (floats)
+  int nTable;             // entries in the table (log: boundaries; lloyd: boundaries)
+  int pad_;
+};
+
+// Device workspace for one batch.
+struct DevBatch {
+  int n;                          // cubelets
+  CubeletDev *cub;                // [n]
+  CubeletState *state;            // [n]
+  float *coef;                    // coefficients (ping)
+  float *coef2;                   // second buffer (pong)
+  uint16_t *bins;                 // quantized bins
+  unsigned *selHist;              // [n][kSelectBins]
+  float *lloydHist;               // [n][kLloydBins][2] (count, sum)
+  float *qtable;                  // quantizer tables
+  float *dqtable;                 // dequant values [n][binCount]
+  unsigned long long *hist;       // [n][kMaxSymbols] Huffman counts
+  int4 *chunkRun;                 // per chunk: lead, trail, allZero, pad
+  long long *chunkRunCtx;         // per chunk: start of incoming run, end of outgoing run (2 each)
+  unsigned long long *chunkBits;  // per chunk bit count / offset
+  unsigned long long *codes;      // [n][kMaxSymbols] code bits
+  uint8_t *codeLen;               // [n][kMaxSymbols]
+  int *decode;                    // [n][4*kMaxSymbols]
+  uint32_t *words;                // Huffman output
+  long long *chunkPrefix;         // [n+1] chunk prefix (== cub[i].chunkBase)
+  int4 *logHdr;                   // [n] log table layout from the host
+  long long totalChunks;
+};
+
+// launchers (dwt.cu)
+void launch_dwt_pass(const PassDesc *d_passes, const int *d_tilePrefix,
+                     int nPasses, int totalTiles, int smemBytes, int inType,
+                     int outType, bool inverse, cudaStream_t s);
+int dwt_tile_rows(int L, bool exact);
+int dwt_smem_bytes(int L, int T, bool exact);
+
+// launchers (select.cu)
+void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
+
+// launchers (quant.cu)
+void launch_quant_params(DevBatch &b, cudaStream_t s);
+void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s);
+void launch_quantize(DevBatch &b, const float *coef, cudaStream_t s);
+
+// launchers (huffman.cu)
+void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);
+void launch_encode(DevBatch &b, cudaStream_t s);
+
+// host-side exact log-quantizer tables (quant_host.cpp)
+struct LogTable {
+  std::vector<float> bounds;   // see quant_host.cpp for the layout
+  int lowBin, highNeg, nPos, nNeg;
+  float negScale, negOffset, posScale, posOffset;
+};
+void log_quant_table(int binCount, float threshold, float maxVal, LogTable &t);
+void dequant_values(int quantAlg, int binCount, float threshold, float maxVal,
+                    const float *codebookValues, float *out);
+
+}  // namespace wl

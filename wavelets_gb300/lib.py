@@ -1,0 +1,396 @@
+"""Python binding of libwlgpu's C ABI (include/wlgpu.h) through ctypes.
+
+Arrays follow the reference's cube layout: a numpy array of shape
+(depth, height, width) holds a cubelet whose x (width) index is fastest,
+i.e. size = (X, Y, Z) = (shape[2], shape[1], shape[0]).
+
+The compute path is the CUDA library only: if ``libwlgpu.so`` is missing or
+no GPU is visible, these calls raise -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import params as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libwlgpu.so")
+
+WL_OK, WL_EINVAL, WL_ENOMEM, WL_ETIMEOUT, WL_EFORMAT, WL_ECUDA, WL_EIO = range(7)
+WL_U8, WL_I32, WL_F32, WL_U16 = 1, 2, 3, 4
+STATUS_NAMES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ETIMEOUT", 4: "EFORMAT",
+                5: "ECUDA", 6: "EIO"}
+
+NP_TO_WL = {np.dtype(np.uint8): WL_U8, np.dtype(np.int32): WL_I32,
+            np.dtype(np.float32): WL_F32, np.dtype(np.uint16): WL_U16}
+WL_TO_NP = {v: k for k, v in NP_TO_WL.items()}
+
+
+class WlParams(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int * 3), ("wavelet", ctypes.c_int),
+                ("threshold_fraction", ctypes.c_float), ("bin_count", ctypes.c_int),
+                ("quant_alg", ctypes.c_int), ("compress_zeros", ctypes.c_int),
+                ("lloyd_iters", ctypes.c_int), ("exact_transform", ctypes.c_int)]
+
+
+class WlResult(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_int * 3), ("original_size", ctypes.c_int * 3),
+                ("original_dtype", ctypes.c_int), ("steps", ctypes.c_int * 3),
+                ("wavelet", ctypes.c_int), ("quant_alg", ctypes.c_int),
+                ("bin_count", ctypes.c_int), ("threshold_fraction", ctypes.c_float),
+                ("threshold_value", ctypes.c_float), ("max_value", ctypes.c_float),
+                ("min_coef", ctypes.c_float), ("max_coef", ctypes.c_float),
+                ("zero_bin", ctypes.c_int), ("dup_key", ctypes.c_int),
+                ("dup_value", ctypes.c_int), ("longest_code", ctypes.c_int),
+                ("n_words", ctypes.c_int), ("words", ctypes.POINTER(ctypes.c_uint32)),
+                ("n_decode", ctypes.c_int), ("decode", ctypes.POINTER(ctypes.c_int32)),
+                ("n_boundaries", ctypes.c_int), ("n_values", ctypes.c_int),
+                ("boundaries", ctypes.POINTER(ctypes.c_float)),
+                ("values", ctypes.POINTER(ctypes.c_float))]
+
+
+class WlCubelet(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int),
+                ("size", ctypes.c_int * 3), ("params", WlParams)]
+
+
+EXPORTS = {
+    "wl_params_default": (None, [ctypes.POINTER(WlParams)]),
+    "wl_result_free": (None, [ctypes.POINTER(WlResult)]),
+    "wl_init": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "wl_destroy": (None, [ctypes.c_void_p]),
+    "wl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "wl_compress_cubelet": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                           ctypes.POINTER(WlParams), ctypes.POINTER(WlResult)]),
+    "wl_compress_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlCubelet), ctypes.c_int,
+                                         ctypes.c_int, ctypes.POINTER(WlResult)]),
+    "wl_decompress_cubelet": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlResult),
+                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
+    "wl_compress_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                        ctypes.POINTER(WlParams)]),
+    "wl_decompress_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "wl_encode_cube": (ctypes.c_int, [ctypes.POINTER(WlResult), ctypes.c_int,
+                                      ctypes.POINTER(ctypes.POINTER(ctypes.c_uint8)),
+                                      ctypes.POINTER(ctypes.c_size_t)]),
+    "wl_free": (None, [ctypes.c_void_p]),
+    "wl_last_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "wl_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "wl_forward_transform": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(WlParams),
+                                            ctypes.c_void_p, ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_int)]),
+    "wl_inverse_transform": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.c_int, ctypes.c_void_p]),
+    "wl_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "wl_host_free": (None, [ctypes.c_void_p]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libwlgpu.so (built by wavelets_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libwlgpu.so not built ({path}); run wavelets_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class WlError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def make_params(p: Optional[P.Params] = None) -> WlParams:
+    p = p or P.Params()
+    w = WlParams()
+    w.steps[:] = [int(s) for s in p.steps]
+    w.wavelet = int(p.wavelet)
+    w.threshold_fraction = float(p.threshold_fraction)
+    w.bin_count = int(p.bin_count)
+    w.quant_alg = int(p.quant_alg)
+    w.compress_zeros = 1 if p.compress_zeros else 0
+    w.lloyd_iters = int(p.lloyd_iters)
+    w.exact_transform = 1 if p.exact_transform else 0
+    return w
+
+
+@dataclasses.dataclass
+class Compressed:
+    """A compressed cubelet (copy of a wl_result)."""
+    size: tuple              # stored (rotated) width, height, depth
+    original_size: tuple     # X, Y, Z
+    original_dtype: int
+    steps: tuple
+    wavelet: int
+    quant_alg: int
+    bin_count: int
+    threshold_fraction: float
+    threshold_value: float
+    max_value: float
+    min_coef: float
+    max_coef: float
+    zero_bin: int
+    dup_key: int
+    dup_value: int
+    longest_code: int
+    words: np.ndarray
+    decode: np.ndarray
+    boundaries: np.ndarray
+    values: np.ndarray
+
+    @classmethod
+    def from_struct(cls, r: WlResult) -> "Compressed":
+        def arr(ptr, n, dt):
+            if n <= 0 or not ptr:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt, copy=True)
+        return cls(tuple(r.size), tuple(r.original_size), r.original_dtype, tuple(r.steps),
+                   r.wavelet, r.quant_alg, r.bin_count, r.threshold_fraction,
+                   r.threshold_value, r.max_value, r.min_coef, r.max_coef, r.zero_bin,
+                   r.dup_key, r.dup_value, r.longest_code,
+                   arr(r.words, r.n_words, np.uint32), arr(r.decode, r.n_decode, np.int32),
+                   arr(r.boundaries, r.n_boundaries, np.float32),
+                   arr(r.values, r.n_values, np.float32))
+
+    def to_struct(self):
+        """A WlResult pointing into this object's arrays (keep self alive)."""
+        r = WlResult()
+        r.size[:] = self.size
+        r.original_size[:] = self.original_size
+        r.original_dtype = self.original_dtype
+        r.steps[:] = self.steps
+        r.wavelet, r.quant_alg, r.bin_count = self.wavelet, self.quant_alg, self.bin_count
+        r.threshold_fraction = self.threshold_fraction
+        r.threshold_value = self.threshold_value
+        r.max_value = self.max_value
+        r.min_coef, r.max_coef = self.min_coef, self.max_coef
+        r.zero_bin, r.dup_key, r.dup_value = self.zero_bin, self.dup_key, self.dup_value
+        r.longest_code = self.longest_code
+        self._keep = [np.ascontiguousarray(self.words, np.uint32),
+                      np.ascontiguousarray(self.decode, np.int32),
+                      np.ascontiguousarray(self.boundaries, np.float32),
+                      np.ascontiguousarray(self.values, np.float32)]
+        w, d, b, v = self._keep
+        r.n_words = w.size
+        r.words = w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        r.n_decode = d.size
+        r.decode = d.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        r.n_boundaries = b.size
+        r.boundaries = b.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        r.n_values = v.size
+        r.values = v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        return r
+
+    @property
+    def compressed_bytes(self) -> int:
+        return int(self.words.size) * 4
+
+
+def _size_of(arr: np.ndarray):
+    a = arr if arr.ndim == 3 else arr.reshape((1,) * (3 - arr.ndim) + arr.shape)
+    Z, Y, X = a.shape
+    return (X, Y, Z)
+
+
+class Context:
+    """A libwlgpu context (one CUDA stream + device workspace) on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        st = self.lib.wl_init(device, ctypes.byref(h))
+        if st != WL_OK:
+            raise WlError(st, f"wl_init(device={device}) failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != WL_OK:
+            raise WlError(st, self.lib.wl_last_error(self.h).decode())
+
+    def compress(self, arr, params: Optional[P.Params] = None, ptr: Optional[int] = None,
+                 dtype: Optional[int] = None, size=None) -> Compressed:
+        """Compress one cubelet given as a numpy array, or as a raw pointer
+        (host or device: set ``ptr`` plus ``dtype``/``size`` and pass
+        ``arr=None``; device pointers use compress_device)."""
+        return self._compress(arr, params, ptr, dtype, size, on_device=False)
+
+    def compress_device(self, ptr: int, dtype: int, size, params=None) -> Compressed:
+        return self._compress(None, params, ptr, dtype, size, on_device=True)
+
+    def _compress(self, arr, params, ptr, dtype, size, on_device):
+        if arr is not None:
+            a = np.ascontiguousarray(arr)
+            dtype = NP_TO_WL[a.dtype]
+            size = _size_of(a)
+            ptr = a.ctypes.data
+        sz = (ctypes.c_int * 3)(*size)
+        res = WlResult()
+        st = self.lib.wl_compress_cubelet(self.h, ctypes.c_void_p(ptr), dtype, sz,
+                                          1 if on_device else 0, ctypes.byref(make_params(params)),
+                                          ctypes.byref(res))
+        self._check(st)
+        out = Compressed.from_struct(res)
+        self.lib.wl_result_free(ctypes.byref(res))
+        return out
+
+    def compress_batch(self, items: Sequence, params=None, on_device: bool = False,
+                       raw: bool = False) -> List[Compressed]:
+        """items: list of numpy arrays, or (array, Params) pairs, or, with
+        on_device/raw, (ptr, dtype, size, Params) tuples."""
+        n = len(items)
+        cubs = (WlCubelet * n)()
+        keep = []
+        for i, it in enumerate(items):
+            if raw or on_device:
+                ptr, dt, size, prm = it
+            else:
+                if isinstance(it, tuple):
+                    a, prm = it
+                else:
+                    a, prm = it, params
+                a = np.ascontiguousarray(a)
+                keep.append(a)
+                ptr, dt, size = a.ctypes.data, NP_TO_WL[a.dtype], _size_of(a)
+            cubs[i].data = ptr
+            cubs[i].dtype = dt
+            cubs[i].size[:] = size
+            cubs[i].params = make_params(prm if prm is not None else params)
+        outs = (WlResult * n)()
+        st = self.lib.wl_compress_batch(self.h, cubs, n, 1 if on_device else 0, outs)
+        self._check(st)
+        res = [Compressed.from_struct(outs[i]) for i in range(n)]
+        for i in range(n):
+            self.lib.wl_result_free(ctypes.byref(outs[i]))
+        return res
+
+    def decompress(self, c: Compressed, dtype=None) -> np.ndarray:
+        """Restore a cubelet; dtype defaults to the original."""
+        wl_dt = NP_TO_WL[np.dtype(dtype)] if dtype is not None else c.original_dtype
+        X, Y, Z = c.original_size
+        out = np.empty((Z, Y, X), WL_TO_NP[wl_dt])
+        r = c.to_struct()
+        st = self.lib.wl_decompress_cubelet(self.h, ctypes.byref(r), wl_dt,
+                                            ctypes.c_void_p(out.ctypes.data), 0)
+        self._check(st)
+        return out
+
+    def forward_transform(self, arr, params: Optional[P.Params] = None):
+        """Coefficients of the forward transform in the stored (rotated) order
+        and the stored size (width, height, depth)."""
+        a = np.ascontiguousarray(arr)
+        size = _size_of(a)
+        prm = params or P.Params()
+        steps = P.clamp_steps(prm.steps, size)
+        n = 1
+        for s, L in zip(steps, size):
+            n *= P.padded_length(L, s)
+        out = np.empty(n, np.float32)
+        stored = (ctypes.c_int * 3)()
+        st = self.lib.wl_forward_transform(self.h, ctypes.c_void_p(a.ctypes.data),
+                                           NP_TO_WL[a.dtype], (ctypes.c_int * 3)(*size),
+                                           ctypes.byref(make_params(prm)),
+                                           ctypes.c_void_p(out.ctypes.data), n, stored)
+        self._check(st)
+        return out, tuple(stored)
+
+    def inverse_transform(self, coeffs, stored_size, steps, wavelet, original_size,
+                          dtype=np.float32):
+        c = np.ascontiguousarray(coeffs, np.float32)
+        X, Y, Z = original_size
+        out = np.empty((Z, Y, X), dtype)
+        st = self.lib.wl_inverse_transform(self.h, ctypes.c_void_p(c.ctypes.data),
+                                           (ctypes.c_int * 3)(*stored_size),
+                                           (ctypes.c_int * 3)(*steps), int(wavelet),
+                                           (ctypes.c_int * 3)(*original_size),
+                                           NP_TO_WL[np.dtype(dtype)],
+                                           ctypes.c_void_p(out.ctypes.data))
+        self._check(st)
+        return out
+
+    def compress_file(self, inp: str, out: str, params: Optional[P.Params] = None):
+        self._check(self.lib.wl_compress_file(self.h, inp.encode(), out.encode(),
+                                              ctypes.byref(make_params(params))))
+
+    def decompress_file(self, inp: str, out: str):
+        self._check(self.lib.wl_decompress_file(self.h, inp.encode(), out.encode()))
+
+    def timings(self):
+        """Device time (ms) of the last compress: transform, select,
+        quantize+count, Huffman build, encode, total."""
+        t = (ctypes.c_float * 6)()
+        self._check(self.lib.wl_last_timings(self.h, t))
+        return list(t)
+
+    def sync(self):
+        self._check(self.lib.wl_sync(self.h))
+
+
+def encode_cube(c: Compressed, footer: bool = False) -> bytes:
+    """The .cube file bytes the reference would write for this cubelet."""
+    lib = load()
+    r = c.to_struct()
+    buf = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_size_t()
+    st = lib.wl_encode_cube(ctypes.byref(r), 1 if footer else 0, ctypes.byref(buf), ctypes.byref(n))
+    if st != WL_OK:
+        raise WlError(st, "wl_encode_cube failed")
+    data = ctypes.string_at(buf, n.value)
+    lib.wl_free(buf)
+    return data
+
+
+class PinnedBuffer:
+    """Page-locked host memory from wl_host_alloc, viewable as numpy."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load()
+        self.nbytes = nbytes
+        self.ptr = self.lib.wl_host_alloc(nbytes)
+        if not self.ptr:
+            raise MemoryError("wl_host_alloc failed")
+
+    def array(self, dtype, shape):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        assert n <= self.nbytes
+        buf = (ctypes.c_uint8 * n).from_address(self.ptr)
+        return np.frombuffer(buf, dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.lib.wl_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
