@@ -1,0 +1,421 @@
+#!/usr/bin/env python
+"""Benchmark of the cubelet compression path on GB300.
+
+Default workload (``--workload mixed``): 512 synthetic cubelets, every axis
+drawn from {16,32,48,64,96,128,256}, 50% uint8 / 30% uint16 / 20% float32,
+Haar or CDF 9/7 (half each) with floor(log2(min axis)) - 2 steps per axis,
+keep the top 10% (threshold fraction 0.9), Lloyd quantizer with 256 bins
+trained 20 iterations on each cubelet's histogram, Huffman with zero runs.
+One step = one batched compression of all 512 cubelets (wl_compress_batch).
+
+Printed JSON line (rank 0):
+  value       input GB/s of the batched path, inputs resident in HBM
+              (device time, CUDA events on the library's stream)
+  e2e         the same through the public API with pinned host inputs:
+              host->device copies and the device->host read of the
+              compressed streams inside the timed region (wall clock)
+  plain_value the same 512 cubelets compressed one cubelet per call
+  roofline    the dominant kernel group: its compulsory bytes / its time
+  pipeline_roofline  (input + compressed bytes) / whole-step device time
+  cpu_baseline the oracle (CPU restatement of the reference path) on a
+              bounded sample of the same cubelets, one host core
+
+``--impl reference`` times the reference algorithm on the host cores instead
+(the oracle port, all host threads, a bounded sample per step) and prints the
+same metric with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from wavelets_gb300 import params as P  # noqa: E402
+from wavelets_gb300 import synth  # noqa: E402
+
+METRIC = "input GB/s on 1 GB300, batched vs plain at equal PSNR; p50/p99 latency"
+UNIT = "GB/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ workloads
+def mixed_workload(seed, count):
+    """(arrays, params) for the mixed batch."""
+    items = []
+    for arr, wavelet in synth.mixed_batch(seed=seed, count=count):
+        steps = max(0, int(np.floor(np.log2(min(arr.shape)))) - 2)
+        p = P.Params(steps=(steps, steps, steps), wavelet=wavelet, threshold_fraction=0.9,
+                     bin_count=256, quant_alg=P.LLOYD, lloyd_iters=20)
+        items.append((arr, p))
+    return items
+
+
+def volume_workload(seed, count):
+    vol = synth.volume_f32(seed=seed)
+    p = P.Params(steps=(3, 3, 3), threshold_fraction=0.95, quant_alg=P.UNIFORM, bin_count=1024)
+    return [(vol, p)]
+
+
+def plain2d_workload(seed, count):
+    img = synth.plain_2d(seed=seed)
+    p = P.Params(steps=(11, 11, 0), threshold_fraction=0.9, quant_alg=P.LOG, bin_count=256)
+    return [(img, p)]
+
+
+WORKLOADS = {
+    "mixed": (mixed_workload, "512 mixed cubelets (axes 16..256, u8/u16/f32, Haar|CDF9/7, "
+                              "Lloyd 256, keep 10%)"),
+    "volume": (volume_workload, "256^3 float32, CDF9/7 3,3,3, keep 5%, uniform 1024"),
+    "plain2d": (plain2d_workload, "2048x2048 uint8, CDF9/7 11,11,0, keep 10%, log 256"),
+}
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def _cpu_compress_one(args):
+    arr, p = args
+    from oracle import oracle
+    qalg = {P.UNIFORM: oracle.UNIFORM, P.LOG: oracle.LOG, P.LLOYD: oracle.LLOYD}[p.quant_alg]
+    t = time.perf_counter()
+    oracle.compress_volume(arr, p.steps, p.wavelet, p.threshold_fraction, p.bin_count, qalg,
+                           p.compress_zeros, None)
+    return arr.nbytes, time.perf_counter() - t
+
+
+def _shuffled(items, seed=7):
+    order = np.random.default_rng(seed).permutation(len(items))
+    return [items[i] for i in order]
+
+
+def _timed_pool(sample, procs, budget_s):
+    """Compress cubelets of `sample` on `procs` spawned processes until the
+    budget runs out; returns (bytes of completed cubelets, elapsed, count).
+    Unfinished cubelets are abandoned (the pool is terminated)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    pool = ctx.Pool(procs)
+    try:
+        # start-up and library page-in on a tiny cubelet, not timed
+        warm = (np.zeros((8, 8, 8), np.uint8), P.Params(steps=(1, 1, 1)))
+        pool.map(_cpu_compress_one, [warm] * procs)
+        t0 = time.perf_counter()
+        done_b, n = 0, 0
+        it = pool.imap_unordered(_cpu_compress_one, sample, chunksize=1)
+        while True:
+            left = budget_s - (time.perf_counter() - t0)
+            if left <= 0:
+                break
+            try:
+                b, _ = it.next(timeout=left)
+            except StopIteration:
+                break
+            except mp.TimeoutError:
+                break
+            done_b += b
+            n += 1
+        elapsed = time.perf_counter() - t0
+    finally:
+        pool.terminate()
+        pool.join()
+    return done_b, elapsed, n
+
+
+def cpu_baseline(items, budget_s=12.0):
+    """Oracle port (the reference algorithm) on ONE host core, on the
+    cubelets in a seeded shuffled order until the time budget."""
+    b, t, n = _timed_pool(_shuffled(items), 1, budget_s)
+    return {"value": b / t / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} of {len(items)} cubelets ({b / 1e6:.1f} MB) completed in "
+                      f"{t:.1f} s, seeded shuffled order, single process; "
+                      "oracle/port CPU restatement of the reference path"}
+
+
+def run_reference(args, items, desc, rank, world):
+    """--impl reference: the reference algorithm on all host cores; each step
+    compresses cubelets (seeded shuffled order) for a bounded time."""
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sample = _shuffled(items)
+    budget = 10.0
+    for _ in range(min(args.warmup, 1)):
+        _timed_pool(sample, cores, 1.0)
+    vals, nbytes, ncub = [], 0, 0
+    for _ in range(args.steps):
+        b, t, n = _timed_pool(sample, cores, budget)
+        vals.append(b / t / 1e9)
+        nbytes += b
+        ncub += n
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": budget * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "cubelets": len(items)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{ncub} cubelets ({nbytes / 1e6:.1f} MB) completed over "
+                                       f"{args.steps} steps of {budget:.0f} s on {cores} "
+                                       "processes, seeded shuffled order; oracle/port "
+                                       "restatement of the reference CPU path"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS))
+    ap.add_argument("--cubelets", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    gen, desc = WORKLOADS[args.workload]
+    items = gen(20261205 + rank, args.cubelets)
+
+    if args.impl == "reference":
+        run_reference(args, items, desc, rank, world)
+        return
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # replicas: barrier + max only
+        dist.init_process_group("gloo")
+
+    from wavelets_gb300 import build
+    build.build()
+    from wavelets_gb300 import lib
+
+    ctx = lib.Context(local)
+    in_bytes = sum(a.nbytes for a, _ in items)
+    # device-resident inputs (256-byte aligned) and pinned host copies
+    offs, off = [], 0
+    for a, _ in items:
+        offs.append(off)
+        off += (a.nbytes + 255) // 256 * 256
+    dev = lib.DeviceBuffer(off)
+    pin = lib.PinnedBuffer(off)
+    for (a, _), o in zip(items, offs):
+        dev.upload(a, o)
+        pin.array(np.uint8, (off,))[o:o + a.nbytes] = a.view(np.uint8).ravel()
+    dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                 for (a, p), o in zip(items, offs)]
+    host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                  for (a, p), o in zip(items, offs)]
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def gmax(x):
+        if not dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident batched path (value) ----
+    for _ in range(args.warmup):
+        ref_out = ctx.compress_batch(dev_items, on_device=True)
+    ctx.set_profiling(True)
+    kt = {k: 0.0 for k in ctx.KERNEL_GROUPS}
+    dev_ms = []
+    launches = 0
+    barrier()
+    ctx.sync()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            out = ctx.compress_batch(dev_items, on_device=True)
+            dev_ms.append(ctx.timings()[5])
+            for k, v in ctx.kernel_timings().items():
+                kt[k] += v
+            launches += ctx.launch_count()
+    ctx.sync()
+    barrier()
+    ctx.set_profiling(False)
+    step_ms = gmax(statistics.mean(dev_ms))
+    comp_bytes = sum(c.compressed_bytes for c in out)
+    same = all(np.array_equal(a.words, b.words) for a, b in zip(out, ref_out))
+    value = world * in_bytes / (step_ms / 1e3) / 1e9
+
+    # ---- end to end through the public API (pinned host inputs) ----
+    barrier()
+    e2e_t = []
+    for _ in range(max(1, args.steps)):
+        t = time.perf_counter()
+        outh = ctx.compress_batch(host_items, raw=True)
+        e2e_t.append(time.perf_counter() - t)
+    barrier()
+    e2e_ms = gmax(statistics.mean(e2e_t) * 1e3)
+    same_h = all(np.array_equal(a.words, b.words) for a, b in zip(outh, out))
+    d2h = sum(c.compressed_bytes + c.decode.nbytes + c.boundaries.nbytes + c.values.nbytes
+              for c in outh)
+
+    # ---- plain: one cubelet per call ----
+    plain = None
+    if not args.no_plain and len(items) > 1:
+        for it in dev_items[:8]:
+            ctx.compress_batch([it], on_device=True)
+        pt = []
+        single = []
+        for it in dev_items:
+            single.append(ctx.compress_batch([it], on_device=True)[0])
+            pt.append(ctx.timings()[5])
+        plain_ms = sum(pt)
+        plain = {"value": in_bytes / (plain_ms / 1e3) / 1e9, "ms_per_step": plain_ms,
+                 "identical_to_batched": all(np.array_equal(a.words, b.words)
+                                             for a, b in zip(single, out))}
+
+    # ---- PSNR on a sample (equal for batched and plain: identical streams) ----
+    psnrs = []
+    for (a, p), c in list(zip(items, out))[:: max(1, len(items) // 32)]:
+        back = ctx.decompress(c).astype(np.float64)
+        x = a.astype(np.float64)
+        peak = 255.0 if a.dtype == np.uint8 else (65535.0 if a.dtype == np.uint16
+                                                  else float(x.max() - x.min()))
+        mse = float(np.mean((back - x) ** 2))
+        psnrs.append(10 * np.log10(peak * peak / mse) if mse > 0 else 999.0)
+
+    # ---- roofline ----
+    hbm, peak_kind = peaks()
+    n_pad = 0
+    n_pad_z = 0
+    for a, p in items:
+        size = lib._size_of(a)
+        st = P.clamp_steps(p.steps, size)
+        n = 1
+        for s_, L in zip(st, size):
+            n *= P.padded_length(L, s_)
+        n_pad += n
+        if st[2] > 0:
+            n_pad_z += n
+    group_bytes = {  # compulsory HBM bytes of each kernel group per step
+        "dwt_x": in_bytes + 4 * n_pad, "dwt_y": 8 * n_pad, "dwt_z": 8 * n_pad_z,
+        "select": 3 * 4 * n_pad, "quantize": 4 * n_pad + 2 * n_pad,
+        "encode": 2 * 2 * n_pad + comp_bytes, "huffman_build": 0, "runs": 0,
+        "quant_setup": 0}
+    per_step = {k: v / args.steps for k, v in kt.items()}
+    dom = max(per_step, key=lambda k: per_step[k])
+    dom_gbs = group_bytes[dom] / (per_step[dom] / 1e3) / 1e9 if per_step[dom] > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": dom_gbs, "peak": hbm,
+                "unit": "GB/s", "frac": dom_gbs / hbm, "traffic": None,
+                "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": group_bytes[dom]}
+    pipe_gbs = (in_bytes + comp_bytes) / (step_ms / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(items)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "cubelets": len(items), "input_bytes": in_bytes,
+                       "padded_voxels": n_pad, "compressed_bytes": comp_bytes,
+                       "l2": "inputs larger than L2 (129 MB): no flush between steps",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain": plain,
+            "batched_vs_plain": (value / plain["value"]) if plain else None,
+            "psnr_db_mean": float(np.mean(psnrs)) if psnrs else None,
+            "psnr_sample": len(psnrs),
+            "deterministic": bool(same and same_h),
+            "e2e": {"value": world * in_bytes / (e2e_ms / 1e3) / 1e9, "unit": UNIT,
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h},
+            "roofline": roofline,
+            "pipeline_roofline": {"achieved": pipe_gbs, "peak": hbm, "unit": "GB/s",
+                                  "frac": pipe_gbs / hbm,
+                                  "bytes": "input + compressed output per step"},
+            "kernel_ms_per_step": per_step,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -166,6 +166,22 @@ wl_status wl_last_timings(const wl_ctx *ctx, float out[6]);
 /* Synchronize the context's stream. */
 wl_status wl_sync(wl_ctx *ctx);
 
+/* Device memory helpers for callers that keep inputs resident on the GPU. */
+void *wl_device_alloc(size_t bytes);
+void wl_device_free(void *p);
+wl_status wl_copy_to_device(void *dst, const void *src, size_t bytes);
+wl_status wl_copy_to_host(void *dst, const void *src, size_t bytes);
+
+/* Number of kernels the last compress/decompress call launched, and the
+ * device time (ms, CUDA events on the context's stream) of each kernel
+ * group: 0 dwt x pass, 1 dwt y pass, 2 dwt z pass, 3 select, 4 quantizer
+ * set-up + Lloyd, 5 quantize + count, 6 zero-run join, 7 Huffman build,
+ * 8 encode (count, scan, pack).  Per-group events are recorded only while
+ * profiling is on (wl_set_profiling); they add a little launch overhead. */
+int wl_last_launch_count(const wl_ctx *ctx);
+wl_status wl_set_profiling(wl_ctx *ctx, int on);
+wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
+
 /* Page-locked host memory for inputs and outputs of the host-pointer entry
  * points (copies from it overlap with device work). */
 void *wl_host_alloc(size_t bytes);

@@ -88,6 +88,10 @@ struct wl_ctx {
   HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals;
   cudaEvent_t ev[7] = {};
   float timings[6] = {0, 0, 0, 0, 0, 0};
+  bool profiling = false;
+  cudaEvent_t pev[10] = {};
+  float ktimes[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int launches = 0;
 };
 
 namespace {
@@ -148,6 +152,11 @@ wl_status ensure_host(wl_ctx *ctx, HostBuf &b, size_t bytes) {
   } while (0)
 
 template <class T> T *P(DevBuf &b) { return static_cast<T *>(b.p); }
+
+// kernel-group boundary for the optional per-group timings
+inline void mark(wl_ctx *ctx, int i) {
+  if (ctx->profiling) cudaEventRecord(ctx->pev[i], ctx->stream);
+}
 template <class T> T *H(HostBuf &b) { return static_cast<T *>(b.p); }
 
 wl_status check_params(wl_ctx *ctx, const wl_params &p) {
@@ -244,6 +253,7 @@ wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
   }
   tp[n] = tiles;
   CU(cudaMemcpyAsync(d, h, bytes - 64, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->launches++;
   launch_dwt_pass(reinterpret_cast<const PassDesc *>(d),
                   reinterpret_cast<const int *>(d + n * sizeof(PassDesc)), (int)n, tiles, smem,
                   inType, outType, inverse, ctx->stream);
@@ -408,13 +418,18 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.totalChunks = chunkTotal;
 
   // ---- transform ----
+  ctx->launches = 0;
   std::vector<PassDesc> xs[5], ys, zs;
   for (int i = 0; i < n; i++)
     forward_passes(plans[i], dIn[i], b.coef, b.coef2, xs, ys, zs);
   size_t hoff = 0;
+  mark(ctx, 0);
   for (int dt = 1; dt <= 4; dt++) TRY(run_group(ctx, xs[dt], hoff, dt, WL_F32, false));
+  mark(ctx, 1);
   TRY(run_group(ctx, ys, hoff, WL_F32, WL_F32, false));
+  mark(ctx, 2);
   TRY(run_group(ctx, zs, hoff, WL_F32, WL_F32, false));
+  mark(ctx, 3);
   CU(cudaEventRecord(ctx->ev[1], s));
   if (coefOut) {  // transform only: hand back the coefficients of cubelet 0
     const Plan &pl = plans[0];
@@ -428,7 +443,9 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- threshold ----
   launch_select(b, b.coef, s);
+  ctx->launches += 7;
   CU(cudaGetLastError());
+  mark(ctx, 4);
 
   // ---- log quantizer tables (host logf) ----
   if (anyLog) {
@@ -455,16 +472,26 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- quantize + count ----
   launch_quant_params(b, s);
-  if (anyLloyd) launch_lloyd(b, b.coef, s);
+  ctx->launches += 1;
+  if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 2; }
+  mark(ctx, 5);
   launch_quantize(b, b.coef, s);
+  mark(ctx, 6);
+  launch_runs(b, s);
+  ctx->launches += 2;
+  mark(ctx, 7);
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[3], s));
 
   // ---- Huffman ----
   launch_huffman_build(b, maxS, s);
+  ctx->launches += 1;
+  mark(ctx, 8);
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[4], s));
   launch_encode(b, s);
+  ctx->launches += 5;
+  mark(ctx, 9);
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[5], s));
 
@@ -517,6 +544,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   cudaEventElapsedTime(&t[4], ctx->ev[4], ctx->ev[5]);
   cudaEventElapsedTime(&t[5], ctx->ev[0], ctx->ev[6]);
   memcpy(ctx->timings, t, sizeof t);
+  if (ctx->profiling)
+    for (int g = 0; g < 9; g++) cudaEventElapsedTime(&ctx->ktimes[g], ctx->pev[g], ctx->pev[g + 1]);
 
   const uint32_t *hw = H<uint32_t>(ctx->hWords);
   for (int i = 0; i < n; i++) {
@@ -710,6 +739,7 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
   cudaStream_t s = ctx->stream;
   CU(cudaMemcpyAsync(ctx->bins.p, bins.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(ctx->dqtable.p, dq.data(), dq.size() * 4, cudaMemcpyHostToDevice, s));
+  ctx->launches = 1;
   launch_dequant(P<int>(ctx->bins), P<float>(ctx->dqtable), P<float>(ctx->coef), n, s);
   CU(cudaGetLastError());
   return inverse_impl(ctx, r->size, r->steps, r->wavelet, r->original_size, outType, out,
@@ -784,6 +814,7 @@ wl_status wl_init(int device, wl_ctx **out) {
     return WL_ECUDA;
   }
   for (auto &e : ctx->ev) cudaEventCreate(&e);
+  for (auto &e : ctx->pev) cudaEventCreate(&e);
   *out = ctx;
   return WL_OK;
 }
@@ -802,6 +833,7 @@ void wl_destroy(wl_ctx *ctx) {
                     &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals};
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
   for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+  for (auto &e : ctx->pev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -965,6 +997,41 @@ wl_status wl_inverse_transform(wl_ctx *ctx, const float *coeffs, const int store
 wl_status wl_last_timings(const wl_ctx *ctx, float out[6]) {
   if (!ctx || !out) return WL_EINVAL;
   memcpy(out, ctx->timings, sizeof ctx->timings);
+  return WL_OK;
+}
+
+void *wl_device_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void wl_device_free(void *p) {
+  if (p) cudaFree(p);
+}
+
+wl_status wl_copy_to_device(void *dst, const void *src, size_t bytes) {
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? WL_OK : WL_ECUDA;
+}
+
+wl_status wl_copy_to_host(void *dst, const void *src, size_t bytes) {
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? WL_OK : WL_ECUDA;
+}
+
+int wl_last_launch_count(const wl_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+wl_status wl_set_profiling(wl_ctx *ctx, int on) {
+  if (!ctx) return WL_EINVAL;
+  ctx->profiling = on != 0;
+  return WL_OK;
+}
+
+wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]) {
+  if (!ctx || !out) return WL_EINVAL;
+  memcpy(out, ctx->ktimes, sizeof ctx->ktimes);
   return WL_OK;
 }
 

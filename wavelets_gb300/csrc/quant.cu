@@ -583,7 +583,8 @@ void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
 
 void launch_quantize(DevBatch &b, const float *coef, cudaStream_t s) {
   quantize_kernel<<<(unsigned)b.totalChunks, kThreads, 0, s>>>(b, coef);
-  runs_kernel<<<b.n, 1024, 0, s>>>(b);
 }
+
+void launch_runs(DevBatch &b, cudaStream_t s) { runs_kernel<<<b.n, 1024, 0, s>>>(b); }
 
 }  // namespace wl

@@ -125,6 +125,7 @@ void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
 void launch_quant_params(DevBatch &b, cudaStream_t s);
 void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s);
 void launch_quantize(DevBatch &b, const float *coef, cudaStream_t s);
+void launch_runs(DevBatch &b, cudaStream_t s);
 
 // launchers (huffman.cu)
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);

@@ -89,6 +89,13 @@ EXPORTS = {
                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                             ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                             ctypes.c_int, ctypes.c_void_p]),
+    "wl_device_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "wl_device_free": (None, [ctypes.c_void_p]),
+    "wl_copy_to_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "wl_copy_to_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "wl_last_launch_count": (ctypes.c_int, [ctypes.c_void_p]),
+    "wl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "wl_kernel_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "wl_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "wl_host_free": (None, [ctypes.c_void_p]),
 }
@@ -350,6 +357,20 @@ class Context:
         self._check(self.lib.wl_last_timings(self.h, t))
         return list(t)
 
+    def launch_count(self) -> int:
+        return int(self.lib.wl_last_launch_count(self.h))
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.wl_set_profiling(self.h, 1 if on else 0))
+
+    KERNEL_GROUPS = ("dwt_x", "dwt_y", "dwt_z", "select", "quant_setup", "quantize",
+                     "runs", "huffman_build", "encode")
+
+    def kernel_timings(self):
+        t = (ctypes.c_float * 9)()
+        self._check(self.lib.wl_kernel_timings(self.h, t))
+        return dict(zip(self.KERNEL_GROUPS, list(t)))
+
     def sync(self):
         self._check(self.lib.wl_sync(self.h))
 
@@ -366,6 +387,36 @@ def encode_cube(c: Compressed, footer: bool = False) -> bytes:
     data = ctypes.string_at(buf, n.value)
     lib.wl_free(buf)
     return data
+
+
+class DeviceBuffer:
+    """Device memory from wl_device_alloc."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load()
+        self.nbytes = nbytes
+        self.ptr = self.lib.wl_device_alloc(nbytes)
+        if not self.ptr:
+            raise MemoryError("wl_device_alloc failed")
+
+    def upload(self, arr: np.ndarray, offset: int = 0):
+        a = np.ascontiguousarray(arr)
+        assert offset + a.nbytes <= self.nbytes
+        st = self.lib.wl_copy_to_device(ctypes.c_void_p(self.ptr + offset),
+                                        ctypes.c_void_p(a.ctypes.data), a.nbytes)
+        if st != WL_OK:
+            raise WlError(st, "upload failed")
+
+    def free(self):
+        if self.ptr:
+            self.lib.wl_device_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class PinnedBuffer:
