@@ -182,6 +182,32 @@ int wl_last_launch_count(const wl_ctx *ctx);
 wl_status wl_set_profiling(wl_ctx *ctx, int on);
 wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
 
+/* Threshold selection that allocates nothing.  This entry point has no
+ * counterpart in the reference.  It is for callers that may not call
+ * cudaMalloc: code running while a stream is being captured (allocation is
+ * illegal there), hosts that give the library a fixed memory budget or their
+ * own pool, and real-time loops that must not wait on the allocator.
+ *
+ * coeffs: n transform coefficients in device memory.  out: 5 floats in
+ * device memory, written on `stream` (a cudaStream_t; NULL = default
+ * stream): threshold (the k-th smallest |c|, k = (int)(fraction * n), 0
+ * replaced by 1e-16), smallest and largest coefficient (tracked like the
+ * reference, starting from FLT_MAX / FLT_MIN), largest and second largest |c|
+ * -- the same values wl_compress_cubelet reports for those coefficients.
+ * The call only enqueues work; it does not synchronize.
+ *
+ * Scratch lives in a static device array of about 272 KB that every GPU that
+ * loads this library keeps until the process exits.  n is limited to
+ * WL_NOALLOC_MAX_ELEMENTS (larger n returns WL_EINVAL).  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress) for
+ * that device, so make the first call on each device before any stream
+ * capture.  Every call shares the one array and clears what must start at
+ * zero; calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and must be serialized by the caller. */
+#define WL_NOALLOC_MAX_ELEMENTS (64LL * 1024 * 1024)
+wl_status wl_select_threshold_noalloc(const float *coeffs, long long n,
+                                      float fraction, void *stream, float *out);
+
 /* Page-locked host memory for inputs and outputs of the host-pointer entry
  * points (copies from it overlap with device work). */
 void *wl_host_alloc(size_t bytes);

@@ -1,0 +1,57 @@
+"""wl_select_threshold_noalloc: threshold selection with no device
+allocation, for callers that may not call cudaMalloc (stream capture, fixed
+memory budgets, real-time loops).  Its scratch is a static device array, so
+this test also checks that a second call right after the first (different
+data) starts from clean scratch.  Compared against wl_compress_cubelet on
+the same coefficients; the values are order statistics and extremes, so they
+must match exactly.  Named test_zz_* so pytest collects it last."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from wavelets_gb300 import lib, params as P, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_threshold_matches_compress():
+    from wavelets_gb300 import build
+    build.build()
+    L = lib.load()
+    ctx = lib.Context(0)
+    cases = [
+        (synth.volume_f32(21, (32, 48, 64), 20),
+         P.Params(steps=(3, 3, 3), threshold_fraction=0.95, quant_alg=P.UNIFORM, bin_count=1024)),
+        (synth.plain_2d(22, 512), P.Params(steps=(9, 9, 0), threshold_fraction=0.9)),
+    ]
+    dout = lib.DeviceBuffer(64)
+    try:
+        for arr, p in cases:  # two calls in a row on different data
+            comp = ctx.compress(arr, p)
+            coeffs, _ = ctx.forward_transform(arr, p)
+            dbuf = lib.DeviceBuffer(coeffs.nbytes)
+            dbuf.upload(coeffs)
+            st = L.wl_select_threshold_noalloc(ctypes.c_void_p(dbuf.ptr), coeffs.size,
+                                               ctypes.c_float(p.threshold_fraction), None,
+                                               ctypes.c_void_p(dout.ptr))
+            assert st == lib.WL_OK
+            ctx.sync()
+            got = np.zeros(5, np.float32)
+            assert L.wl_copy_to_host(ctypes.c_void_p(got.ctypes.data),
+                                     ctypes.c_void_p(dout.ptr), 20) == lib.WL_OK
+            assert got[0] == np.float32(comp.threshold_value)
+            assert got[1] == np.float32(comp.min_coef)
+            assert got[2] == np.float32(comp.max_coef)
+            assert got[3] == np.float32(comp.max_value)
+            dbuf.free()
+    finally:
+        dout.free()
+        ctx.close()
+
+
+def test_noalloc_rejects_oversize():
+    L = lib.load()
+    st = L.wl_select_threshold_noalloc(ctypes.c_void_p(1), (64 << 20) + 1, ctypes.c_float(0.5),
+                                       None, ctypes.c_void_p(1))
+    assert st == lib.WL_EINVAL

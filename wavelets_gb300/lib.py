@@ -96,6 +96,9 @@ EXPORTS = {
     "wl_last_launch_count": (ctypes.c_int, [ctypes.c_void_p]),
     "wl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "wl_kernel_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "wl_select_threshold_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong,
+                                                   ctypes.c_float, ctypes.c_void_p,
+                                                   ctypes.c_void_p]),
     "wl_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "wl_host_free": (None, [ctypes.c_void_p]),
 }
