@@ -92,133 +92,131 @@ __device__ __forceinline__ int band_to_pos(int q, int L, int S, int &lev) {
   return ((q - (L >> (t + 1))) << (t + 1)) + (1 << t);
 }
 
-// ---- forward levels -------------------------------------------------------
-__device__ void fwd_lifting(float *row, int L, int S, int lane) {
-  for (int lev = 0; lev < S; lev++) {
-    const int n = L >> lev, half = n >> 1, st = 1 << lev;
-    for (int i = lane; i < half; i += 32) {  // d += alpha (s_i + s_i+1)
-      float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
+// ---- one level of one row --------------------------------------------------
+// A level runs on the strided view row[j*st], j < n = 2*half.  The lanes of a
+// warp are split into groups of G lanes (G = 32, or the power of two >= half
+// when half < 32) so several short rows share a warp; `sub` is the lane's
+// index in its group and `ok` whether the group has a row.  Every lane of
+// the warp executes the same __syncwarp calls.
+
+__device__ __forceinline__ void fwd_lifting_level(float *row, int half, int st, int sub,
+                                                  int G, bool ok) {
+  if (ok)
+    for (int i = sub; i < half; i += G) {  // d += alpha (s_i + s_i+1)
+      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
       row[(2 * i + 1) * st] += kAlpha * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {  // s += beta (d_i-1 + d_i)
-      float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {  // s += beta (d_i-1 + d_i)
+      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
       row[(2 * i) * st] += kBeta * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
       row[(2 * i + 1) * st] += kGamma * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
       row[(2 * i) * st] += kDelta * (a + b);
     }
-    __syncwarp();
-  }
+  __syncwarp();
 }
 
-__device__ void fwd_haar(float *row, int L, int S, int lane) {
-  for (int lev = 0; lev < S; lev++) {
-    const int half = (L >> lev) >> 1, st = 1 << lev;
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * i) * st], b = row[(2 * i + 1) * st];
-      row[(2 * i + 1) * st] = __fmul_rn(__fsub_rn(a, b), kInvSqrt2);
-      row[(2 * i) * st] = __fmul_rn(__fadd_rn(a, b), kInvSqrt2);
-    }
-    __syncwarp();
-  }
-}
-
-// reference filter bank, reference operation order (dwt_cpu.cc:699-725)
-__device__ void fwd_cdf97_exact(float *row, float *tmp, int L, int S, int lane) {
-  for (int lev = 0; lev < S; lev++) {
-    const int n = L >> lev, half = n >> 1, st = 1 << lev;
-    for (int j = lane; j < n; j += 32) tmp[j] = row[j * st];
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      const int j = 2 * i;
-      float s = __fmul_rn(kL0, tmp[j]);
-      s = __fadd_rn(s, __fmul_rn(kL1, __fadd_rn(tmp[mirror(j + 1, n)], tmp[mirror(j - 1, n)])));
-      s = __fadd_rn(s, __fmul_rn(kL2, __fadd_rn(tmp[mirror(j + 2, n)], tmp[mirror(j - 2, n)])));
-      s = __fadd_rn(s, __fmul_rn(kL3, __fadd_rn(tmp[mirror(j + 3, n)], tmp[mirror(j - 3, n)])));
-      s = __fadd_rn(s, __fmul_rn(kL4, __fadd_rn(tmp[mirror(j + 4, n)], tmp[mirror(j - 4, n)])));
-      row[j * st] = s;
-      const int k = j + 1;
-      float d = __fmul_rn(kH0, tmp[k]);
-      d = __fadd_rn(d, __fmul_rn(kH1, __fadd_rn(tmp[mirror(k + 1, n)], tmp[mirror(k - 1, n)])));
-      d = __fadd_rn(d, __fmul_rn(kH2, __fadd_rn(tmp[mirror(k + 2, n)], tmp[mirror(k - 2, n)])));
-      d = __fadd_rn(d, __fmul_rn(kH3, __fadd_rn(tmp[mirror(k + 3, n)], tmp[mirror(k - 3, n)])));
-      row[k * st] = d;
-    }
-    __syncwarp();
-  }
-}
-
-// ---- inverse levels -------------------------------------------------------
-__device__ void inv_lifting(float *row, int L, int S, int lane) {
-  for (int lev = S - 1; lev >= 0; lev--) {
-    const int n = L >> lev, half = n >> 1, st = 1 << lev;
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
+__device__ __forceinline__ void inv_lifting_level(float *row, int half, int st, int sub,
+                                                  int G, bool ok) {
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
       row[(2 * i) * st] -= kDelta * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
       row[(2 * i + 1) * st] -= kGamma * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
       row[(2 * i) * st] -= kBeta * (a + b);
     }
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
       row[(2 * i + 1) * st] -= kAlpha * (a + b);
     }
-    __syncwarp();
-  }
+  __syncwarp();
 }
 
-// haar_inv_internal (dwt_cpu.cc:193-196)
-__device__ void inv_haar(float *row, int L, int S, int lane) {
-  for (int lev = S - 1; lev >= 0; lev--) {
-    const int half = (L >> lev) >> 1, st = 1 << lev;
-    for (int i = lane; i < half; i += 32) {
-      float s = row[(2 * i) * st], d = row[(2 * i + 1) * st];
-      row[(2 * i) * st] = __fmul_rn(kInvSqrt2, __fadd_rn(s, d));
-      row[(2 * i + 1) * st] = __fmul_rn(kInvSqrt2, __fsub_rn(s, d));
+// Haar butterflies (dwt_cpu.cc:159-162 forward, :193-196 inverse)
+__device__ __forceinline__ void haar_level(float *row, int half, int st, int sub, int G,
+                                           bool ok, bool inverse) {
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const float a = row[(2 * i) * st], b = row[(2 * i + 1) * st];
+      if (!inverse) {
+        row[(2 * i + 1) * st] = __fmul_rn(__fsub_rn(a, b), kInvSqrt2);
+        row[(2 * i) * st] = __fmul_rn(__fadd_rn(a, b), kInvSqrt2);
+      } else {
+        row[(2 * i) * st] = __fmul_rn(kInvSqrt2, __fadd_rn(a, b));
+        row[(2 * i + 1) * st] = __fmul_rn(kInvSqrt2, __fsub_rn(a, b));
+      }
     }
-    __syncwarp();
-  }
+  __syncwarp();
 }
 
-// cdf97_inverse_tmpl (dwt_cpu.cc:770-796), reference operation order
-__device__ void inv_cdf97_exact(float *row, float *tmp, int L, int S, int lane) {
-  for (int lev = S - 1; lev >= 0; lev--) {
-    const int n = L >> lev, half = n >> 1, st = 1 << lev;
-    for (int j = lane; j < n; j += 32) tmp[j] = row[j * st];
-    __syncwarp();
-    for (int i = lane; i < half; i += 32) {
-      const int j = 2 * i;
-      float s = __fmul_rn(tmp[j], kSL0);
-      s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 1, n)], tmp[mirror(j - 1, n)]), kSL1));
-      s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 2, n)], tmp[mirror(j - 2, n)]), kSL2));
-      s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 3, n)], tmp[mirror(j - 3, n)]), kSL3));
+// reference filter bank in the reference operation order: analysis
+// dwt_cpu.cc:699-725, synthesis :776-795
+__device__ __forceinline__ void exact_level(float *row, float *tmp, int half, int st, int sub,
+                                            int G, bool ok, bool inverse) {
+  const int n = 2 * half;
+  if (ok)
+    for (int j = sub; j < n; j += G) tmp[j] = row[j * st];
+  __syncwarp();
+  if (ok)
+    for (int i = sub; i < half; i += G) {
+      const int j = 2 * i, k = j + 1;
+      float s, d;
+      if (!inverse) {
+        s = __fmul_rn(kL0, tmp[j]);
+        s = __fadd_rn(s, __fmul_rn(kL1, __fadd_rn(tmp[mirror(j + 1, n)], tmp[mirror(j - 1, n)])));
+        s = __fadd_rn(s, __fmul_rn(kL2, __fadd_rn(tmp[mirror(j + 2, n)], tmp[mirror(j - 2, n)])));
+        s = __fadd_rn(s, __fmul_rn(kL3, __fadd_rn(tmp[mirror(j + 3, n)], tmp[mirror(j - 3, n)])));
+        s = __fadd_rn(s, __fmul_rn(kL4, __fadd_rn(tmp[mirror(j + 4, n)], tmp[mirror(j - 4, n)])));
+        d = __fmul_rn(kH0, tmp[k]);
+        d = __fadd_rn(d, __fmul_rn(kH1, __fadd_rn(tmp[mirror(k + 1, n)], tmp[mirror(k - 1, n)])));
+        d = __fadd_rn(d, __fmul_rn(kH2, __fadd_rn(tmp[mirror(k + 2, n)], tmp[mirror(k - 2, n)])));
+        d = __fadd_rn(d, __fmul_rn(kH3, __fadd_rn(tmp[mirror(k + 3, n)], tmp[mirror(k - 3, n)])));
+      } else {
+        s = __fmul_rn(tmp[j], kSL0);
+        s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 1, n)], tmp[mirror(j - 1, n)]), kSL1));
+        s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 2, n)], tmp[mirror(j - 2, n)]), kSL2));
+        s = __fadd_rn(s, __fmul_rn(__fadd_rn(tmp[mirror(j + 3, n)], tmp[mirror(j - 3, n)]), kSL3));
+        d = __fmul_rn(tmp[k], kSH0);
+        d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 1, n)], tmp[mirror(k - 1, n)]), kSH1));
+        d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 2, n)], tmp[mirror(k - 2, n)]), kSH2));
+        d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 3, n)], tmp[mirror(k - 3, n)]), kSH3));
+        d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 4, n)], tmp[mirror(k - 4, n)]), kSH4));
+      }
       row[j * st] = s;
-      const int k = j + 1;
-      float d = __fmul_rn(tmp[k], kSH0);
-      d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 1, n)], tmp[mirror(k - 1, n)]), kSH1));
-      d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 2, n)], tmp[mirror(k - 2, n)]), kSH2));
-      d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 3, n)], tmp[mirror(k - 3, n)]), kSH3));
-      d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 4, n)], tmp[mirror(k - 4, n)]), kSH4));
       row[k * st] = d;
     }
-    __syncwarp();
-  }
+  __syncwarp();
+}
+
+// lane group for rows of `len` elements handled `len`-wide
+__device__ __forceinline__ int group_width(int len) {
+  if (len >= 32) return 32;
+  int G = 1;
+  while (G < len) G <<= 1;
+  return G;
 }
 
 // per-level store scale of the lifting form: index t < S detail, t == S low
@@ -269,38 +267,45 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
 
   // ---- load --------------------------------------------------------------
   const InT *in = static_cast<const InT *>(d.in);
-  for (int rr = warp; rr < nr; rr += kWarps) {
-    const InT *src = in + rowIn[rr];
-    float *trow = tile + rr * pitch;
-    if (!INV) {
-      const int cl = d.clampL - 1;
-      for (int c = lane; c < L; c += 32) trow[c] = load_as_float(src + min(c, cl));
-    } else {
-      for (int q = lane; q < L; q += 32) {
-        int lev;
-        const int p = band_to_pos(q, L, S, lev);
-        const float v = load_as_float(src + q);
-        trow[p] = lifting ? v / scaleTab[lev] : v;
+  {
+    const int G = group_width(L), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
+    for (int rb = warp * rpi; rb < nr; rb += kWarps * rpi) {
+      const int rr = rb + rsub;
+      if (rr >= nr) continue;
+      const InT *src = in + rowIn[rr];
+      float *trow = tile + rr * pitch;
+      if (!INV) {
+        const int cl = d.clampL - 1;
+        for (int c = sub; c < L; c += G) trow[c] = load_as_float(src + min(c, cl));
+      } else {
+        for (int q = sub; q < L; q += G) {
+          int lev;
+          const int p = band_to_pos(q, L, S, lev);
+          const float v = load_as_float(src + q);
+          trow[p] = lifting ? v / scaleTab[lev] : v;
+        }
       }
     }
   }
   __syncthreads();
 
   // ---- levels ------------------------------------------------------------
-  for (int rr = warp; rr < nr; rr += kWarps) {
-    float *trow = tile + rr * pitch;
-    float *tmp = tmpb + rr * L;
-    if (!INV) {
-      if (d.wavelet == WL_HAAR) fwd_haar(trow, L, S, lane);
-      else if (d.exact) fwd_cdf97_exact(trow, tmp, L, S, lane);
-      else fwd_lifting(trow, L, S, lane);
-    } else {
-      if (d.wavelet == WL_HAAR) inv_haar(trow, L, S, lane);
-      else if (d.exact) inv_cdf97_exact(trow, tmp, L, S, lane);
-      else inv_lifting(trow, L, S, lane);
+  for (int it = 0; it < S; it++) {
+    const int lev = INV ? S - 1 - it : it;
+    const int half = (L >> lev) >> 1, st = 1 << lev;
+    const int G = group_width(half), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
+    for (int rb = warp * rpi; rb < nr; rb += kWarps * rpi) {
+      const int rr = rb + rsub;
+      const bool ok = rr < nr;
+      float *trow = tile + (ok ? rr : 0) * pitch;
+      float *tmp = tmpb + (ok ? rr : 0) * L;
+      if (d.wavelet == WL_HAAR) haar_level(trow, half, st, sub, G, ok, INV);
+      else if (d.exact) exact_level(trow, tmp, half, st, sub, G, ok, INV);
+      else if (!INV) fwd_lifting_level(trow, half, st, sub, G, ok);
+      else inv_lifting_level(trow, half, st, sub, G, ok);
     }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- store -------------------------------------------------------------
   OutT *out = static_cast<OutT *>(d.out);
@@ -324,10 +329,14 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       store_from_float(out + base + (long long)q * d.outSC, v);
     }
   } else {
-    for (int rr = warp; rr < nr; rr += kWarps) {
+    const int Lc = min(L, cropL);
+    const int G = group_width(Lc), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
+    for (int rb = warp * rpi; rb < nr; rb += kWarps * rpi) {
+      const int rr = rb + rsub;
+      if (rr >= nr) continue;
       const long long base = rowOut[rr];
       if (base < 0) continue;
-      for (int q = lane; q < min(L, cropL); q += 32) {
+      for (int q = sub; q < Lc; q += G) {
         float v;
         if (!INV) {
           int lev;

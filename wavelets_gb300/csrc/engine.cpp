@@ -82,7 +82,7 @@ struct wl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  DevBuf input, coef, coef2, bins, state, cub, selHist, lloydHist, qtable, dqtable,
+  DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, codes, codeLen, decode,
       words, passes, logHdr, outbuf;
   HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals;
@@ -275,7 +275,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   CU(cudaSetDevice(ctx->device));
   std::vector<Plan> plans(n);
   long long coefTotal = 0, chunkTotal = 0, inBytes = 0, wordsTotal = 0;
-  int tableTotal = 0, maxS = 2;
+  int tableTotal = 0, maxS = 2, maxTable = 0;
   bool anyLog = false, anyLloyd = false;
   for (int i = 0; i < n; i++) {
     const wl_cubelet &it = items[i];
@@ -315,6 +315,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     pl.tableOff = tableTotal;
     tableTotal += ((2 * pl.p.bin_count + 2) + 63) & ~63;
     maxS = std::max(maxS, pl.p.bin_count + 1);
+    if (pl.p.quant_alg == WL_LLOYD) maxTable = std::max(maxTable, pl.p.bin_count);
+    if (pl.p.quant_alg == WL_LOG) maxTable = std::max(maxTable, 2 * pl.p.bin_count);
     if (pl.p.quant_alg == WL_LOG) anyLog = true;
     if (pl.p.quant_alg == WL_LLOYD) anyLloyd = true;
   }
@@ -322,7 +324,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   // ---- workspace ----
   TRY(ensure(ctx, ctx->coef, coefTotal * 4));
   TRY(ensure(ctx, ctx->coef2, coefTotal * 4));
-  TRY(ensure(ctx, ctx->bins, coefTotal * 2));
+  TRY(ensure(ctx, ctx->bins, (coefTotal + (long long)n * kChunk) * 2));
+  TRY(ensure(ctx, ctx->tokCount, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->state, n * sizeof(CubeletState)));
   TRY(ensure(ctx, ctx->cub, n * sizeof(CubeletDev)));
   TRY(ensure(ctx, ctx->chunkPrefix, n * sizeof(long long)));
@@ -400,7 +403,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.state = P<CubeletState>(ctx->state);
   b.coef = P<float>(ctx->coef);
   b.coef2 = P<float>(ctx->coef2);
-  b.bins = P<uint16_t>(ctx->bins);
+  b.tok = P<uint16_t>(ctx->bins);
+  b.chunkTok = P<int>(ctx->tokCount);
   b.selHist = P<unsigned>(ctx->selHist);
   b.lloydHist = P<float>(ctx->lloydHist);
   b.qtable = P<float>(ctx->qtable);
@@ -460,7 +464,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       if (plans[i].p.quant_alg != WL_LOG) continue;
       LogTable t;
       log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
-      if (t.nPos + t.nNeg > kMaxBins)
+      if (t.nPos + t.nNeg > 2 * plans[i].p.bin_count)
         return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)", i);
       lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
       std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
@@ -475,7 +479,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   ctx->launches += 1;
   if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 2; }
   mark(ctx, 5);
-  launch_quantize(b, b.coef, s);
+  launch_quantize(b, b.coef, maxTable, s);
   mark(ctx, 6);
   launch_runs(b, s);
   ctx->launches += 2;
@@ -823,7 +827,8 @@ void wl_destroy(wl_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->state, &ctx->cub,
+  DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->tokCount,
+                   &ctx->state, &ctx->cub,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,

@@ -28,8 +28,6 @@ namespace wl {
 namespace {
 
 constexpr int kThreads = kChunkThreads;
-constexpr int kPer = kChunk / kThreads;
-constexpr int INF = 0x7fffffff;
 constexpr int kMaxCodeBits = 58;  // + 3 dup bits fits 61 bits -> at most 3 words
 
 __device__ __forceinline__ int find_cubelet(const long long *prefix, int n, long long c) {
@@ -232,128 +230,50 @@ __global__ void __launch_bounds__(1024) huffman_build_kernel(DevBatch b) {
 }
 
 // ---- tokens -----------------------------------------------------------------
-struct TokCtx {
-  const uint8_t *len;             // smem copy of code lengths
-  const unsigned long long *code; // smem copy of codes (may be null when counting)
-  int dupV, dupKey;
-  long long chunkStart;           // cubelet coordinate of chunk element 0
-  long long runIn, runOut;        // run entering / leaving the chunk
-};
+constexpr int kMaxEdgeTokens = 32;   // tokens of one run inside one chunk: <= 19
+constexpr int kMaxChunkTokens = kChunk + 2 * kMaxEdgeTokens;
 
-// Token of element at cubelet position P inside a zero-bin run [s, e).
-// Returns the token length (0 = element is covered by an earlier dup token);
-// bits receive the token bits when code != null.
-__device__ __forceinline__ int run_token(long long P, long long s, long long e, const TokCtx &t,
-                                         unsigned long long &bits) {
-  const long long o = P - s, L = e - s;
-  const long long q = L / 1024;
-  int dupE = -1;
-  if (o < q * 1024) {
-    if ((o & 1023) == 0) dupE = 7;
-    else return 0;
-  } else {
-    int r = (int)(L - q * 1024);
-    int oo = (int)(o - q * 1024);
-    int pos = 0;
-    while (r > 8) {
-      int p2 = 8, e2 = 0;
-      while ((p2 << 1) <= r) { p2 <<= 1; e2++; }
-      if (oo == pos) { dupE = e2; break; }
-      if (oo < pos + p2) return 0;
-      pos += p2;
-      r -= p2;
+// Build the ordered token list of a chunk in shared memory: the tokens of
+// the run entering the chunk, the chunk's stored tokens, the tokens of the
+// run leaving it.  Returns the count.  Collective (two barriers).
+__device__ int chunk_tokens(const DevBatch &b, long long chunk, const CubeletDev &cd,
+                            int dupV, uint16_t *list, int *sCount) {
+  const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
+  const int nInt = b.chunkTok[chunk];
+  const uint16_t *src = b.tok + cd.coefOff + cstart;
+  if (threadIdx.x == 0) {
+    int nPre = 0, nPost = 0;
+    uint16_t pre[kMaxEdgeTokens], post[kMaxEdgeTokens];
+    if (dupV >= 0) {
+      const int4 cr = b.chunkRun[chunk];  // lead, trail, allZero, len
+      const long long runIn = b.chunkRunCtx[2 * chunk], runOut = b.chunkRunCtx[2 * chunk + 1];
+      const int dupKey = cd.binCount;
+      if (cr.x > 0) {
+        const long long e = cr.z ? runOut : cstart + cr.x;
+        run_tokens(runIn, e, cstart, cstart + (cr.z ? cr.w : cr.x), dupKey, dupV,
+                   [&](uint16_t t) { if (nPre < kMaxEdgeTokens) pre[nPre++] = t; });
+      }
+      if (!cr.z && cr.y > 0) {
+        const long long s0 = cstart + cr.w - cr.y;
+        run_tokens(s0, runOut, s0, cstart + cr.w, dupKey, dupV,
+                   [&](uint16_t t) { if (nPost < kMaxEdgeTokens) post[nPost++] = t; });
+      }
     }
+    for (int i = 0; i < nPre; i++) list[i] = pre[i];
+    for (int i = 0; i < nPost; i++) list[nPre + nInt + i] = post[i];
+    sCount[0] = nPre;
+    sCount[1] = nPre + nInt + nPost;
   }
-  if (dupE >= 0) {
-    const int l = t.len[t.dupKey];
-    if (t.code) bits = t.code[t.dupKey] | ((unsigned long long)dupE << l);
-    return l + 3;
-  }
-  if (t.code) bits = t.code[t.dupV];
-  return t.len[t.dupV];
+  __syncthreads();
+  const int nPre = sCount[0];
+  for (int i = threadIdx.x; i < nInt; i += kThreads) list[nPre + i] = src[i];
+  __syncthreads();
+  return sCount[1];
 }
 
-// Token lengths (and bits) for this thread's kPer elements.  Collective over
-// the block (uses two block-wide scans).
-__device__ void thread_tokens(const int (&bins)[kPer], int p0, int len, const TokCtx &t,
-                              int (&tl)[kPer], unsigned long long (&tb)[kPer],
-                              int *wFirst, int *wLast) {
-  const int dupV = t.dupV;
-  int first = INF, last = -1;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) {
-    const int p = p0 + k;
-    if (p < len && bins[k] != dupV) {
-      if (first == INF) first = p;
-      last = p;
-    }
-  }
-  int nextNZ = INF, prevNZ = -1;
-  if (dupV >= 0) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int incMin = first, incMax = last;
-    for (int off = 1; off < 32; off <<= 1) {
-      int vmin = __shfl_down_sync(0xffffffffu, incMin, off);
-      int vmax = __shfl_up_sync(0xffffffffu, incMax, off);
-      if (lane + off < 32) incMin = min(incMin, vmin);
-      if (lane >= off) incMax = max(incMax, vmax);
-    }
-    if (lane == 0) wFirst[w] = incMin;
-    if (lane == 31) wLast[w] = incMax;
-    __syncthreads();
-    nextNZ = __shfl_down_sync(0xffffffffu, incMin, 1);
-    if (lane == 31) nextNZ = INF;
-    prevNZ = __shfl_up_sync(0xffffffffu, incMax, 1);
-    if (lane == 0) prevNZ = -1;
-    for (int v = w + 1; v < kThreads / 32; v++) nextNZ = min(nextNZ, wFirst[v]);
-    for (int v = 0; v < w; v++) prevNZ = max(prevNZ, wLast[v]);
-    __syncthreads();
-  }
-  // walk: last non-zero position seen so far (chunk coordinates)
-  int lastNZ = prevNZ;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) {
-    const int p = p0 + k;
-    tl[k] = 0;
-    tb[k] = 0;
-    if (p >= len) continue;
-    const int v = bins[k];
-    if (v != dupV) {
-      tl[k] = t.len[v];
-      if (t.code) tb[k] = t.code[v];
-      lastNZ = p;
-      continue;
-    }
-    // run start
-    const long long s = lastNZ < 0 ? t.runIn : t.chunkStart + lastNZ + 1;
-    // run end: next non-zero position after p
-    int nz = INF;
-    for (int k2 = k + 1; k2 < kPer; k2++)
-      if (p0 + k2 < len && bins[k2] != dupV) { nz = p0 + k2; break; }
-    if (nz == INF) nz = nextNZ;
-    const long long e = (nz == INF || nz >= len) ? t.runOut : t.chunkStart + nz;
-    unsigned long long bits = 0;
-    tl[k] = run_token(t.chunkStart + p, s, e, t, bits);
-    tb[k] = bits;
-  }
-}
-
-__device__ __forceinline__ void load_bins(const uint16_t *src, int p0, int len, int dupV,
-                                          int (&bins)[kPer]) {
-  if (p0 + kPer <= len) {
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(src + p0);
-#pragma unroll
-    for (int k = 0; k < kPer / 8; k++) {
-      const uint4 v = s4[k];
-      bins[8 * k + 0] = v.x & 0xffff; bins[8 * k + 1] = v.x >> 16;
-      bins[8 * k + 2] = v.y & 0xffff; bins[8 * k + 3] = v.y >> 16;
-      bins[8 * k + 4] = v.z & 0xffff; bins[8 * k + 5] = v.z >> 16;
-      bins[8 * k + 6] = v.w & 0xffff; bins[8 * k + 7] = v.w >> 16;
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < kPer; k++) bins[k] = (p0 + k < len) ? src[p0 + k] : dupV;
-  }
+__device__ __forceinline__ int token_len(uint16_t t, const uint8_t *len, int dupKey) {
+  const int sym = t & 0x1fff;
+  return len[sym] + (sym == dupKey ? 3 : 0);
 }
 
 // block sum of unsigned long long (256 threads)
@@ -388,44 +308,20 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, un
   return before + inc - v;
 }
 
-__device__ __forceinline__ void setup_ctx(const DevBatch &b, long long chunk, int ci,
-                                          const CubeletDev &cd, TokCtx &t, uint8_t *sLen,
-                                          unsigned long long *sCode) {
-  const CubeletState *st = b.state + ci;
-  t.dupV = st->dupValue;
-  t.dupKey = cd.binCount;
-  t.chunkStart = (chunk - cd.chunkBase) * (long long)kChunk;
-  t.runIn = t.dupV >= 0 ? b.chunkRunCtx[2 * chunk] : 0;
-  t.runOut = t.dupV >= 0 ? b.chunkRunCtx[2 * chunk + 1] : 0;
-  const int S = cd.binCount + 1;
-  for (int i = threadIdx.x; i < S; i += kThreads) {
-    sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
-    if (sCode) sCode[i] = b.codes[(size_t)ci * kMaxSymbols + i];
-  }
-  t.len = sLen;
-  t.code = sCode;
-}
-
 __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
   __shared__ uint8_t sLen[kMaxSymbols + 3];
-  __shared__ int wFirst[kThreads / 32], wLast[kThreads / 32];
+  __shared__ uint16_t list[kMaxChunkTokens];
+  __shared__ int sCount[2];
   __shared__ unsigned long long sh[kThreads / 32];
   const long long chunk = blockIdx.x;
   const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
   const CubeletDev cd = b.cub[ci];
-  TokCtx t;
-  setup_ctx(b, chunk, ci, cd, t, sLen, nullptr);
-  __syncthreads();
-  const int len = (int)min((long long)kChunk, cd.n - t.chunkStart);
-  const int p0 = threadIdx.x * kPer;
-  int bins[kPer];
-  load_bins(b.bins + cd.coefOff + t.chunkStart, p0, len, t.dupV, bins);
-  int tl[kPer];
-  unsigned long long tb[kPer];
-  thread_tokens(bins, p0, len, t, tl, tb, wFirst, wLast);
+  const int dupV = b.state[ci].dupValue;
+  const int S = cd.binCount + 1;
+  for (int i = threadIdx.x; i < S; i += kThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
+  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);
   unsigned long long s = 0;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) s += tl[k];
+  for (int i = threadIdx.x; i < n; i += kThreads) s += token_len(list[i], sLen, cd.binCount);
   s = block_sum(s, sh);
   if (threadIdx.x == 0) b.chunkBits[chunk] = s;
 }
@@ -496,7 +392,8 @@ constexpr int kMaxChunkWords = (kChunk * (kMaxCodeBits + 3) + 31) / 32 + 2;
 __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   __shared__ uint8_t sLen[kMaxSymbols + 3];
   __shared__ unsigned long long sCode[kMaxSymbols];
-  __shared__ int wFirst[kThreads / 32], wLast[kThreads / 32];
+  __shared__ uint16_t list[kMaxChunkTokens];
+  __shared__ int sCount[2];
   __shared__ unsigned shs[kThreads / 32];
   extern __shared__ uint32_t sw[];
   const long long chunk = blockIdx.x;
@@ -504,40 +401,43 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   if (st->error) return;
-  TokCtx t;
-  setup_ctx(b, chunk, ci, cd, t, sLen, sCode);
+  const int dupV = st->dupValue, dupKey = cd.binCount;
+  const int S = cd.binCount + 1;
+  for (int i = threadIdx.x; i < S; i += kThreads) {
+    sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
+    sCode[i] = b.codes[(size_t)ci * kMaxSymbols + i];
+  }
   const unsigned long long chunkOff = b.chunkBits[chunk];
   const unsigned long long chunkEnd = (chunk + 1 < cd.chunkBase + cd.nChunks)
                                           ? b.chunkBits[chunk + 1] : st->totalBits;
   const int shift = (int)(chunkOff & 31);
   const int nW = (int)((shift + (chunkEnd - chunkOff) + 31) >> 5);
   for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
-  __syncthreads();
-  const int len = (int)min((long long)kChunk, cd.n - t.chunkStart);
-  const int p0 = threadIdx.x * kPer;
-  int bins[kPer];
-  load_bins(b.bins + cd.coefOff + t.chunkStart, p0, len, t.dupV, bins);
-  int tl[kPer];
-  unsigned long long tb[kPer];
-  thread_tokens(bins, p0, len, t, tl, tb, wFirst, wLast);
+  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);
+  // each thread takes a contiguous slice of the tokens
+  const int per = (n + kThreads - 1) / kThreads;
+  const int t0 = min(n, (int)threadIdx.x * per), t1 = min(n, t0 + per);
   unsigned mine = 0;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) mine += tl[k];
+  for (int i = t0; i < t1; i++) mine += token_len(list[i], sLen, dupKey);
   unsigned total;
   unsigned pos = block_excl_scan(mine, shs, total) + shift;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) {
-    int l = tl[k];
-    if (!l) continue;
-    unsigned long long v = tb[k];
+  for (int i = t0; i < t1; i++) {
+    const uint16_t t = list[i];
+    const int sym = t & 0x1fff;
+    int l = sLen[sym];
+    unsigned long long v = sCode[sym];
+    if (sym == dupKey) {
+      v |= (unsigned long long)(t >> 13) << l;
+      l += 3;
+    }
     unsigned p = pos;
     pos += l;
     // up to 61 bits starting anywhere in a word: at most 3 words
     while (l > 0) {
       const int o = p & 31;
       const int take = min(l, 32 - o);
-      const unsigned chunkBits = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
-      atomicOr(&sw[p >> 5], chunkBits << o);
+      const unsigned part = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
+      atomicOr(&sw[p >> 5], part << o);
       v >>= take;
       p += take;
       l -= take;

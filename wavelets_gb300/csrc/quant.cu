@@ -140,17 +140,43 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
   const float l0 = degenerate ? 0.f : log2f(lo);
   const float w = degenerate ? 1.f : (log2f(hi) - l0) / kLloydBins;
 
-  // prefix sums (fixed order, so the codebook is deterministic)
-  if (threadIdx.x == 0) { pw[0] = 0; pwx[0] = 0; }
-  for (int i = threadIdx.x; i < kLloydBins; i += 1024) {
-    const double c = degenerate ? 0.0 : (double)g[i];
-    const double x = exp2((double)l0 + ((double)i + 0.5) * (double)w);
-    pw[i + 1] = c;
-    pwx[i + 1] = c * x;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int i = 1; i <= kLloydBins; i++) { pw[i] += pw[i - 1]; pwx[i] += pwx[i - 1]; }
+  // prefix sums of counts and count*centre; fixed order, so the codebook is
+  // deterministic: each thread sums 4 consecutive bins, then a block scan
+  {
+    const int per = kLloydBins / 1024;
+    double c4[per], x4[per], sc = 0, sx = 0;
+    for (int j = 0; j < per; j++) {
+      const int i = threadIdx.x * per + j;
+      const double c = degenerate ? 0.0 : (double)g[i];
+      const double x = exp2((double)l0 + ((double)i + 0.5) * (double)w);
+      sc += c;
+      sx += c * x;
+      c4[j] = sc;
+      x4[j] = sx;
+    }
+    // inclusive warp scan of the per-thread totals
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    double ic = sc, ix = sx;
+    for (int off = 1; off < 32; off <<= 1) {
+      const double tc = __shfl_up_sync(0xffffffffu, ic, off);
+      const double tx = __shfl_up_sync(0xffffffffu, ix, off);
+      if (lane >= off) { ic += tc; ix += tx; }
+    }
+    double *wc = reinterpret_cast<double *>(nxt);  // scratch before the iterations
+    double *wx = wc + 32;
+    if (lane == 31) { wc[wp] = ic; wx[wp] = ix; }
+    __syncthreads();
+    double bc = 0, bx = 0;
+    for (int v = 0; v < wp; v++) { bc += wc[v]; bx += wx[v]; }
+    bc += ic - sc;
+    bx += ix - sx;
+    if (threadIdx.x == 0) { pw[0] = 0; pwx[0] = 0; }
+    for (int j = 0; j < per; j++) {
+      const int i = threadIdx.x * per + j;
+      pw[i + 1] = bc + c4[j];
+      pwx[i + 1] = bx + x4[j];
+    }
+    __syncthreads();
   }
   // initialLloydCodebook (test_compress_common.cc:749-779)
   if (cbs >= 1) {
@@ -241,6 +267,21 @@ struct QParams {
   int lowBin, highNeg, nPos, nNeg;
 };
 
+// number of entries of the sorted table t[0..n) that are <= x / < x, by a
+// fixed number of halving steps (no divergent loop exits)
+__device__ __forceinline__ int count_le(const float *t, int n, float x) {
+  int pos = 0;
+  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
+    if (step <= n - pos && t[pos + step - 1] <= x) pos += step;
+  return pos;
+}
+__device__ __forceinline__ int count_lt(const float *t, int n, float x) {
+  int pos = 0;
+  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
+    if (step <= n - pos && t[pos + step - 1] < x) pos += step;
+  return pos;
+}
+
 __device__ __forceinline__ int quant_value(float x, const QParams &q, const float *tab) {
   if (q.alg == WL_UNIFORM) {
     // QuantUniform::quant (quant.h:244-276)
@@ -260,31 +301,16 @@ __device__ __forceinline__ int quant_value(float x, const QParams &q, const floa
     if (x < 0) {
       const float y = -x;
       if (y <= q.thr) return q.zb;
-      const float *N = tab + q.nPos;
-      int lo = 0, hi = q.nNeg;  // count entries <= y
-      while (lo < hi) {
-        int m = (lo + hi) >> 1;
-        if (N[m] <= y) lo = m + 1; else hi = m;
-      }
-      return q.highNeg - lo;
+      return q.highNeg - count_le(tab + q.nPos, q.nNeg, y);
     }
     if (x <= q.thr) return q.zb;
-    int lo = 0, hi = q.nPos;
-    while (lo < hi) {
-      int m = (lo + hi) >> 1;
-      if (tab[m] <= x) lo = m + 1; else hi = m;
-    }
-    return q.lowBin + lo;
+    return q.lowBin + count_le(tab, q.nPos, x);
   }
-  // QuantCodebook::quant (quant.h:515-526)
+  // QuantCodebook::quant (quant.h:515-526): x >= last boundary -> nb, else
+  // lower_bound (the number of boundaries below x)
   if (q.nb == 0) return 0;
   if (x >= tab[q.nb - 1]) return q.nb;
-  int lo = 0, hi = q.nb;
-  while (lo < hi) {
-    int m = (lo + hi) >> 1;
-    if (tab[m] < x) lo = m + 1; else hi = m;
-  }
-  return lo;
+  return count_lt(tab, q.nb, x);
 }
 
 __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const CubeletState *st) {
@@ -308,13 +334,20 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
   return q;
 }
 
-// ---- quantize + count + chunk run summary ----------------------------------
+// ---- quantize + count + tokens of the chunk ----------------------------------
+// Each thread quantizes 16 consecutive coefficients.  Instead of storing a bin
+// per coefficient, the chunk stores its Huffman tokens in order: every value
+// that is not the zero bin, and the tokens of every zero-bin run that starts
+// and ends inside the chunk.  Runs touching a chunk edge are left to
+// runs_kernel (counts) and the encoder (tokens).
 __global__ void __launch_bounds__(kThreads)
 quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kMaxSymbols + 1];
-  __shared__ float tab[kMaxBins];
+  extern __shared__ float tab[];  // quantizer table (Lloyd / log), sized by the launch
   __shared__ int wFirst[kThreads / 32], wLast[kThreads / 32];
-  __shared__ unsigned long long sDup;
+  __shared__ unsigned wCnt[kThreads / 32];
+  __shared__ uint16_t sTok[kChunk];
+  __shared__ uint16_t sBin[kChunk];
   const long long chunk = blockIdx.x;
   const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
   const CubeletDev cd = b.cub[ci];
@@ -325,14 +358,13 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   const int nTab = q.alg == WL_LLOYD ? q.nb : (q.alg == WL_LOG ? q.nPos + q.nNeg : 0);
   for (int i = threadIdx.x; i < B + 1; i += kThreads) hist[i] = 0;
   for (int i = threadIdx.x; i < nTab; i += kThreads) tab[i] = b.qtable[cd.tableOff + i];
-  if (threadIdx.x == 0) sDup = 0;
   __syncthreads();
 
   const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
   const int len = (int)min((long long)kChunk, cd.n - start);
   const float *src = coef + cd.coefOff + start;
-  uint16_t *dst = b.bins + cd.coefOff + start;
   const int p0 = threadIdx.x * kPer;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 
   int bins[kPer];
   if (p0 + kPer <= len) {
@@ -345,82 +377,102 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
       bins[4 * k + 2] = quant_value(v.z, q, tab);
       bins[4 * k + 3] = quant_value(v.w, q, tab);
     }
-    uint4 *d4 = reinterpret_cast<uint4 *>(dst + p0);
-#pragma unroll
-    for (int k = 0; k < kPer / 8; k++) {
-      uint4 o;
-      o.x = (unsigned)bins[8 * k + 0] | ((unsigned)bins[8 * k + 1] << 16);
-      o.y = (unsigned)bins[8 * k + 2] | ((unsigned)bins[8 * k + 3] << 16);
-      o.z = (unsigned)bins[8 * k + 4] | ((unsigned)bins[8 * k + 5] << 16);
-      o.w = (unsigned)bins[8 * k + 6] | ((unsigned)bins[8 * k + 7] << 16);
-      d4[k] = o;
-    }
   } else {
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      const int p = p0 + k;
-      bins[k] = p < len ? quant_value(src[p], q, tab) : dupV;
-      if (p < len) dst[p] = (uint16_t)bins[k];
-    }
+    for (int k = 0; k < kPer; k++) bins[k] = p0 + k < len ? quant_value(src[p0 + k], q, tab) : 0;
   }
-
-  // histogram of the values that are not part of zero runs
-  int first = INF, last = -1;
+  const unsigned valid = p0 >= len ? 0u : (p0 + kPer <= len ? 0xffffu : ((1u << (len - p0)) - 1u));
+  unsigned zm = 0;
 #pragma unroll
-  for (int k = 0; k < kPer; k++) {
-    const int p = p0 + k;
-    if (p >= len) break;
-    if (bins[k] != dupV) {
-      atomicAdd(&hist[bins[k]], 1u);
-      if (first == INF) first = p;
-      last = p;
-    }
-  }
+  for (int k = 0; k < kPer; k++) zm |= (bins[k] == dupV ? 1u : 0u) << k;
+  zm &= valid;
+  const unsigned nzm = valid & ~zm;
 
+  // next non-zero position after this thread's range, last one before it
+  int nextNZ = INF, prevNZ = -1;
   if (dupV >= 0) {
-    // next non-zero-bin position after this thread's range, previous before it
-    int sufMin = first, preMax = last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int incMin = sufMin, incMax = preMax;
+    const int first = nzm ? p0 + __ffs(nzm) - 1 : INF;
+    const int last = nzm ? p0 + 31 - __clz(nzm) : -1;
+    int incMin = first, incMax = last;
     for (int off = 1; off < 32; off <<= 1) {
-      int vmin = __shfl_down_sync(0xffffffffu, incMin, off);
-      int vmax = __shfl_up_sync(0xffffffffu, incMax, off);
+      const int vmin = __shfl_down_sync(0xffffffffu, incMin, off);
+      const int vmax = __shfl_up_sync(0xffffffffu, incMax, off);
       if (lane + off < 32) incMin = min(incMin, vmin);
       if (lane >= off) incMax = max(incMax, vmax);
     }
-    if (lane == 0) wFirst[w] = incMin;   // min over the whole warp
-    if (lane == 31) wLast[w] = incMax;   // max over the whole warp
+    if (lane == 0) wFirst[w] = incMin;
+    if (lane == 31) wLast[w] = incMax;
     __syncthreads();
-    int nextNZ = __shfl_down_sync(0xffffffffu, incMin, 1);
+    nextNZ = __shfl_down_sync(0xffffffffu, incMin, 1);
     if (lane == 31) nextNZ = INF;
-    int prevNZ = __shfl_up_sync(0xffffffffu, incMax, 1);
+    prevNZ = __shfl_up_sync(0xffffffffu, incMax, 1);
     if (lane == 0) prevNZ = -1;
     for (int v = w + 1; v < kThreads / 32; v++) nextNZ = min(nextNZ, wFirst[v]);
     for (int v = 0; v < w; v++) prevNZ = max(prevNZ, wLast[v]);
+  }
 
-    // runs that start inside this thread's range and end inside the chunk
-    long long singles = 0, dups = 0;
-    int k = 0;
-    while (k < kPer && p0 + k < len) {
-      if (bins[k] != dupV) { k++; continue; }
-      const int s = p0 + k;
-      const bool startsHere = (k > 0) ? true : (prevNZ == s - 1);
-      int e = k;
-      while (e < kPer && p0 + e < len && bins[e] == dupV) e++;
-      int endPos;
-      if (e < kPer && p0 + e < len) endPos = p0 + e;
-      else endPos = (p0 + e >= len) ? INF : nextNZ;
-      if (startsHere && s > 0 && endPos != INF && endPos < len) {
-        long long sg, dp;
-        run_split(endPos - s, sg, dp);
-        singles += sg;
-        dups += dp;
-      }
-      k = e;
+  // Tokens of this thread in position order: a token for every non-zero-bin
+  // value, and the tokens of every run that starts here and ends inside the
+  // chunk.  run start = zero-bin value whose predecessor is not one.
+  unsigned starts = zm & ((nzm << 1) | (prevNZ == p0 - 1 && p0 > 0 ? 1u : 0u));
+  // drop runs that reach the chunk end (trailing) -- they belong to runs_kernel
+  unsigned cnt = __popc(nzm);
+  {
+    unsigned m = starts;
+    while (m) {
+      const int k = __ffs(m) - 1;
+      m &= m - 1;
+      const unsigned later = nzm & ~((2u << k) - 1u);
+      const int end = later ? p0 + __ffs(later) - 1 : ((p0 + kPer >= len) ? INF : nextNZ);
+      if (end == INF) { starts &= ~(1u << k); continue; }
+      cnt += run_token_count(end - (p0 + k));
     }
-    if (singles) atomicAdd(&hist[dupV], (unsigned)singles);
-    if (dups) atomicAdd(&sDup, (unsigned long long)dups);
-    if (threadIdx.x == 0) {
+  }
+  // exclusive scan of the per-thread counts
+  unsigned base;
+  {
+    unsigned inc = cnt;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += t;
+    }
+    if (lane == 31) wCnt[w] = inc;
+    // stage the bins for the emission loop (dynamic index, shared memory)
+#pragma unroll
+    for (int k = 0; k < kPer; k++) sBin[threadIdx.x * kPer + k] = (uint16_t)bins[k];
+    __syncthreads();
+    unsigned before = 0;
+    for (int v = 0; v < w; v++) before += wCnt[v];
+    base = before + inc - cnt;
+  }
+  {
+    unsigned o = base;
+    unsigned ev = nzm | starts;
+    const uint16_t *mb = sBin + threadIdx.x * kPer;
+    auto put = [&](uint16_t t) {
+      sTok[o++] = t;
+      atomicAdd(&hist[t & 0x1fff], 1u);
+    };
+    while (ev) {
+      const int k = __ffs(ev) - 1;
+      ev &= ev - 1;
+      if (nzm & (1u << k)) {
+        put(make_token(mb[k], 0));
+      } else {
+        const unsigned later = nzm & ~((2u << k) - 1u);
+        const int end = later ? p0 + __ffs(later) - 1 : nextNZ;
+        run_tokens(p0 + k, end, p0 + k, end, B, dupV, put);
+      }
+    }
+  }
+  __syncthreads();
+  unsigned total = 0;
+  for (int v = 0; v < kThreads / 32; v++) total += wCnt[v];
+  uint16_t *dst = b.tok + cd.coefOff + start;
+  for (unsigned i = threadIdx.x; i < total; i += kThreads) dst[i] = sTok[i];
+  if (threadIdx.x == 0) {
+    b.chunkTok[chunk] = (int)total;
+    if (dupV >= 0) {
       int fz = INF, lz = -1;
       for (int v = 0; v < kThreads / 32; v++) { fz = min(fz, wFirst[v]); lz = max(lz, wLast[v]); }
       const int lead = fz == INF ? len : fz;
@@ -428,11 +480,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
       b.chunkRun[chunk] = make_int4(lead, trail, lz < 0 ? 1 : 0, len);
     }
   }
-  __syncthreads();
   unsigned long long *gh = b.hist + (size_t)ci * kMaxSymbols;
-  for (int i = threadIdx.x; i < B; i += kThreads)
+  for (int i = threadIdx.x; i <= B; i += kThreads)
     if (hist[i]) atomicAdd(&gh[i], (unsigned long long)hist[i]);
-  if (threadIdx.x == 0 && sDup) atomicAdd(&gh[B], sDup);
 }
 
 // Join zero runs across chunk edges; one CTA per cubelet.
@@ -581,8 +631,11 @@ void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
   lloyd_solve_kernel<<<b.n, 1024, kLloydSmem, s>>>(b);
 }
 
-void launch_quantize(DevBatch &b, const float *coef, cudaStream_t s) {
-  quantize_kernel<<<(unsigned)b.totalChunks, kThreads, 0, s>>>(b, coef);
+void launch_quantize(DevBatch &b, const float *coef, int maxTable, cudaStream_t s) {
+  const int smem = maxTable * (int)sizeof(float);
+  cudaFuncSetAttribute(quantize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem > 0 ? smem : 1);
+  quantize_kernel<<<(unsigned)b.totalChunks, kThreads, smem, s>>>(b, coef);
 }
 
 void launch_runs(DevBatch &b, cudaStream_t s) { runs_kernel<<<b.n, 1024, 0, s>>>(b); }

@@ -11,6 +11,14 @@
 
 namespace wl {
 
+__host__ __device__ inline int clz32(unsigned x) {
+#ifdef __CUDA_ARCH__
+  return __clz(x);
+#else
+  return __builtin_clz(x);
+#endif
+}
+
 constexpr int kMaxBins = 4096;          // bins per cubelet (kernel tables)
 constexpr int kMaxSymbols = kMaxBins + 1;
 constexpr int kChunk = 4096;            // elements per quantize/encode chunk
@@ -24,6 +32,56 @@ constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile
 // row kernel.  Rows are flattened r = b + B*a; row (a,b) of the input starts
 // at in + a*inSA + b*inSB (contiguous along c); element (a,b,c) of the
 // output goes to out + a*outSA + b*outSB + c*outSC.
+// A Huffman token: symbol (bin, or binCount = the zero-run key) in bits 0-12,
+// the zero-run length code v (run of 2^(v+3)) in bits 13-15.
+__host__ __device__ inline uint16_t make_token(int sym, int v) {
+  return (uint16_t)(sym | (v << 13));
+}
+
+// Tokens of a zero-bin run [s, e) that start inside [w0, w1), in order
+// (HuffmanDup::dupCount / Huffman::dupEncodeString, huffman.h:31-57,
+// 278-296: greedy runs of 1024, then the largest power of two >= 8 while
+// more than 8 remain, then single zero-bin tokens).  Calls f(token).  At
+// most 19 tokens start in a window of kChunk elements.
+template <class F>
+__host__ __device__ inline void run_tokens(long long s, long long e, long long w0,
+                                           long long w1, int dupKey, int dupV, F f) {
+  const long long L = e - s;
+  const long long q = L >> 10;
+  long long j0 = 0;
+  if (w0 > s) j0 = (w0 - s + 1023) >> 10;
+  for (long long j = j0; j < q; j++) {
+    const long long pos = s + (j << 10);
+    if (pos >= w1) break;
+    f(make_token(dupKey, 7));
+  }
+  long long pos = s + (q << 10);
+  int r = (int)(L - (q << 10));
+  while (r > 8) {
+    int lg = 31 - clz32(r);
+    if (pos >= w0 && pos < w1) f(make_token(dupKey, lg - 3));
+    pos += 1 << lg;
+    r -= 1 << lg;
+  }
+  long long a = pos > w0 ? pos : w0, z = pos + r < w1 ? pos + r : w1;
+  for (long long x = a; x < z; x++) f(make_token(dupV, 0));
+}
+
+// Number of tokens of a zero-bin run of length L (the same split as
+// run_tokens): runs of 1024, then one token per set bit of the remainder at
+// or above 8 -- except that a last 8 left over is coded as 8 single tokens.
+__host__ __device__ inline int run_token_count(long long L) {
+  const int q = (int)(L >> 10), r = (int)(L & 1023);
+  const int hi = r & ~7, lo = r & 7;
+#ifdef __CUDA_ARCH__
+  int big = __popc(hi >> 4);
+#else
+  int big = __builtin_popcount(hi >> 4);
+#endif
+  if (hi & 8) return q + big + (lo > 0 ? 1 + lo : 8);
+  return q + big + lo;
+}
+
 struct PassDesc {
   const void *in;
   void *out;
@@ -93,13 +151,14 @@ struct DevBatch {
   CubeletState *state;            // [n]
   float *coef;                    // coefficients (ping)
   float *coef2;                   // second buffer (pong)
-  uint16_t *bins;                 // quantized bins
+  uint16_t *tok;                  // Huffman tokens, one slot of kChunk per chunk
+  int *chunkTok;                  // tokens stored per chunk
   unsigned *selHist;              // [n][kSelectBins]
   float *lloydHist;               // [n][kLloydBins][2] (count, sum)
   float *qtable;                  // quantizer tables
   float *dqtable;                 // dequant values [n][binCount]
   unsigned long long *hist;       // [n][kMaxSymbols] Huffman counts
-  int4 *chunkRun;                 // per chunk: lead, trail, allZero, pad
+  int4 *chunkRun;                 // per chunk: lead, trail, allZero, len
   long long *chunkRunCtx;         // per chunk: start of incoming run, end of outgoing run (2 each)
   unsigned long long *chunkBits;  // per chunk bit count / offset
   unsigned long long *codes;      // [n][kMaxSymbols] code bits
@@ -124,7 +183,7 @@ void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
 // launchers (quant.cu)
 void launch_quant_params(DevBatch &b, cudaStream_t s);
 void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s);
-void launch_quantize(DevBatch &b, const float *coef, cudaStream_t s);
+void launch_quantize(DevBatch &b, const float *coef, int maxTable, cudaStream_t s);
 void launch_runs(DevBatch &b, cudaStream_t s);
 
 // launchers (huffman.cu)
