@@ -198,17 +198,39 @@ EDGE = [
                                                                     threshold_fraction=0.8)),
     ("long_runs", np.pad(np.ones((2, 2, 2), np.float32), ((0, 30), (0, 30), (0, 62))),
      P.Params(threshold_fraction=0.99)),
+    # nearly equal code lengths: speculative decoding does not resynchronise
+    ("flat_codes", np.random.default_rng(9).uniform(-1, 1, (32, 32, 64)).astype(np.float32),
+     P.Params(steps=(0, 0, 0), threshold_fraction=0.0, quant_alg=P.UNIFORM, bin_count=256)),
 ]
 
 
 @pytest.mark.parametrize("name,arr,p", EDGE, ids=[e[0] for e in EDGE])
 def test_edge_cases(ctx, name, arr, p):
     comp, coeffs = _check_integer_stages(ctx, arr, p)
-    # decoding the GPU stream with the reference's table walk gives bins of
-    # the right count
+    # the reference's table walk decodes the GPU stream to bins of the right count
     bins = oracle.huffman_decode(comp.words, comp.decode, comp.dup_key, comp.dup_value,
                                  coeffs.size)
     assert bins.size == coeffs.size
+    # GPU decompression (GPU Huffman decode) == oracle dequantize + inverse
+    got = ctx.decompress(comp, np.float32)
+    qalg = {P.UNIFORM: oracle.UNIFORM, P.LOG: oracle.LOG, P.LLOYD: oracle.LLOYD}[p.quant_alg]
+    deq = oracle.dequantize(bins, qalg, p.bin_count, comp.threshold_value, comp.max_value,
+                            comp.values if p.quant_alg == P.LLOYD else None)
+    if comp.steps == (0, 0, 0):
+        Xp, Yp, Zp = comp.size
+    else:
+        Zp, Xp, Yp = comp.size
+    ref = oracle.inverse(deq, (Zp, Yp, Xp), comp.steps, p.wavelet)
+    a3 = arr if arr.ndim == 3 else arr.reshape((1,) * (3 - arr.ndim) + arr.shape)
+    ref = ref[:a3.shape[0], :a3.shape[1], :a3.shape[2]]
+    assert got.shape == ref.shape
+    # a 3-bin log quantizer has a zero scale on one side; the reference's own
+    # dequantizer then yields NaN/inf there, and so does this one
+    fin = np.isfinite(ref)
+    assert np.array_equal(fin, np.isfinite(got))
+    if fin.any():
+        scale = max(1e-30, float(np.abs(ref[fin]).max()))
+        assert float(np.abs(got[fin].astype(np.float64) - ref[fin]).max()) <= 1e-4 * scale
 
 
 def test_batch_equals_single(ctx):

@@ -1,0 +1,313 @@
+// Huffman decoding on the device for streams without any index (files the
+// reference wrote decode too).
+//
+// Reference: HuffmanDecoder::decodeFromStream (huffman.h:96-131) walks the
+// breadth-first decode table bit by bit; a zero-run key is followed by 3
+// length bits and expands to 2^(v+3) copies of the zero bin.
+//
+// The stream is cut into subsequences of kSubBits bits.  Phase 1: every
+// subsequence is decoded speculatively from its first bit until the decoder
+// crosses into the next subsequence; it records where that happens (its exit,
+// a token boundary) and how many elements it produced.  Huffman codes
+// resynchronise after a few tokens, so the exit rarely depends on where the
+// decoding started.  Rounds: a subsequence whose start differs from its
+// predecessor's exit is decoded again from that exit; rounds repeat until no
+// start changes (each round fixes at least the first wrong subsequence).
+// Then an exclusive scan of the element counts gives every subsequence its
+// output offset, and a last pass decodes again and writes the elements.
+// A 12-bit lookup table resolves most codes in one step.
+#include <cstring>
+
+#include "wl_internal.h"
+
+namespace wl {
+namespace {
+
+constexpr int kSubBits = 1024;
+constexpr int kLutBits = 12;
+constexpr int kThreads = 256;
+
+struct DecCub {
+  const uint32_t *words;
+  long long nWords;
+  const int *table;
+  int nTable;
+  int dupKey, dupValue;
+  int binCount;
+  long long n;        // elements
+  int *out;           // bins
+  long long subBase;  // first subsequence
+  long long nSub;
+  int lutOff;
+};
+
+__device__ __forceinline__ int find_cub(const DecCub *c, int n, long long sub) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (c[mid].subBase <= sub) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// 64 bits of the stream starting at bit p (zero past the end)
+__device__ __forceinline__ unsigned long long peek64(const uint32_t *w, long long nw, long long p) {
+  const long long i = p >> 5;
+  const int o = (int)(p & 31);
+  unsigned long long a = i < nw ? w[i] : 0u;
+  unsigned long long b = i + 1 < nw ? w[i + 1] : 0u;
+  unsigned long long c = i + 2 < nw ? w[i + 2] : 0u;
+  const unsigned long long lo = a | (b << 32);
+  return o ? ((lo >> o) | (c << (64 - o))) : lo;
+}
+
+// LUT entry: bit 31 leaf; leaf: bits 16-23 code length, bits 0-15 symbol;
+// not a leaf: bits 0-30 node offset in the decode table after kLutBits bits
+__global__ void build_lut_kernel(const DecCub *cubs, unsigned *lut) {
+  const DecCub c = cubs[blockIdx.x];
+  unsigned *L = lut + (size_t)c.lutOff;
+  for (int p = threadIdx.x; p < (1 << kLutBits); p += blockDim.x) {
+    if (c.nTable == 2) {  // one node: a zero-length code
+      L[p] = 0x80000000u | (unsigned)c.table[1];
+      continue;
+    }
+    int node = 0;
+    unsigned e = 0;
+    bool leaf = false;
+    for (int d = 0; d < kLutBits; d++) {
+      const int bit = (p >> d) & 1;
+      const int nx = c.table[node + bit] * 2;
+      if (nx < 0 || nx + 1 >= c.nTable) { e = 0x80000000u | (0xffu << 16) | 0xffffu; leaf = true; break; }
+      node = nx;
+      if (c.table[node] == 0) {
+        e = 0x80000000u | ((unsigned)(d + 1) << 16) | (unsigned)c.table[node + 1];
+        leaf = true;
+        break;
+      }
+    }
+    L[p] = leaf ? e : (unsigned)node;
+  }
+}
+
+// Decode one token at bit p.  Returns bits consumed (0 = malformed), sets the
+// element count and the value.
+__device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, long long p,
+                                            int &count, int &value) {
+  unsigned long long bits = peek64(c.words, c.nWords, p);
+  const unsigned e = L[bits & ((1u << kLutBits) - 1)];
+  int len, sym;
+  if (e & 0x80000000u) {
+    len = (e >> 16) & 0xff;
+    sym = e & 0xffff;
+    if (len == 0xff) return 0;
+  } else {
+    int node = (int)e;
+    len = kLutBits;
+    bits >>= kLutBits;
+    while (true) {
+      const int nx = c.table[node + (int)(bits & 1)] * 2;
+      bits >>= 1;
+      len++;
+      if (nx < 0 || nx + 1 >= c.nTable || len > 60) return 0;
+      node = nx;
+      if (c.table[node] == 0) break;
+    }
+    sym = c.table[node + 1];
+  }
+  if (sym == c.dupKey && c.dupKey >= 0) {
+    const unsigned v = (unsigned)((peek64(c.words, c.nWords, p + len)) & 7u);
+    count = 1 << (v + 3);
+    value = c.dupValue;
+    return len + 3;
+  }
+  count = 1;
+  value = sym;
+  return len > 0 ? len : -1;  // -1: zero-length code (one-symbol stream)
+}
+
+// Decode tokens from `start` until the position reaches `limit`; returns the
+// exit position and the number of elements.
+__device__ long long decode_span(const DecCub &c, const unsigned *L, long long start, long long limit,
+                                 long long &elems, bool &bad) {
+  long long p = start, e = 0;
+  const long long total = c.nWords * 32;
+  while (p < limit && p < total) {
+    int cnt, val;
+    const int used = decode_token(c, L, p, cnt, val);
+    if (used <= 0) { bad = true; break; }
+    p += used;
+    e += cnt;
+  }
+  elems = e;
+  return p;
+}
+
+__global__ void spec_kernel(const DecCub *cubs, int nCub, const unsigned *lut, long long totalSub,
+                            long long *start, long long *exitPos, long long *elems, int *flags,
+                            int round) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= totalSub) return;
+  const int ci = find_cub(cubs, nCub, i);
+  const DecCub c = cubs[ci];
+  const long long local = i - c.subBase;
+  long long s;
+  if (round == 0) {
+    s = local * kSubBits;
+  } else {
+    if (local == 0) {  // always starts right; carry its exit to this round's buffer
+      exitPos[2 * i + (round & 1)] = exitPos[2 * i + ((round - 1) & 1)];
+      return;
+    }
+    s = exitPos[2 * (i - 1) + ((round - 1) & 1)];
+    if (s == start[i]) {
+      exitPos[2 * i + (round & 1)] = exitPos[2 * i + ((round - 1) & 1)];
+      return;
+    }
+    atomicAdd(&flags[0], 1);
+  }
+  start[i] = s;
+  bool bad = false;
+  long long e;
+  const long long x = decode_span(c, lut + c.lutOff, s, (local + 1) * kSubBits, e, bad);
+  exitPos[2 * i + (round & 1)] = x;
+  elems[i] = e;
+  if (bad) atomicAdd(&flags[1], 1);
+}
+
+// per cubelet exclusive scan of element counts (one CTA per cubelet)
+__global__ void __launch_bounds__(1024) elem_scan_kernel(const DecCub *cubs, long long *elems,
+                                                         long long *totalOut) {
+  __shared__ long long sh[32];
+  const DecCub c = cubs[blockIdx.x];
+  long long carry = 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (long long seg = 0; seg < c.nSub; seg += 1024) {
+    const long long j = seg + threadIdx.x;
+    const long long v = j < c.nSub ? elems[c.subBase + j] : 0;
+    long long inc = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += t;
+    }
+    if (lane == 31) sh[w] = inc;
+    __syncthreads();
+    long long before = 0, tot = 0;
+    for (int k = 0; k < 32; k++) { if (k < w) before += sh[k]; tot += sh[k]; }
+    if (j < c.nSub) elems[c.subBase + j] = carry + before + inc - v;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) totalOut[blockIdx.x] = carry;
+}
+
+__global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, long long totalSub,
+                             const long long *start, const long long *exitPos, const long long *offs,
+                             int lastRound) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= totalSub) return;
+  const int ci = find_cub(cubs, nCub, i);
+  const DecCub c = cubs[ci];
+  const unsigned *L = lut + c.lutOff;
+  const long long limit = exitPos[2 * i + (lastRound & 1)];
+  long long p = start[i], o = offs[i];
+  const long long total = c.nWords * 32;
+  while (p < limit && p < total && o < c.n) {
+    int cnt, val;
+    const int used = decode_token(c, L, p, cnt, val);
+    if (used <= 0) break;
+    p += used;
+    for (int k = 0; k < cnt && o < c.n; k++) c.out[o++] = val;
+  }
+}
+
+// Fallback when rounds do not converge (codes that never resynchronise, e.g.
+// all of one length): one thread fixes the subsequences in order.
+__global__ void seq_fix_kernel(const DecCub *cubs, const unsigned *lut, long long *start,
+                               long long *exitPos, long long *elems, int buf, int *flags) {
+  const DecCub c = cubs[0];
+  for (long long i = 1; i < c.nSub; i++) {
+    const long long s = exitPos[2 * (i - 1) + buf];
+    if (s == start[i]) continue;
+    start[i] = s;
+    bool bad = false;
+    long long e;
+    exitPos[2 * i + buf] = decode_span(c, lut + c.lutOff, s, (i + 1) * kSubBits, e, bad);
+    elems[i] = e;
+    if (bad) flags[1]++;
+  }
+}
+
+__global__ void fill_kernel(int *out, long long n, int v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = v;
+}
+
+}  // namespace
+
+// Decode one stream (device words/table) into n ints at out.  Synchronizes
+// the stream between rounds.  Returns 0 on success, 1 malformed stream,
+// -1 CUDA error.  Scratch comes from `ws` (decode_workspace_bytes).  A
+// one-node table whose symbol is not the zero-run key codes every element
+// with zero bits: fill_value() handles that case.
+size_t decode_workspace_bytes(long long nWords) {
+  const long long nSub = (nWords * 32 + kSubBits - 1) / kSubBits + 1;
+  return (size_t)nSub * 8 * 4 + 4096 * 4 + 256 + 64;
+}
+
+int decode_stream(const uint32_t *words, long long nWords, const int *table, int nTable,
+                  int dupKey, int dupValue, int binCount, long long n, int *out, void *ws,
+                  int *hostFlags, cudaStream_t s) {
+  const long long nSub = (nWords * 32 + kSubBits - 1) / kSubBits > 0
+                             ? (nWords * 32 + kSubBits - 1) / kSubBits : 1;
+  char *p = static_cast<char *>(ws);
+  DecCub *dc = reinterpret_cast<DecCub *>(p); p += 256;
+  unsigned *lut = reinterpret_cast<unsigned *>(p); p += 4096 * 4;
+  long long *start = reinterpret_cast<long long *>(p); p += nSub * 8;
+  long long *exitPos = reinterpret_cast<long long *>(p); p += nSub * 16;
+  long long *elems = reinterpret_cast<long long *>(p); p += nSub * 8;
+  long long *total = reinterpret_cast<long long *>(p); p += 8;
+  int *flags = reinterpret_cast<int *>(p);
+  DecCub c;
+  c.words = words; c.nWords = nWords; c.table = table; c.nTable = nTable;
+  c.dupKey = dupKey; c.dupValue = dupValue; c.binCount = binCount; c.n = n; c.out = out;
+  c.subBase = 0; c.nSub = nSub; c.lutOff = 0;
+  if (cudaMemcpyAsync(dc, &c, sizeof c, cudaMemcpyHostToDevice, s) != cudaSuccess) return -1;
+  build_lut_kernel<<<1, 1024, 0, s>>>(dc, lut);
+  const unsigned grid = (unsigned)((nSub + kThreads - 1) / kThreads);
+  constexpr int kRounds = 6;
+  int round = 0;
+  cudaMemsetAsync(flags, 0, 8, s);
+  spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, 0);
+  bool converged = false;
+  for (round = 1; round <= kRounds; round++) {
+    cudaMemsetAsync(flags, 0, 4, s);
+    spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, round);
+    cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (hostFlags[0] == 0) { converged = true; break; }
+  }
+  if (!converged) {
+    round = kRounds;
+    seq_fix_kernel<<<1, 1, 0, s>>>(dc, lut, start, exitPos, elems, round & 1, flags);
+    cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  }
+  if (hostFlags[1]) return 1;
+  elem_scan_kernel<<<1, 1024, 0, s>>>(dc, elems, total);
+  cudaMemcpyAsync(hostFlags + 2, total, 8, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  long long got;
+  memcpy(&got, hostFlags + 2, 8);
+  if (got < n) return 1;  // the reference stops with fewer values than the cubelet holds
+  write_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, round);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+void fill_value(int *out, long long n, int v, cudaStream_t s) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  fill_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, s>>>(out, n, v);
+}
+
+}  // namespace wl

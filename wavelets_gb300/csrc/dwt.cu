@@ -397,19 +397,20 @@ void launch_dwt_pass(const PassDesc *p, const int *tp, int n, int tiles, int sme
 namespace wl {
 namespace {
 __global__ void dequant_kernel(const int *__restrict__ bins, const float *__restrict__ table,
-                               float *__restrict__ out, long long n) {
+                               float *__restrict__ out, long long n, int nTable) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    out[i] = table[bins[i]];
+    out[i] = table[min(max(bins[i], 0), nTable - 1)];
 }
 }  // namespace
 
 // bins -> dequantized values through a per-bin table (dequantize,
 // test_compress_common.cc:567-584; the table holds the reference's values)
-void launch_dequant(const int *bins, const float *table, float *out, long long n, cudaStream_t s) {
+void launch_dequant(const int *bins, const float *table, float *out, long long n, int nTable,
+                    cudaStream_t s) {
   long long blocks = (n + 255) / 256;
   if (blocks > 152 * 64) blocks = 152 * 64;
   if (blocks < 1) blocks = 1;
-  dequant_kernel<<<(unsigned)blocks, 256, 0, s>>>(bins, table, out, n);
+  dequant_kernel<<<(unsigned)blocks, 256, 0, s>>>(bins, table, out, n, nTable);
 }
 }  // namespace wl

@@ -84,8 +84,8 @@ struct wl_ctx {
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, codes, codeLen, decode,
-      words, passes, logHdr, outbuf;
-  HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals;
+      words, passes, logHdr, outbuf, decWords, decTable, decWs;
+  HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   cudaEvent_t ev[7] = {};
   float timings[6] = {0, 0, 0, 0, 0, 0};
   bool profiling = false;
@@ -593,60 +593,12 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 }
 
 // ---- decompression -----------------------------------------------------------
-// Table walk of HuffmanDecoder::decodeFromStream (huffman.h:96-131) on the
-// host.  A one-node table codes its symbol with zero bits.
-wl_status huffman_decode_host(wl_ctx *ctx, const wl_result *r, long long n, int *out) {
-  const uint32_t *w = r->words;
-  const long long total = (long long)r->n_words * 32;
-  const int *t = r->decode;
-  const int nt = r->n_decode;
-  if (nt < 2) return fail(ctx, WL_EFORMAT, "empty Huffman decode table");
-  if (r->dup_key >= 0 && (r->dup_value < 0 || r->dup_value >= r->bin_count))
-    return fail(ctx, WL_EFORMAT, "zero-run value out of range");
-  long long pos = 0, i = 0;
-  auto bit = [&](long long p) -> unsigned {
-    return p < total ? (w[p >> 5] >> (p & 31)) & 1u : 0u;
-  };
-  auto emit_run = [&](unsigned e) {
-    long long L = 1LL << (e + 3);
-    while (L-- > 0 && i < n) out[i++] = r->dup_value;
-  };
-  if (nt == 2 && t[0] == 0) {
-    if (t[1] != r->dup_key) { for (; i < n; i++) out[i] = t[1]; return WL_OK; }
-    while (i < n && pos + 3 <= total) {
-      unsigned e = bit(pos) | (bit(pos + 1) << 1) | (bit(pos + 2) << 2);
-      pos += 3;
-      emit_run(e);
-    }
-  } else {
-    while (i < n && pos < total) {
-      int node = 0;
-      while (true) {
-        const int nx = t[node + (int)bit(pos++)] * 2;
-        if (nx < 0 || nx + 1 >= nt) return fail(ctx, WL_EFORMAT, "corrupt Huffman stream");
-        node = nx;
-        if (t[node] == 0) break;
-      }
-      const int v = t[node + 1];
-      if (v == r->dup_key && r->dup_key >= 0) {
-        unsigned e = bit(pos) | (bit(pos + 1) << 1) | (bit(pos + 2) << 2);
-        pos += 3;
-        emit_run(e);
-      } else {
-        if (v < 0 || v >= r->bin_count) return fail(ctx, WL_EFORMAT, "symbol out of range");
-        out[i++] = v;
-      }
-    }
-  }
-  if (i != n) return fail(ctx, WL_EFORMAT, "stream holds %lld of %lld values", i, n);
-  return WL_OK;
-}
-
 }  // namespace
 
 // dequantize kernel launcher lives in dwt.cu
 namespace wl {
-void launch_dequant(const int *bins, const float *table, float *out, long long n, cudaStream_t s);
+void launch_dequant(const int *bins, const float *table, float *out, long long n, int nTable,
+                    cudaStream_t s);
 }
 
 namespace {
@@ -729,8 +681,15 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
   if (r->size[0] > kMaxAxis || r->size[1] > kMaxAxis || r->size[2] > kMaxAxis)
     return fail(ctx, WL_EINVAL, "axis length above %d", kMaxAxis);
   if (r->bin_count < 2 || r->bin_count > kMaxBins) return fail(ctx, WL_EFORMAT, "bad bin count");
-  std::vector<int> bins((size_t)n);
-  TRY(huffman_decode_host(ctx, r, n, bins.data()));
+  if (r->n_decode < 2 || !r->decode) return fail(ctx, WL_EFORMAT, "empty Huffman decode table");
+  if (r->dup_key >= 0 && (r->dup_value < 0 || r->dup_value >= r->bin_count))
+    return fail(ctx, WL_EFORMAT, "zero-run value out of range");
+  for (int i = 0; i < r->n_decode; i += 2) {  // every entry must be a node or a symbol
+    const int a = r->decode[i], b = r->decode[i + 1];
+    if (a == 0 ? (b < 0 || (b >= r->bin_count && b != r->dup_key))
+               : (a < 0 || 2 * a >= r->n_decode || b < 0 || 2 * b >= r->n_decode))
+      return fail(ctx, WL_EFORMAT, "corrupt Huffman decode table");
+  }
   std::vector<float> dq(r->bin_count);
   if (r->quant_alg == WL_LLOYD && (!r->values || r->n_values != r->bin_count))
     return fail(ctx, WL_EFORMAT, "codebook values missing");
@@ -740,11 +699,26 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
   TRY(ensure(ctx, ctx->coef2, padded * 4));
   TRY(ensure(ctx, ctx->bins, padded * 4));  // int bins for the dequant kernel
   TRY(ensure(ctx, ctx->dqtable, (size_t)kMaxBins * 4));
+  TRY(ensure(ctx, ctx->decWords, (size_t)r->n_words * 4 + 16));
+  TRY(ensure(ctx, ctx->decTable, (size_t)r->n_decode * 4 + 16));
+  TRY(ensure(ctx, ctx->decWs, decode_workspace_bytes(r->n_words)));
+  TRY(ensure_host(ctx, ctx->hFlags, 64));
   cudaStream_t s = ctx->stream;
-  CU(cudaMemcpyAsync(ctx->bins.p, bins.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->decWords.p, r->words, (size_t)r->n_words * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->decTable.p, r->decode, (size_t)r->n_decode * 4, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(ctx->dqtable.p, dq.data(), dq.size() * 4, cudaMemcpyHostToDevice, s));
+  if (r->n_decode == 2 && r->decode[0] == 0 && r->decode[1] != r->dup_key) {
+    fill_value(P<int>(ctx->bins), n, r->decode[1], s);  // one symbol, zero-length code
+  } else {
+    const int rc = decode_stream(P<uint32_t>(ctx->decWords), r->n_words, P<int>(ctx->decTable),
+                                 r->n_decode, r->dup_key, r->dup_value, r->bin_count, n,
+                                 P<int>(ctx->bins), ctx->decWs.p, H<int>(ctx->hFlags), s);
+    if (rc < 0) return fail(ctx, WL_ECUDA, "decode failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc > 0) return fail(ctx, WL_EFORMAT, "corrupt Huffman stream");
+  }
   ctx->launches = 1;
-  launch_dequant(P<int>(ctx->bins), P<float>(ctx->dqtable), P<float>(ctx->coef), n, s);
+  launch_dequant(P<int>(ctx->bins), P<float>(ctx->dqtable), P<float>(ctx->coef), n,
+                 r->bin_count, s);
   CU(cudaGetLastError());
   return inverse_impl(ctx, r->size, r->steps, r->wavelet, r->original_size, outType, out,
                       outOnDevice);
@@ -832,10 +806,11 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
-                   &ctx->logHdr, &ctx->outbuf};
+                   &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
   HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses, &ctx->hCub,
-                    &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals};
+                    &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals,
+                    &ctx->hFlags};
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
   for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
   for (auto &e : ctx->pev) if (e) cudaEventDestroy(e);

@@ -190,6 +190,13 @@ void launch_runs(DevBatch &b, cudaStream_t s);
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);
 void launch_encode(DevBatch &b, cudaStream_t s);
 
+// GPU Huffman decoding (decode.cu)
+size_t decode_workspace_bytes(long long nWords);
+int decode_stream(const uint32_t *words, long long nWords, const int *table, int nTable,
+                  int dupKey, int dupValue, int binCount, long long n, int *out, void *ws,
+                  int *hostFlags, cudaStream_t s);
+void fill_value(int *out, long long n, int v, cudaStream_t s);
+
 // host-side exact log-quantizer tables (quant_host.cpp)
 struct LogTable {
   std::vector<float> bounds;   // see quant_host.cpp for the layout
