@@ -53,6 +53,12 @@ constexpr float kInvSqrt2 = 0.70710678118654752440f;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 
+// Shared-memory position of row element p: one pad word after every 32, so
+// the power-of-two strides of the in-place levels hit distinct banks.
+__host__ __device__ __forceinline__ int sw(int p) { return p + (p >> 5); }
+// odd row pitch, so a warp reading one element of 32 rows is conflict-free
+__host__ __device__ __forceinline__ int row_pitch(int L) { return sw(L) | 1; }
+
 // whole-sample mirror with repeated folding (dwt_cpu.h:162-176)
 __device__ __forceinline__ int mirror(int i, int n) {
   if (i < 0) i = -i;
@@ -93,7 +99,7 @@ __device__ __forceinline__ int band_to_pos(int q, int L, int S, int &lev) {
 }
 
 // ---- one level of one row --------------------------------------------------
-// A level runs on the strided view row[j*st], j < n = 2*half.  The lanes of a
+// A level runs on the strided view row[sw(j*st)], j < n = 2*half.  The lanes of a
 // warp are split into groups of G lanes (G = 32, or the power of two >= half
 // when half < 32) so several short rows share a warp; `sub` is the lane's
 // index in its group and `ok` whether the group has a row.  Every lane of
@@ -103,26 +109,26 @@ __device__ __forceinline__ void fwd_lifting_level(float *row, int half, int st, 
                                                   int G, bool ok) {
   if (ok)
     for (int i = sub; i < half; i += G) {  // d += alpha (s_i + s_i+1)
-      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
-      row[(2 * i + 1) * st] += kAlpha * (a + b);
+      const float a = row[sw((2 * i) * st)], b = row[sw((2 * min(i + 1, half - 1)) * st)];
+      row[sw((2 * i + 1) * st)] += kAlpha * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {  // s += beta (d_i-1 + d_i)
-      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
-      row[(2 * i) * st] += kBeta * (a + b);
+      const float a = row[sw((2 * max(i - 1, 0) + 1) * st)], b = row[sw((2 * i + 1) * st)];
+      row[sw((2 * i) * st)] += kBeta * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
-      row[(2 * i + 1) * st] += kGamma * (a + b);
+      const float a = row[sw((2 * i) * st)], b = row[sw((2 * min(i + 1, half - 1)) * st)];
+      row[sw((2 * i + 1) * st)] += kGamma * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
-      row[(2 * i) * st] += kDelta * (a + b);
+      const float a = row[sw((2 * max(i - 1, 0) + 1) * st)], b = row[sw((2 * i + 1) * st)];
+      row[sw((2 * i) * st)] += kDelta * (a + b);
     }
   __syncwarp();
 }
@@ -131,26 +137,26 @@ __device__ __forceinline__ void inv_lifting_level(float *row, int half, int st, 
                                                   int G, bool ok) {
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
-      row[(2 * i) * st] -= kDelta * (a + b);
+      const float a = row[sw((2 * max(i - 1, 0) + 1) * st)], b = row[sw((2 * i + 1) * st)];
+      row[sw((2 * i) * st)] -= kDelta * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
-      row[(2 * i + 1) * st] -= kGamma * (a + b);
+      const float a = row[sw((2 * i) * st)], b = row[sw((2 * min(i + 1, half - 1)) * st)];
+      row[sw((2 * i + 1) * st)] -= kGamma * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * max(i - 1, 0) + 1) * st], b = row[(2 * i + 1) * st];
-      row[(2 * i) * st] -= kBeta * (a + b);
+      const float a = row[sw((2 * max(i - 1, 0) + 1) * st)], b = row[sw((2 * i + 1) * st)];
+      row[sw((2 * i) * st)] -= kBeta * (a + b);
     }
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * i) * st], b = row[(2 * min(i + 1, half - 1)) * st];
-      row[(2 * i + 1) * st] -= kAlpha * (a + b);
+      const float a = row[sw((2 * i) * st)], b = row[sw((2 * min(i + 1, half - 1)) * st)];
+      row[sw((2 * i + 1) * st)] -= kAlpha * (a + b);
     }
   __syncwarp();
 }
@@ -160,13 +166,13 @@ __device__ __forceinline__ void haar_level(float *row, int half, int st, int sub
                                            bool ok, bool inverse) {
   if (ok)
     for (int i = sub; i < half; i += G) {
-      const float a = row[(2 * i) * st], b = row[(2 * i + 1) * st];
+      const float a = row[sw((2 * i) * st)], b = row[sw((2 * i + 1) * st)];
       if (!inverse) {
-        row[(2 * i + 1) * st] = __fmul_rn(__fsub_rn(a, b), kInvSqrt2);
-        row[(2 * i) * st] = __fmul_rn(__fadd_rn(a, b), kInvSqrt2);
+        row[sw((2 * i + 1) * st)] = __fmul_rn(__fsub_rn(a, b), kInvSqrt2);
+        row[sw((2 * i) * st)] = __fmul_rn(__fadd_rn(a, b), kInvSqrt2);
       } else {
-        row[(2 * i) * st] = __fmul_rn(kInvSqrt2, __fadd_rn(a, b));
-        row[(2 * i + 1) * st] = __fmul_rn(kInvSqrt2, __fsub_rn(a, b));
+        row[sw((2 * i) * st)] = __fmul_rn(kInvSqrt2, __fadd_rn(a, b));
+        row[sw((2 * i + 1) * st)] = __fmul_rn(kInvSqrt2, __fsub_rn(a, b));
       }
     }
   __syncwarp();
@@ -178,7 +184,7 @@ __device__ __forceinline__ void exact_level(float *row, float *tmp, int half, in
                                             int G, bool ok, bool inverse) {
   const int n = 2 * half;
   if (ok)
-    for (int j = sub; j < n; j += G) tmp[j] = row[j * st];
+    for (int j = sub; j < n; j += G) tmp[j] = row[sw(j * st)];
   __syncwarp();
   if (ok)
     for (int i = sub; i < half; i += G) {
@@ -205,8 +211,8 @@ __device__ __forceinline__ void exact_level(float *row, float *tmp, int half, in
         d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 3, n)], tmp[mirror(k - 3, n)]), kSH3));
         d = __fadd_rn(d, __fmul_rn(__fadd_rn(tmp[mirror(k + 4, n)], tmp[mirror(k - 4, n)]), kSH4));
       }
-      row[j * st] = s;
-      row[k * st] = d;
+      row[sw(j * st)] = s;
+      row[sw(k * st)] = d;
     }
   __syncwarp();
 }
@@ -243,7 +249,7 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
     if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
   }
   const PassDesc &d = passes[lo];
-  const int L = d.L, S = d.steps, T = d.T, pitch = L + 1;
+  const int L = d.L, S = d.steps, T = d.T, pitch = row_pitch(L);
   const int r0 = (bid - tilePrefix[lo]) * T;
   const int nr = min(T, d.rows - r0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -276,13 +282,13 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       float *trow = tile + rr * pitch;
       if (!INV) {
         const int cl = d.clampL - 1;
-        for (int c = sub; c < L; c += G) trow[c] = load_as_float(src + min(c, cl));
+        for (int c = sub; c < L; c += G) trow[sw(c)] = load_as_float(src + min(c, cl));
       } else {
         for (int q = sub; q < L; q += G) {
           int lev;
           const int p = band_to_pos(q, L, S, lev);
           const float v = load_as_float(src + q);
-          trow[p] = lifting ? v / scaleTab[lev] : v;
+          trow[sw(p)] = lifting ? v / scaleTab[lev] : v;
         }
       }
     }
@@ -322,9 +328,9 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       if (!INV) {
         int lev;
         const int p = band_to_pos(q, L, S, lev);
-        v = tile[rr * pitch + p] * scaleTab[lev];
+        v = tile[rr * pitch + sw(p)] * scaleTab[lev];
       } else {
-        v = tile[rr * pitch + q];
+        v = tile[rr * pitch + sw(q)];
       }
       store_from_float(out + base + (long long)q * d.outSC, v);
     }
@@ -341,9 +347,9 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
         if (!INV) {
           int lev;
           const int p = band_to_pos(q, L, S, lev);
-          v = tile[rr * pitch + p] * scaleTab[lev];
+          v = tile[rr * pitch + sw(p)] * scaleTab[lev];
         } else {
-          v = tile[rr * pitch + q];
+          v = tile[rr * pitch + sw(q)];
         }
         store_from_float(out + base + (long long)q * d.outSC, v);
       }
@@ -362,14 +368,14 @@ void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, cuda
 }  // namespace
 
 int dwt_tile_rows(int L, bool exact) {
-  const int per_row = (L + 1) + (exact ? L : 0);
+  const int per_row = row_pitch(L) + (exact ? L : 0);
   int T = 1;
   while (T * 2 * per_row <= kTileBudget && T < 256) T *= 2;
   return T;
 }
 
 int dwt_smem_bytes(int L, int T, bool exact) {
-  return (T * (L + 1) + (exact ? T * L : 0)) * (int)sizeof(float);
+  return (T * row_pitch(L) + (exact ? T * L : 0)) * (int)sizeof(float);
 }
 
 // inType/outType: wl_dtype codes (F32 for intermediate passes)

@@ -84,7 +84,7 @@ struct wl_ctx {
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, codes, codeLen, decode,
-      words, passes, logHdr, outbuf, decWords, decTable, decWs;
+      words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
   HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   cudaEvent_t ev[7] = {};
   float timings[6] = {0, 0, 0, 0, 0, 0};
@@ -342,6 +342,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->decode, (size_t)n * 4 * kMaxSymbols * 4));
   TRY(ensure(ctx, ctx->words, wordsTotal * 4));
   TRY(ensure(ctx, ctx->logHdr, n * sizeof(int4)));
+  TRY(ensure(ctx, ctx->meta, (size_t)n * (4 * kMaxSymbols + 2 * kMaxBins) * 4));
   const size_t passBytes = (size_t)3 * n * (sizeof(PassDesc) + sizeof(int)) + 8 * 4096;
   TRY(ensure(ctx, ctx->passes, passBytes));
   TRY(ensure_host(ctx, ctx->hPasses, passBytes));
@@ -419,6 +420,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.words = P<uint32_t>(ctx->words);
   b.chunkPrefix = P<long long>(ctx->chunkPrefix);
   b.logHdr = P<int4>(ctx->logHdr);
+  b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
 
   // ---- transform ----
@@ -494,7 +496,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[4], s));
   launch_encode(b, s);
-  ctx->launches += 5;
+  launch_pack_meta(b, s);
+  ctx->launches += 6;
   mark(ctx, 9);
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[5], s));
@@ -505,37 +508,26 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   CU(cudaStreamSynchronize(s));
   const CubeletState *hs = H<CubeletState>(ctx->hState);
   long long totalWords = 0;
-  size_t decodeInts = 0;
   for (int i = 0; i < n; i++) {
     if (hs[i].error)
       return fail(ctx, WL_EINVAL, "cubelet %d: device error %d (code too long or output overflow)",
                   i, hs[i].error);
     totalWords += hs[i].nWords;
-    decodeInts += hs[i].nDecode;
   }
   TRY(ensure_host(ctx, ctx->hWords, (size_t)totalWords * 4));
-  TRY(ensure_host(ctx, ctx->hDecode, decodeInts * 4 + (size_t)n * 2 * kMaxBins * 4));
+  size_t metaInts = 0;
+  for (int i = 0; i < n; i++)
+    metaInts += hs[i].nDecode + (plans[i].p.quant_alg == WL_LLOYD ? hs[i].nBounds + hs[i].nValues : 0);
+  TRY(ensure_host(ctx, ctx->hDecode, metaInts * 4 + 16));
   if (totalWords)
     CU(cudaMemcpyAsync(ctx->hWords.p, b.words, (size_t)totalWords * 4, cudaMemcpyDeviceToHost, s));
+  if (metaInts)
+    CU(cudaMemcpyAsync(ctx->hDecode.p, b.meta, metaInts * 4, cudaMemcpyDeviceToHost, s));
   int *hd = H<int>(ctx->hDecode);
-  size_t doff = 0;
   std::vector<size_t> decOff(n), cbOff(n, 0);
   for (int i = 0; i < n; i++) {
-    decOff[i] = doff;
-    if (hs[i].nDecode)
-      CU(cudaMemcpyAsync(hd + doff, b.decode + (size_t)i * 4 * kMaxSymbols,
-                         (size_t)hs[i].nDecode * 4, cudaMemcpyDeviceToHost, s));
-    doff += hs[i].nDecode;
-  }
-  for (int i = 0; i < n; i++) {
-    if (plans[i].p.quant_alg != WL_LLOYD) continue;
-    cbOff[i] = doff;
-    CU(cudaMemcpyAsync(hd + doff, b.qtable + plans[i].tableOff, (size_t)hs[i].nBounds * 4,
-                       cudaMemcpyDeviceToHost, s));
-    doff += hs[i].nBounds;
-    CU(cudaMemcpyAsync(hd + doff, b.dqtable + (size_t)i * kMaxBins, (size_t)hs[i].nValues * 4,
-                       cudaMemcpyDeviceToHost, s));
-    doff += hs[i].nValues;
+    decOff[i] = (size_t)hs[i].metaBase;
+    cbOff[i] = (size_t)hs[i].metaBase + hs[i].nDecode;
   }
   CU(cudaEventRecord(ctx->ev[6], s));
   CU(cudaStreamSynchronize(s));
@@ -806,7 +798,8 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
-                   &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs};
+                   &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
+                   &ctx->meta};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
   HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses, &ctx->hCub,
                     &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals,

@@ -361,13 +361,33 @@ __global__ void __launch_bounds__(1024) encode_scan_kernel(DevBatch b) {
   }
 }
 
-// packed word offset of every cubelet (one thread; n is small)
+// packed word and metadata offsets of every cubelet (one thread; n is small)
 __global__ void cubelet_offsets_kernel(DevBatch b) {
-  long long off = 0;
+  long long off = 0, moff = 0;
   for (int i = 0; i < b.n; i++) {
     CubeletState *st = b.state + i;
     st->wordsBase = off;
     off += st->error ? 0 : st->nWords;
+    st->metaBase = moff;
+    moff += st->nDecode + (b.cub[i].quantAlg == WL_LLOYD ? st->nBounds + st->nValues : 0);
+  }
+}
+
+// decode table and Lloyd codebook of every cubelet into one buffer
+__global__ void pack_meta_kernel(DevBatch b) {
+  const int ci = blockIdx.x;
+  const CubeletState *st = b.state + ci;
+  const CubeletDev cd = b.cub[ci];
+  int *m = b.meta + st->metaBase;
+  const int *dec = b.decode + (size_t)ci * 4 * kMaxSymbols;
+  for (int i = threadIdx.x; i < st->nDecode; i += blockDim.x) m[i] = dec[i];
+  if (cd.quantAlg == WL_LLOYD) {
+    const float *bnd = b.qtable + cd.tableOff;
+    const float *val = b.dqtable + (size_t)ci * kMaxBins;
+    for (int i = threadIdx.x; i < st->nBounds; i += blockDim.x)
+      m[st->nDecode + i] = __float_as_int(bnd[i]);
+    for (int i = threadIdx.x; i < st->nValues; i += blockDim.x)
+      m[st->nDecode + st->nBounds + i] = __float_as_int(val[i]);
   }
 }
 
@@ -461,6 +481,8 @@ void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s) {
   cudaFuncSetAttribute(huffman_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   huffman_build_kernel<<<b.n, 1024, smem, s>>>(b);
 }
+
+void launch_pack_meta(DevBatch &b, cudaStream_t s) { pack_meta_kernel<<<b.n, 256, 0, s>>>(b); }
 
 void launch_encode(DevBatch &b, cudaStream_t s) {
   const unsigned chunks = (unsigned)b.totalChunks;

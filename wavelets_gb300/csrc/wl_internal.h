@@ -118,6 +118,7 @@ struct CubeletState {
   // Huffman
   unsigned long long totalBits;
   long long wordsBase;           // word offset of this cubelet in the packed output
+  long long metaBase;            // int offset of its decode table (+ codebook) in the packed metadata
   int nWords;
   int longest;
   int nDecode;
@@ -167,6 +168,7 @@ struct DevBatch {
   uint32_t *words;                // Huffman output
   long long *chunkPrefix;         // [n+1] chunk prefix (== cub[i].chunkBase)
   int4 *logHdr;                   // [n] log table layout from the host
+  int *meta;                      // packed decode tables and Lloyd codebooks
   long long totalChunks;
 };
 
@@ -189,6 +191,7 @@ void launch_runs(DevBatch &b, cudaStream_t s);
 // launchers (huffman.cu)
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);
 void launch_encode(DevBatch &b, cudaStream_t s);
+void launch_pack_meta(DevBatch &b, cudaStream_t s);
 
 // GPU Huffman decoding (decode.cu)
 size_t decode_workspace_bytes(long long nWords);
