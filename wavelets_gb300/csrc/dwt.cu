@@ -25,17 +25,12 @@
 // reference's own butterfly (a +- b) * (1/sqrt 2) (dwt_cpu.cc:159-162).
 #include <cuda_runtime.h>
 
+#include "dwt_common.cuh"
 #include "wl_internal.h"
 
 namespace wl {
 namespace {
-
-// lifting factorisation of the CDF 9/7 analysis filters
-constexpr float kAlpha = -1.586134342059924f;
-constexpr float kBeta = -0.052980118572961f;
-constexpr float kGamma = 0.882911075530934f;
-constexpr float kDelta = 0.443506852043971f;
-constexpr double kK = 1.149604398860241;
+using namespace dwtc;
 
 // reference taps (dwt_cpu.cc:15-43), double literals rounded to float
 constexpr float kL0 = (float).85269867900940, kL1 = (float).377402855612650,
@@ -48,7 +43,6 @@ constexpr float kSL0 = (float).788485616405660, kSL1 = (float).377402855612650,
 constexpr float kSH0 = (float)-.85269867900940, kSH1 = (float).418092273222210,
                 kSH2 = (float).110624404418420, kSH3 = (float)-.064538882628938,
                 kSH4 = (float)-.037828455506995;
-constexpr float kInvSqrt2 = 0.70710678118654752440f;
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
@@ -67,25 +61,6 @@ __device__ __forceinline__ int mirror(int i, int n) {
     if (i < 0) i = -i;
   }
   return i;
-}
-
-template <typename T> __device__ __forceinline__ float load_as_float(const T *p) {
-  return (float)(*p);
-}
-
-template <typename T> __device__ __forceinline__ void store_from_float(T *p, float f);
-template <> __device__ __forceinline__ void store_from_float<float>(float *p, float f) { *p = f; }
-// ByteInputDataUnchanged::floatToByte (wavelet.h:155-163)
-template <> __device__ __forceinline__ void store_from_float<uint8_t>(uint8_t *p, float f) {
-  *p = f <= 0.f ? (uint8_t)0 : (f >= 255.f ? (uint8_t)255 : (uint8_t)f);
-}
-// IntInputDataUnchanged::floatToInt (wavelet.h:210-212)
-template <> __device__ __forceinline__ void store_from_float<int32_t>(int32_t *p, float f) {
-  *p = (int)__fadd_rn(f, 0.5f);
-}
-template <> __device__ __forceinline__ void store_from_float<uint16_t>(uint16_t *p, float f) {
-  int v = (int)__fadd_rn(f, 0.5f);
-  *p = (uint16_t)(v < 0 ? 0 : (v > 65535 ? 65535 : v));
 }
 
 // band index q (reference order) -> in-place position p and level
@@ -223,14 +198,6 @@ __device__ __forceinline__ int group_width(int len) {
   int G = 1;
   while (G < len) G <<= 1;
   return G;
-}
-
-// per-level store scale of the lifting form: index t < S detail, t == S low
-__device__ __forceinline__ float lifting_scale(int t, int S) {
-  double k = 1.0;
-  if (t == S) { for (int i = 0; i < S; i++) k *= kK; return (float)k; }
-  for (int i = 0; i < t; i++) k *= kK;
-  return (float)(-k / kK);
 }
 
 template <typename InT, typename OutT, bool INV>

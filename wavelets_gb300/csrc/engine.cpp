@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "cubelet_io.h"
@@ -35,6 +36,12 @@ struct HostBuf {
   size_t cap = 0;
 };
 
+int ceil_log2_int(int v) {
+  int k = 0;
+  while ((1 << k) < v) k++;
+  return k;
+}
+
 // Per-cubelet plan computed on the host.
 struct Plan {
   const void *data;
@@ -51,7 +58,23 @@ struct Plan {
   long long wordsCap;
   int tableOff;
   bool identity;       // all steps zero: no transform, no axis rotation
+  bool cols;           // transform runs on the column-tile kernel
 };
+
+// Column-tile kernel for every lifting / Haar cubelet whose padded axes fit
+// its tile; exact-order CDF 9/7 and longer rows use the row-cooperative one.
+bool use_cols(int Xp, int Yp, int Zp, bool identity, const wl_params &p) {
+  if (identity || (p.exact_transform && p.wavelet == WL_CDF97)) return false;
+  return Xp <= kColsMaxL && Yp <= kColsMaxL && Zp <= kColsMaxL;
+}
+
+// Launch groups of one transform phase, keyed by (kernel, source type, row
+// length class): a launch's shared memory is sized for its longest row, so
+// rows of very different lengths go to different launches.
+using PassGroups = std::map<int, std::vector<PassDesc>>;
+int group_key(bool cols, int dtype, int L) {
+  return ((cols ? 1 : 0) << 12) | (dtype << 8) | (cols ? ceil_log2_int(L) : 0);
+}
 
 int dtype_size(int dt) {
   switch (dt) {
@@ -174,9 +197,61 @@ wl_status check_params(wl_ctx *ctx, const wl_params &p) {
 }
 
 // Build PassDescs for one cubelet's forward transform.
+// Column-tile layouts: x pass [raw x-y-z] -> z-y-x, y pass z-y-x -> z-x-y,
+// z pass z-x-y in place (a-b-c lists axes from fastest to slowest).  Rows
+// are numbered so that neighbouring rows are neighbours in memory on every
+// side whose element stride is not 1.
+void forward_passes_cols(const Plan &pl, const void *in, float *coef, float *coef2,
+                         PassGroups &xs, PassGroups &ys, PassGroups &zs) {
+  const int big = 0x7fffffff;
+  const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
+  float *o = coef + pl.coefOff;
+  float *o2 = coef2 + pl.coefOff;
+  const int T = dwt_cols_tile_rows();
+  PassDesc d;
+  memset(&d, 0, sizeof d);
+  d.cropL = d.cropB = d.cropA = big;
+  d.wavelet = pl.p.wavelet;
+  // x pass: rows (a = y, b = z), REPEAT padding by clamping
+  d.in = in;
+  d.inSA = pl.X; d.inSB = (long long)pl.X * pl.Y; d.inSC = 1;
+  d.clampL = pl.X; d.clampA = pl.Y; d.clampB = pl.Z;
+  d.L = pl.Xp; d.B = pl.Zp; d.rows = (int)(Yp * Zp);
+  d.out = o2;
+  d.outSA = Zp; d.outSB = 1; d.outSC = Zp * Yp;
+  d.steps = pl.sx;
+  d.T = T; d.tiles = (d.rows + T - 1) / T;
+  xs[group_key(true, pl.dtype, d.L)].push_back(d);
+  // y pass: rows (a = x, b = z) of z-y-x -> z-x-y
+  PassDesc e = d;
+  e.clampL = e.clampB = e.clampA = big;
+  e.in = o2;
+  e.inSA = Zp * Yp; e.inSB = 1; e.inSC = Zp;
+  e.L = pl.Yp; e.B = pl.Zp; e.rows = (int)(Zp * Xp);
+  e.out = o;
+  e.outSA = Zp; e.outSB = 1; e.outSC = Zp * Xp;
+  e.steps = pl.sy;
+  e.tiles = (e.rows + T - 1) / T;
+  ys[group_key(true, WL_F32, e.L)].push_back(e);
+  if (pl.sz == 0) return;
+  // z pass: rows (a = y, b = x) of z-x-y, in place
+  PassDesc f = e;
+  f.in = o;
+  f.inSA = Zp * Xp; f.inSB = Zp; f.inSC = 1;
+  f.L = pl.Zp; f.B = pl.Xp; f.rows = (int)(Xp * Yp);
+  f.out = o;
+  f.outSA = Zp * Xp; f.outSB = Zp; f.outSC = 1;
+  f.steps = pl.sz;
+  f.tiles = (f.rows + T - 1) / T;
+  zs[group_key(true, WL_F32, f.L)].push_back(f);
+}
+
 void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
-                    std::vector<PassDesc> *xs, std::vector<PassDesc> &ys,
-                    std::vector<PassDesc> &zs) {
+                    PassGroups &xs, PassGroups &ys, PassGroups &zs) {
+  if (pl.cols) {
+    forward_passes_cols(pl, in, coef, coef2, xs, ys, zs);
+    return;
+  }
   const int big = 0x7fffffff;
   const float *c = coef + pl.coefOff;
   float *o = coef + pl.coefOff;
@@ -189,6 +264,7 @@ void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
   d.in = in;
   d.inSA = (long long)pl.X * pl.Y;
   d.inSB = pl.X;
+  d.inSC = 1;
   d.clampL = pl.X; d.clampB = pl.Y; d.clampA = pl.Z;
   d.L = pl.Xp; d.B = pl.Yp; d.rows = (int)(Yp * Zp);
   d.wavelet = pl.p.wavelet; d.exact = pl.p.exact_transform;
@@ -203,7 +279,7 @@ void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
   }
   d.T = dwt_tile_rows(d.L, d.exact && d.wavelet == WL_CDF97);
   d.tiles = (d.rows + d.T - 1) / d.T;
-  xs[pl.dtype].push_back(d);
+  xs[group_key(false, pl.dtype, d.L)].push_back(d);
   if (pl.identity) return;
   // y pass: rows (x, z) of the y-z-x cube -> z-x-y
   PassDesc e;
@@ -211,14 +287,14 @@ void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
   e.cropL = e.cropB = e.cropA = big;
   e.clampL = e.clampB = e.clampA = big;
   e.in = o2;
-  e.inSA = Zp * Yp; e.inSB = Yp;
+  e.inSA = Zp * Yp; e.inSB = Yp; e.inSC = 1;
   e.L = pl.Yp; e.B = pl.Zp; e.rows = (int)(Zp * Xp);
   e.out = o;
   e.outSA = Zp; e.outSB = 1; e.outSC = Zp * Xp;
   e.steps = pl.sy; e.wavelet = pl.p.wavelet; e.exact = pl.p.exact_transform;
   e.T = dwt_tile_rows(e.L, e.exact && e.wavelet == WL_CDF97);
   e.tiles = (e.rows + e.T - 1) / e.T;
-  ys.push_back(e);
+  ys[group_key(false, WL_F32, e.L)].push_back(e);
   if (pl.sz == 0) return;
   // z pass: rows (y, x) of the z-x-y cube, in place
   PassDesc f = e;
@@ -230,12 +306,12 @@ void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
   f.steps = pl.sz;
   f.T = dwt_tile_rows(f.L, f.exact && f.wavelet == WL_CDF97);
   f.tiles = (f.rows + f.T - 1) / f.T;
-  zs.push_back(f);
+  zs[group_key(false, WL_F32, f.L)].push_back(f);
 }
 
 // Upload a group of passes (descriptor + tile prefix) and launch it.
 wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
-                    int inType, int outType, bool inverse) {
+                    int inType, int outType, bool inverse, bool cols = false) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int) + 64;
@@ -249,16 +325,30 @@ wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
   for (size_t i = 0; i < n; i++) {
     tp[i] = tiles;
     tiles += g[i].tiles;
-    smem = std::max(smem, dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
+    smem = std::max(smem, cols ? dwt_cols_smem_bytes(g[i].L)
+                               : dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
   }
   tp[n] = tiles;
   CU(cudaMemcpyAsync(d, h, bytes - 64, cudaMemcpyHostToDevice, ctx->stream));
   ctx->launches++;
-  launch_dwt_pass(reinterpret_cast<const PassDesc *>(d),
-                  reinterpret_cast<const int *>(d + n * sizeof(PassDesc)), (int)n, tiles, smem,
-                  inType, outType, inverse, ctx->stream);
+  const PassDesc *dp = reinterpret_cast<const PassDesc *>(d);
+  const int *dtp = reinterpret_cast<const int *>(d + n * sizeof(PassDesc));
+  if (cols)
+    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
+  else
+    launch_dwt_pass(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
   CU(cudaGetLastError());
   hoff += (bytes + 255) & ~(size_t)255;
+  return WL_OK;
+}
+
+wl_status run_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int outType,
+                     bool inverse) {
+  for (const auto &kv : gs) {
+    const bool cols = (kv.first >> 12) & 1;
+    const int dt = (kv.first >> 8) & 15;
+    TRY(run_group(ctx, kv.second, hoff, inverse ? WL_F32 : dt, outType, inverse, cols));
+  }
   return WL_OK;
 }
 
@@ -298,6 +388,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     pl.Yp = padded_length(pl.Y, pl.sy);
     pl.Zp = padded_length(pl.Z, pl.sz);
     pl.identity = pl.sx == 0 && pl.sy == 0 && pl.sz == 0;
+    pl.cols = use_cols(pl.Xp, pl.Yp, pl.Zp, pl.identity, pl.p);
     if (pl.Xp > kMaxAxis || pl.Yp > kMaxAxis || pl.Zp > kMaxAxis)
       return fail(ctx, WL_EINVAL, "cubelet %d: padded axis length above %d", i, kMaxAxis);
     pl.n = (long long)pl.Xp * pl.Yp * pl.Zp;
@@ -425,16 +516,16 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- transform ----
   ctx->launches = 0;
-  std::vector<PassDesc> xs[5], ys, zs;
+  PassGroups xs, ys, zs;
   for (int i = 0; i < n; i++)
     forward_passes(plans[i], dIn[i], b.coef, b.coef2, xs, ys, zs);
   size_t hoff = 0;
   mark(ctx, 0);
-  for (int dt = 1; dt <= 4; dt++) TRY(run_group(ctx, xs[dt], hoff, dt, WL_F32, false));
+  TRY(run_groups(ctx, xs, hoff, WL_F32, false));
   mark(ctx, 1);
-  TRY(run_group(ctx, ys, hoff, WL_F32, WL_F32, false));
+  TRY(run_groups(ctx, ys, hoff, WL_F32, false));
   mark(ctx, 2);
-  TRY(run_group(ctx, zs, hoff, WL_F32, WL_F32, false));
+  TRY(run_groups(ctx, zs, hoff, WL_F32, false));
   mark(ctx, 3);
   CU(cudaEventRecord(ctx->ev[1], s));
   if (coefOut) {  // transform only: hand back the coefficients of cubelet 0
@@ -614,8 +705,42 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
   float *c1 = P<float>(ctx->coef), *c2 = P<float>(ctx->coef2);
   size_t hoff = 0;
   auto mk = [&]() { PassDesc d; memset(&d, 0, sizeof d); d.cropL = d.cropB = d.cropA = big;
-                    d.clampL = d.clampB = d.clampA = big; d.wavelet = wavelet; d.exact = 0; return d; };
+                    d.clampL = d.clampB = d.clampA = big; d.wavelet = wavelet; d.exact = 0;
+                    d.inSC = 1; return d; };
   const bool exactCdf = false;
+  wl_params wp;
+  memset(&wp, 0, sizeof wp);
+  wp.wavelet = wavelet;
+  if (use_cols(Xp, Yp, Zp, identity, wp)) {
+    // column-tile layouts, the forward passes in reverse
+    const int T = dwt_cols_tile_rows();
+    if (steps[2] > 0) {  // z pass in place on z-x-y, rows (a = y, b = x)
+      PassDesc a = mk();
+      a.in = c1; a.inSA = (long long)Zp * Xp; a.inSB = Zp; a.inSC = 1;
+      a.out = c1; a.outSA = (long long)Zp * Xp; a.outSB = Zp; a.outSC = 1;
+      a.L = Zp; a.B = Xp; a.rows = Xp * Yp; a.steps = steps[2];
+      a.T = T; a.tiles = (a.rows + T - 1) / T;
+      TRY(run_group(ctx, {a}, hoff, WL_F32, WL_F32, true, true));
+    }
+    // y pass z-x-y -> z-y-x, rows (a = x, b = z)
+    PassDesc e = mk();
+    e.in = c1; e.inSA = Zp; e.inSB = 1; e.inSC = (long long)Zp * Xp;
+    e.out = c2; e.outSA = (long long)Zp * Yp; e.outSB = 1; e.outSC = Zp;
+    e.L = Yp; e.B = Zp; e.rows = Zp * Xp; e.steps = steps[1];
+    e.T = T; e.tiles = (e.rows + T - 1) / T;
+    TRY(run_group(ctx, {e}, hoff, WL_F32, WL_F32, true, true));
+    // x pass z-y-x -> x-y-z + crop + dtype, rows (a = y, b = z)
+    PassDesc x = mk();
+    x.in = c2; x.inSA = Zp; x.inSB = 1; x.inSC = (long long)Zp * Yp;
+    x.out = dst; x.outSA = X; x.outSB = (long long)X * Y; x.outSC = 1;
+    x.cropL = X; x.cropA = Y; x.cropB = Z;
+    x.L = Xp; x.B = Zp; x.rows = Yp * Zp; x.steps = steps[0];
+    x.T = T; x.tiles = (x.rows + T - 1) / T;
+    TRY(run_group(ctx, {x}, hoff, WL_F32, outType, true, true));
+    if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return WL_OK;
+  }
   if (!identity) {
     // inverse z pass: z-x-y -> y-z-x
     PassDesc a = mk();

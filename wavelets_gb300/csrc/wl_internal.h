@@ -86,6 +86,7 @@ struct PassDesc {
   const void *in;
   void *out;
   long long inSA, inSB;
+  long long inSC;                   // input element stride (column-tile kernel)
   long long outSA, outSB, outSC;
   int L;          // row length (padded)
   int B;          // rows per 'a'
@@ -178,6 +179,12 @@ void launch_dwt_pass(const PassDesc *d_passes, const int *d_tilePrefix,
                      int outType, bool inverse, cudaStream_t s);
 int dwt_tile_rows(int L, bool exact);
 int dwt_smem_bytes(int L, int T, bool exact);
+// column-tile passes (dwt_cols.cu): lifting / Haar, rows up to kColsMaxL
+constexpr int kColsMaxL = 512;
+void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int tiles,
+                     int smem, int inType, int outType, bool inverse, cudaStream_t s);
+int dwt_cols_tile_rows();
+int dwt_cols_smem_bytes(int L);
 
 // launchers (select.cu)
 void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
