@@ -540,7 +540,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- threshold ----
   launch_select(b, b.coef, s);
-  ctx->launches += 7;
+  ctx->launches += 8;
   CU(cudaGetLastError());
   mark(ctx, 4);
 
@@ -570,7 +570,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   // ---- quantize + count ----
   launch_quant_params(b, s);
   ctx->launches += 1;
-  if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 2; }
+  if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 3; }
   mark(ctx, 5);
   launch_quantize(b, b.coef, maxTable, s);
   mark(ctx, 6);

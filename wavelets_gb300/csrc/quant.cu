@@ -88,30 +88,52 @@ __device__ __forceinline__ void lloyd_range(const CubeletState *st, float &lo, f
   if (!(hi > lo)) hi = st->maxAbs;
 }
 
+// The Lloyd histogram counts threshold < |c| <= hi in bins of the |c| bit
+// pattern, (bits - lloydBase) >> lloydShift: above the threshold bucket the
+// compaction pass of the threshold select already counted them; the bucket's
+// candidates are added here once the threshold is known.
 __global__ void __launch_bounds__(kThreads)
-lloyd_hist_kernel(DevBatch b, const float *__restrict__ coef) {
+lloyd_cand_kernel(DevBatch b, const unsigned *__restrict__ cand) {
   __shared__ unsigned hist[kLloydBins];
-  const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = blockIdx.y;
   const CubeletDev cd = b.cub[ci];
-  if (cd.quantAlg != WL_LLOYD) return;
   const CubeletState *st = b.state + ci;
-  float lo, hi;
-  lloyd_range(st, lo, hi);
-  if (!(hi > lo)) return;
-  const float l0 = log2f(lo), scale = kLloydBins / (log2f(hi) - l0);
+  const unsigned n = st->candCount;
+  if (cd.quantAlg != WL_LLOYD || st->lloydDeferred || (unsigned)blockIdx.x * kThreads >= n) return;
+  const unsigned lo = __float_as_uint(st->threshold), hi = st->lloydHiBits, base = st->lloydBase;
+  const int shift = st->lloydShift;
   for (int i = threadIdx.x; i < kLloydBins; i += kThreads) hist[i] = 0;
   __syncthreads();
-  const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int len = (int)min((long long)kChunk, cd.n - start);
-  const float *src = coef + cd.coefOff + start;
-  for (int i = threadIdx.x; i < len; i += kThreads) {
-    const float a = fabsf(src[i]);
-    if (a > lo && a <= hi) {
-      int h = (int)((log2f(a) - l0) * scale);
-      h = min(max(h, 0), kLloydBins - 1);
-      atomicAdd(&hist[h], 1u);
-    }
+  const unsigned *src = cand + cd.coefOff;
+  for (unsigned i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const unsigned a = src[i];
+    if (a > lo && a <= hi) atomicAdd(&hist[(a - base) >> shift], 1u);
+  }
+  __syncthreads();
+  unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
+  for (int i = threadIdx.x; i < kLloydBins; i += kThreads)
+    if (hist[i]) atomicAdd(&g[i], hist[i]);
+}
+
+// Cubelets whose Lloyd range the select passes could not settle early (the
+// second largest |c| in the threshold bucket, or bucket 0): one pass over
+// their coefficients with the final threshold.
+__global__ void __launch_bounds__(kThreads)
+lloyd_deferred_kernel(DevBatch b, const float *__restrict__ coef) {
+  __shared__ unsigned hist[kLloydBins];
+  const int ci = blockIdx.y;
+  const CubeletDev cd = b.cub[ci];
+  const CubeletState *st = b.state + ci;
+  if (cd.quantAlg != WL_LLOYD || !st->lloydDeferred) return;
+  const unsigned lo = st->lloydBase, hi = st->lloydHiBits;
+  const int shift = st->lloydShift;
+  for (int i = threadIdx.x; i < kLloydBins; i += kThreads) hist[i] = 0;
+  __syncthreads();
+  const float *src = coef + cd.coefOff;
+  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < cd.n;
+       i += (long long)gridDim.x * kThreads) {
+    const unsigned a = __float_as_uint(src[i]) & 0x7fffffffu;
+    if (a > lo && a <= hi) atomicAdd(&hist[(a - lo) >> shift], 1u);
   }
   __syncthreads();
   unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
@@ -137,8 +159,16 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
   lloyd_range(st, lo, hi);
   const unsigned *g = reinterpret_cast<const unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
   const bool degenerate = !(hi > lo) || cbs < 1;
-  const float l0 = degenerate ? 0.f : log2f(lo);
-  const float w = degenerate ? 1.f : (log2f(hi) - l0) / kLloydBins;
+  // histogram bin i covers |c| bits [base + i 2^shift, base + (i+1) 2^shift)
+  const unsigned base = st->lloydBase;
+  const int shift = st->lloydShift;
+  const unsigned half = (1u << shift) >> 1;
+  // first bin whose centre is >= m (m > 0)
+  auto first_bin = [&](float m) {
+    const long long d = (long long)__float_as_uint(m) - (long long)base - (long long)half;
+    const long long a = d <= 0 ? 0 : (d + (1ll << shift) - 1) >> shift;
+    return (int)min(a, (long long)kLloydBins);
+  };
 
   // prefix sums of counts and count*centre; fixed order, so the codebook is
   // deterministic: each thread sums 4 consecutive bins, then a block scan
@@ -148,7 +178,7 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
     for (int j = 0; j < per; j++) {
       const int i = threadIdx.x * per + j;
       const double c = degenerate ? 0.0 : (double)g[i];
-      const double x = exp2((double)l0 + ((double)i + 0.5) * (double)w);
+      const double x = (double)__uint_as_float(base + ((unsigned)i << shift) + half);
       sc += c;
       sx += c * x;
       c4[j] = sc;
@@ -190,19 +220,8 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
     // cell i covers histogram bins [first(i), first(i+1)): first bin whose
     // centre is >= mid[i-1]
     for (int i = threadIdx.x; i < cbs; i += 1024) {
-      int a = 0, z = 0;
-      if (i > 0) {
-        const double m = log2((double)mid[i - 1]);
-        a = (int)ceil((m - l0) / w - 0.5);
-        a = min(max(a, 0), kLloydBins);
-      }
-      if (i + 1 < cbs) {
-        const double m = log2((double)mid[i]);
-        z = (int)ceil((m - l0) / w - 0.5);
-        z = min(max(z, 0), kLloydBins);
-      } else {
-        z = kLloydBins;
-      }
+      const int a = i > 0 ? first_bin(mid[i - 1]) : 0;
+      int z = i + 1 < cbs ? first_bin(mid[i]) : kLloydBins;
       if (z < a) z = a;
       const double cw = pw[z] - pw[a];
       nxt[i] = cw > 0 ? (float)((pwx[z] - pwx[a]) / cw) : cb[i];
@@ -626,7 +645,9 @@ void launch_quant_params(DevBatch &b, cudaStream_t s) {
 }
 
 void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
-  lloyd_hist_kernel<<<(unsigned)b.totalChunks, kThreads, 0, s>>>(b, coef);
+  lloyd_cand_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(
+      b, reinterpret_cast<const unsigned *>(b.coef2));
+  lloyd_deferred_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, coef);
   cudaFuncSetAttribute(lloyd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kLloydSmem);
   lloyd_solve_kernel<<<b.n, 1024, kLloydSmem, s>>>(b);
 }

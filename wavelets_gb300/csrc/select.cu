@@ -10,6 +10,13 @@
 // the coefficients that still match the prefix.  The first pass also reduces
 // min, max and the two largest |c| (the second largest feeds the Lloyd
 // codebook, test_compress_cpu.cc:422).
+//
+// Only the first pass reads the whole volume for the first digit; a second
+// full pass compacts the coefficients of the threshold's 12-bit bucket (a few
+// percent of them) into the cubelet's region of the free second coefficient
+// buffer, and the last two digits are histogrammed over those candidates
+// alone.  The compaction pass also builds the Lloyd histogram of every
+// |c| above the bucket, so the Lloyd quantizer needs no pass of its own.
 #include <cfloat>
 
 #include "wl_internal.h"
@@ -19,6 +26,7 @@ namespace {
 
 constexpr int kThreads = kChunkThreads;
 constexpr int kPerThread = kChunk / kThreads;
+static_assert(kPerThread == 16, "load_chunk assumes four float4 per thread");
 
 // float -> unsigned with the same order (for atomicMin/Max on signed values)
 __device__ __forceinline__ unsigned ord_enc(float f) {
@@ -46,9 +54,34 @@ __device__ __forceinline__ void top2_merge(unsigned &a1, unsigned &a2, unsigned 
   a2 = t2;
 }
 
-template <int PASS>
+
+// element of the chunk held in v[k] by this thread: float4 j = threadIdx.x +
+// kThreads * (k / 4), so every warp load is 512 contiguous bytes
+__device__ __forceinline__ int chunk_index(int k) {
+  return 4 * (threadIdx.x + kThreads * (k >> 2)) + (k & 3);
+}
+// all loads of the thread issued before any use; elements past len read 0
+__device__ __forceinline__ void load_chunk(const float *src, int len, float (&v)[kPerThread]) {
+  if (len == kChunk && (reinterpret_cast<size_t>(src) & 15) == 0) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+#pragma unroll
+    for (int j = 0; j < kPerThread / 4; j++) {
+      const float4 q = s4[threadIdx.x + kThreads * j];
+      v[4 * j] = q.x; v[4 * j + 1] = q.y; v[4 * j + 2] = q.z; v[4 * j + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kPerThread; k++) {
+      const int i = chunk_index(k);
+      v[k] = i < len ? src[i] : 0.f;
+    }
+  }
+}
+
+// First digit (bits 31..20 of |c|) plus min, max and the two largest |c|.
+// Each thread loads its four float4 of the chunk before using any of them.
 __global__ void __launch_bounds__(kThreads)
-select_pass(DevBatch b, const float *__restrict__ coef) {
+select_pass0(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kSelectBins];
   __shared__ unsigned sMin[kThreads / 32], sMax[kThreads / 32], sA1[kThreads / 32], sA2[kThreads / 32];
   const long long chunk = blockIdx.x;
@@ -60,51 +93,39 @@ select_pass(DevBatch b, const float *__restrict__ coef) {
   CubeletState *st = b.state + ci;
 
   for (int i = threadIdx.x; i < kSelectBins; i += kThreads) hist[i] = 0;
-  unsigned prefix = 0;
-  if (PASS > 0) prefix = st->prefix;
+  float v[kPerThread];
+  load_chunk(src, len, v);
   __syncthreads();
 
   unsigned mn = 0xffffffffu, mx = 0u, a1 = 0u, a2 = 0u;
+#pragma unroll
   for (int k = 0; k < kPerThread; k++) {
-    const int i = threadIdx.x + k * kThreads;
-    if (i >= len) break;
-    const float v = src[i];
-    const unsigned a = __float_as_uint(v) & 0x7fffffffu;
-    if (PASS == 0) {
-      atomicAdd(&hist[a >> 20], 1u);
-      mn = min(mn, ord_enc(v));
-      mx = max(mx, ord_enc(v));
-      top2_merge(a1, a2, a, 0u);
-    } else if (PASS == 1) {
-      if ((a >> 20) == prefix) atomicAdd(&hist[(a >> 8) & 0xfffu], 1u);
-    } else {
-      if ((a >> 8) == prefix) atomicAdd(&hist[a & 0xffu], 1u);
-    }
+    if (chunk_index(k) >= len) continue;
+    const unsigned a = __float_as_uint(v[k]) & 0x7fffffffu;
+    atomicAdd(&hist[a >> 20], 1u);
+    mn = min(mn, ord_enc(v[k]));
+    mx = max(mx, ord_enc(v[k]));
+    top2_merge(a1, a2, a, 0u);
   }
-  if (PASS == 0) {
-    for (int off = 16; off > 0; off >>= 1) {
-      mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-      unsigned b1 = __shfl_xor_sync(0xffffffffu, a1, off);
-      unsigned b2 = __shfl_xor_sync(0xffffffffu, a2, off);
-      top2_merge(a1, a2, b1, b2);
-    }
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sMin[w] = mn; sMax[w] = mx; sA1[w] = a1; sA2[w] = a2; }
+  for (int off = 16; off > 0; off >>= 1) {
+    mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    unsigned b1 = __shfl_xor_sync(0xffffffffu, a1, off);
+    unsigned b2 = __shfl_xor_sync(0xffffffffu, a2, off);
+    top2_merge(a1, a2, b1, b2);
   }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { sMin[w] = mn; sMax[w] = mx; sA1[w] = a1; sA2[w] = a2; }
   __syncthreads();
-  const int nb = PASS == 2 ? 256 : kSelectBins;
   unsigned *g = b.selHist + (size_t)ci * kSelectBins;
-  for (int i = threadIdx.x; i < nb; i += kThreads)
+  for (int i = threadIdx.x; i < kSelectBins; i += kThreads)
     if (hist[i]) atomicAdd(&g[i], hist[i]);
-  if (PASS == 0 && threadIdx.x == 0) {
-    for (int w = 1; w < kThreads / 32; w++) {
-      mn = min(mn, sMin[w]);
-      mx = max(mx, sMax[w]);
-      top2_merge(a1, a2, sA1[w], sA2[w]);
+  if (threadIdx.x == 0) {
+    for (int w2 = 1; w2 < kThreads / 32; w2++) {
+      mn = min(mn, sMin[w2]);
+      mx = max(mx, sMax[w2]);
+      top2_merge(a1, a2, sA1[w2], sA2[w2]);
     }
-    mn = min(mn, sMin[0]); mx = max(mx, sMax[0]);
-    top2_merge(a1, a2, sA1[0], sA2[0]);
     atomicMin(&st->minOrd, mn);
     atomicMax(&st->maxOrd, mx);
     // merge the pair into (absMax, absMax2) with a 64-bit CAS loop
@@ -120,6 +141,109 @@ select_pass(DevBatch b, const float *__restrict__ coef) {
       old = atomicCAS(pair, assumed, nv);
     } while (old != assumed);
   }
+}
+
+// Second full pass: compact the coefficients of the threshold bucket
+// (|c| >> 20 == prefix) into the cubelet's candidate region, and add every
+// |c| above the bucket to the Lloyd histogram (those are above the threshold
+// whatever its low 20 bits turn out to be).
+__global__ void __launch_bounds__(kThreads)
+select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict__ cand) {
+  __shared__ unsigned lh[kLloydBins];
+  __shared__ unsigned wCnt[kThreads / 32];
+  __shared__ unsigned sBase;
+  const long long chunk = blockIdx.x;
+  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const CubeletDev cd = b.cub[ci];
+  const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
+  const int len = (int)min((long long)kChunk, cd.n - start);
+  const float *src = coef + cd.coefOff + start;
+  CubeletState *st = b.state + ci;
+  const unsigned prefix = st->prefix;
+  const bool lloyd = cd.quantAlg == WL_LLOYD && !st->lloydDeferred;
+  const unsigned lbase = st->lloydBase, lhi = st->lloydHiBits;
+  const int lshift = st->lloydShift;
+  if (lloyd)
+    for (int i = threadIdx.x; i < kLloydBins; i += kThreads) lh[i] = 0;
+  float v[kPerThread];
+  load_chunk(src, len, v);
+  __syncthreads();
+
+  unsigned m = 0;  // candidates among this thread's values
+#pragma unroll
+  for (int k = 0; k < kPerThread; k++) {
+    const unsigned a = __float_as_uint(v[k]) & 0x7fffffffu;
+    const bool in = chunk_index(k) < len;
+    if (in && (a >> 20) == prefix) m |= 1u << k;
+    if (lloyd && in && (a >> 20) > prefix && a <= lhi) atomicAdd(&lh[(a - lbase) >> lshift], 1u);
+  }
+  // block-wide exclusive count of candidates, one reservation per block
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned cnt = __popc(m);
+  unsigned inc = cnt;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc += t;
+  }
+  if (lane == 31) wCnt[w] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned tot = 0;
+    for (int i = 0; i < kThreads / 32; i++) tot += wCnt[i];
+    sBase = tot ? atomicAdd(&st->candCount, tot) : 0u;
+  }
+  __syncthreads();
+  unsigned o = sBase + inc - cnt;
+  for (int i = 0; i < w; i++) o += wCnt[i];
+  unsigned *dst = cand + cd.coefOff;
+  while (m) {
+    const int k = __ffs(m) - 1;
+    m &= m - 1;
+    dst[o++] = __float_as_uint(v[k]) & 0x7fffffffu;
+  }
+  if (lloyd) {
+    unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
+    for (int i = threadIdx.x; i < kLloydBins; i += kThreads)
+      if (lh[i]) atomicAdd(&g[i], lh[i]);
+  }
+}
+
+// Digit histograms over the candidates: PASS 1 bits 19..8, PASS 2 bits 7..0
+// of the candidates that match the 24-bit prefix.  blockIdx.y = cubelet.
+template <int PASS>
+__global__ void __launch_bounds__(kThreads)
+cand_hist(DevBatch b, const unsigned *__restrict__ cand) {
+  __shared__ unsigned hist[kSelectBins];
+  const int ci = blockIdx.y;
+  const CubeletDev cd = b.cub[ci];
+  const CubeletState *st = b.state + ci;
+  const unsigned n = st->candCount;
+  if ((unsigned)blockIdx.x * kThreads >= n) return;
+  const unsigned prefix = st->prefix;
+  const int nb = PASS == 2 ? 256 : kSelectBins;
+  for (int i = threadIdx.x; i < nb; i += kThreads) hist[i] = 0;
+  __syncthreads();
+  const unsigned *src = cand + cd.coefOff;
+  for (unsigned i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const unsigned a = src[i];
+    if (PASS == 1) atomicAdd(&hist[(a >> 8) & 0xfffu], 1u);
+    else if ((a >> 8) == prefix) atomicAdd(&hist[a & 0xffu], 1u);
+  }
+  __syncthreads();
+  unsigned *g = b.selHist + (size_t)ci * kSelectBins;
+  for (int i = threadIdx.x; i < nb; i += kThreads)
+    if (hist[i]) atomicAdd(&g[i], hist[i]);
+}
+
+// Lloyd histogram bins for threshold < |c| <= hi: bin = (bits - base) >> shift,
+// the shift the smallest that keeps the range inside kLloydBins bins
+__device__ __forceinline__ void set_lloyd_bins(CubeletState *st, unsigned base, unsigned hiBits) {
+  const unsigned span = hiBits > base ? hiBits - base : 0u;
+  int shift = 0;
+  while ((span >> shift) >= (unsigned)kLloydBins) shift++;
+  st->lloydBase = base;
+  st->lloydHiBits = hiBits;
+  st->lloydShift = shift;
 }
 
 // Find the digit bucket holding the remaining rank; one CTA per cubelet.
@@ -175,6 +299,19 @@ __global__ void __launch_bounds__(1024) select_resolve(DevBatch b) {
           st->maxVal = ord_dec(st->maxOrd);
           st->maxAbs = __uint_as_float(st->absMax);
           st->maxAbs2 = __uint_as_float(st->absMax2);
+          if (cd.quantAlg == WL_LLOYD) {
+            // Lloyd range top: the second largest |c| unless it is not above
+            // the threshold (test_compress_cpu.cc:419-422).  Decidable from
+            // the bucket alone unless it lies in the bucket; bucket 0 may
+            // hold a zero threshold, which becomes 1e-16.
+            const unsigned P = (unsigned)i, a2 = st->absMax2;
+            int deferred = 0;
+            unsigned hiBits = 0;
+            if (P == 0 || (a2 >> 20) == P) deferred = 1;
+            else hiBits = (a2 >> 20) > P ? a2 : st->absMax;
+            st->lloydDeferred = deferred;
+            if (!deferred) set_lloyd_bins(st, P << 20, hiBits);
+          }
         } else if (PASS == 1) {
           st->prefix = (st->prefix << 12) | (unsigned)i;
           st->rank = rem;
@@ -183,6 +320,10 @@ __global__ void __launch_bounds__(1024) select_resolve(DevBatch b) {
           float t = __uint_as_float(bits);
           if (t == 0.0f) t = 1e-16f;  // thresh_cpu.cc:98
           st->threshold = t;
+          if (cd.quantAlg == WL_LLOYD && st->lloydDeferred) {
+            const float hi = st->maxAbs2 > t ? st->maxAbs2 : st->maxAbs;
+            set_lloyd_bins(st, __float_as_uint(t), __float_as_uint(hi));
+          }
         }
         break;
       }
@@ -203,6 +344,8 @@ __global__ void select_init(DevBatch b) {
   st->maxOrd = ord_enc(FLT_MIN);
   st->absMax = 0u;
   st->absMax2 = 0u;
+  st->candCount = 0u;
+  st->lloydDeferred = 0;
 }
 
 }  // namespace
@@ -210,11 +353,13 @@ __global__ void select_init(DevBatch b) {
 void launch_select(DevBatch &b, const float *coef, cudaStream_t s) {
   select_init<<<(b.n + 127) / 128, 128, 0, s>>>(b);
   const unsigned chunks = (unsigned)b.totalChunks;
-  select_pass<0><<<chunks, kThreads, 0, s>>>(b, coef);
+  unsigned *cand = reinterpret_cast<unsigned *>(b.coef2);
+  select_pass0<<<chunks, kThreads, 0, s>>>(b, coef);
   select_resolve<0><<<b.n, 1024, 0, s>>>(b);
-  select_pass<1><<<chunks, kThreads, 0, s>>>(b, coef);
+  select_compact<<<chunks, kThreads, 0, s>>>(b, coef, cand);
+  cand_hist<1><<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, cand);
   select_resolve<1><<<b.n, 1024, 0, s>>>(b);
-  select_pass<2><<<chunks, kThreads, 0, s>>>(b, coef);
+  cand_hist<2><<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, cand);
   select_resolve<2><<<b.n, 1024, 0, s>>>(b);
 }
 

@@ -25,6 +25,7 @@ constexpr int kChunk = 4096;            // elements per quantize/encode chunk
 constexpr int kChunkThreads = 256;
 constexpr int kSelectBins = 4096;       // radix-select digit histogram
 constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
+constexpr int kCandSlices = 64;         // CTAs per cubelet over its threshold candidates
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
 constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
 
@@ -126,6 +127,15 @@ struct CubeletState {
   int nLeaves;
   int error;                     // nonzero: kernel-side failure code
   int pad_;
+  // threshold bucket candidates, compacted into the cubelet's own region of
+  // the second coefficient buffer (free once the transform is done)
+  unsigned candCount;
+  // Lloyd histogram bins: bin = (bits(|c|) - lloydBase) >> lloydShift for
+  // threshold < |c| <= the Lloyd range top (bits lloydHiBits)
+  unsigned lloydBase, lloydHiBits;
+  int lloydShift;
+  int lloydDeferred;             // 1: the compaction pass cannot tell; separate pass
+  int pad2_;
 };
 
 // Everything a kernel needs about one cubelet of a batch.
