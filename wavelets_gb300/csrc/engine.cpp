@@ -105,8 +105,8 @@ struct wl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, codes, codeLen, decode,
+  DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable, qlut,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, chunkCub, codes, codeLen, decode,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
   HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   cudaEvent_t ev[7] = {};
@@ -420,9 +420,11 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->state, n * sizeof(CubeletState)));
   TRY(ensure(ctx, ctx->cub, n * sizeof(CubeletDev)));
   TRY(ensure(ctx, ctx->chunkPrefix, n * sizeof(long long)));
+  TRY(ensure(ctx, ctx->chunkCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
   if (anyLloyd) TRY(ensure(ctx, ctx->lloydHist, (size_t)n * kLloydBins * 4));
   TRY(ensure(ctx, ctx->qtable, (size_t)tableTotal * 4));
+  if (anyLloyd) TRY(ensure(ctx, ctx->qlut, (size_t)n * (kLutCells + 1) * 2));
   TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
   TRY(ensure(ctx, ctx->hist, (size_t)n * kMaxSymbols * 8));
   TRY(ensure(ctx, ctx->chunkRun, chunkTotal * sizeof(int4)));
@@ -500,6 +502,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.selHist = P<unsigned>(ctx->selHist);
   b.lloydHist = P<float>(ctx->lloydHist);
   b.qtable = P<float>(ctx->qtable);
+  b.qlut = P<uint16_t>(ctx->qlut);
   b.dqtable = P<float>(ctx->dqtable);
   b.hist = P<unsigned long long>(ctx->hist);
   b.chunkRun = P<int4>(ctx->chunkRun);
@@ -510,6 +513,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.decode = P<int>(ctx->decode);
   b.words = P<uint32_t>(ctx->words);
   b.chunkPrefix = P<long long>(ctx->chunkPrefix);
+  b.chunkCub = P<int>(ctx->chunkCub);
   b.logHdr = P<int4>(ctx->logHdr);
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
@@ -540,7 +544,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- threshold ----
   launch_select(b, b.coef, s);
-  ctx->launches += 8;
+  ctx->launches += 9;
   CU(cudaGetLastError());
   mark(ctx, 4);
 
@@ -920,8 +924,8 @@ void wl_destroy(wl_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->tokCount,
                    &ctx->state, &ctx->cub,
-                   &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->hist,
-                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix,
+                   &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
+                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix, &ctx->chunkCub,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
                    &ctx->meta};

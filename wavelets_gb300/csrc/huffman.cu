@@ -30,15 +30,6 @@ namespace {
 constexpr int kThreads = kChunkThreads;
 constexpr int kMaxCodeBits = 58;  // + 3 dup bits fits 61 bits -> at most 3 words
 
-__device__ __forceinline__ int find_cubelet(const long long *prefix, int n, long long c) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= c) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // ---- tree -------------------------------------------------------------------
 struct BuildSmem {
   unsigned long long *keys;  // sorted leaves, later codes of all nodes
@@ -314,7 +305,7 @@ __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
   __shared__ int sCount[2];
   __shared__ unsigned long long sh[kThreads / 32];
   const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
   const int dupV = b.state[ci].dupValue;
   const int S = cd.binCount + 1;
@@ -395,7 +386,7 @@ __global__ void pack_meta_kernel(DevBatch b) {
 __global__ void encode_zero_kernel(DevBatch b) {
   const long long chunk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (chunk >= b.totalChunks) return;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletState *st = b.state + ci;
   if (st->error) return;
   const unsigned long long off = b.chunkBits[chunk];
@@ -417,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   __shared__ unsigned shs[kThreads / 32];
   extern __shared__ uint32_t sw[];
   const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   if (st->error) return;

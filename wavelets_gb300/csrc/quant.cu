@@ -30,15 +30,6 @@ constexpr int kThreads = kChunkThreads;
 constexpr int kPer = kChunk / kThreads;  // 16 consecutive elements per thread
 constexpr int INF = 0x7fffffff;
 
-__device__ __forceinline__ int find_cubelet(const long long *prefix, int n, long long c) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= c) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // greedy split of a zero-bin run (HuffmanDup::dupCount, huffman.h:46-57)
 __device__ __forceinline__ void run_split(long long L, long long &singles, long long &dups) {
   dups = L / 1024;  // dupFindLongest returns 7 (1024) while L >= 1024
@@ -79,6 +70,36 @@ __global__ void quant_params_kernel(DevBatch b) {
   }
   // Lloyd: zeroBin is set by lloyd_solve
   if (cd.quantAlg != WL_LLOYD) st->dupValue = cd.compressZeros ? st->zeroBin : -1;
+}
+
+// number of entries of the sorted table t[0..n) that are <= x / < x, by a
+// fixed number of halving steps (no divergent loop exits)
+__device__ __forceinline__ int count_le(const float *t, int n, float x) {
+  int pos = 0;
+  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
+    if (step <= n - pos && t[pos + step - 1] <= x) pos += step;
+  return pos;
+}
+__device__ __forceinline__ int count_lt(const float *t, int n, float x) {
+  int pos = 0;
+  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
+    if (step <= n - pos && t[pos + step - 1] < x) pos += step;
+  return pos;
+}
+
+// Lloyd bin lookup table.  Floats map to an order-preserving 32-bit key
+// (sign flipped for positives, all bits for negatives); cell c holds the keys
+// c << 20 .. (c+1) << 20, i.e. 1/8 octave of one sign.  lut[c] counts the
+// boundaries below the smallest float of cell c, so for x in the cell the
+// reference's lower_bound is lut[c] plus the boundaries of
+// [lut[c], lut[c+1]) that are below x.
+__device__ __forceinline__ unsigned order_key(float x) {
+  const unsigned u = __float_as_uint(x);
+  return u ^ ((unsigned)((int)u >> 31) | 0x80000000u);
+}
+__device__ __forceinline__ float cell_min(int c) {
+  const unsigned k = (unsigned)c << 20;
+  return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
 }
 
 // ---- Lloyd on the |coefficient| histogram -----------------------------------
@@ -276,6 +297,17 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
     st->nValues = nv;
     if (nv != B) st->error = 3;
   }
+  __syncthreads();
+  {
+    const float *bnd = b.qtable + cd.tableOff;
+    const int nb = st->nBounds;
+    uint16_t *lut = b.qlut + (size_t)ci * (kLutCells + 1);
+    for (int c = threadIdx.x; c < kLutCells; c += 1024) {
+      const float m = cell_min(c);  // NaN cells: never looked up; keep the table monotone
+      lut[c] = (uint16_t)(m != m ? (c >= kLutCells / 2 ? nb : 0) : count_lt(bnd, nb, m));
+    }
+    if (threadIdx.x == 0) lut[kLutCells] = (uint16_t)nb;
+  }
 }
 
 // ---- quantize one value ------------------------------------------------------
@@ -286,22 +318,8 @@ struct QParams {
   int lowBin, highNeg, nPos, nNeg;
 };
 
-// number of entries of the sorted table t[0..n) that are <= x / < x, by a
-// fixed number of halving steps (no divergent loop exits)
-__device__ __forceinline__ int count_le(const float *t, int n, float x) {
-  int pos = 0;
-  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
-    if (step <= n - pos && t[pos + step - 1] <= x) pos += step;
-  return pos;
-}
-__device__ __forceinline__ int count_lt(const float *t, int n, float x) {
-  int pos = 0;
-  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1)
-    if (step <= n - pos && t[pos + step - 1] < x) pos += step;
-  return pos;
-}
-
-__device__ __forceinline__ int quant_value(float x, const QParams &q, const float *tab) {
+__device__ __forceinline__ int quant_value(float x, const QParams &q, const float *tab,
+                                           const uint16_t *lut) {
   if (q.alg == WL_UNIFORM) {
     // QuantUniform::quant (quant.h:244-276)
     if (x < 0) {
@@ -326,10 +344,12 @@ __device__ __forceinline__ int quant_value(float x, const QParams &q, const floa
     return q.lowBin + count_le(tab, q.nPos, x);
   }
   // QuantCodebook::quant (quant.h:515-526): x >= last boundary -> nb, else
-  // lower_bound (the number of boundaries below x)
-  if (q.nb == 0) return 0;
+  // lower_bound (the number of boundaries below x; 0 for NaN)
+  if (q.nb == 0 || x != x) return 0;
   if (x >= tab[q.nb - 1]) return q.nb;
-  return count_lt(tab, q.nb, x);
+  const int c = (int)(order_key(x) >> 20);
+  const int lo = lut[c], hi = lut[c + 1];
+  return lo + count_lt(tab + lo, hi - lo, x);
 }
 
 __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const CubeletState *st) {
@@ -367,8 +387,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned wCnt[kThreads / 32];
   __shared__ uint16_t sTok[kChunk];
   __shared__ uint16_t sBin[kChunk];
+  __shared__ uint16_t sLut[kLutCells + 1];
   const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   const QParams q = load_qparams(cd, st);
@@ -377,6 +398,10 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   const int nTab = q.alg == WL_LLOYD ? q.nb : (q.alg == WL_LOG ? q.nPos + q.nNeg : 0);
   for (int i = threadIdx.x; i < B + 1; i += kThreads) hist[i] = 0;
   for (int i = threadIdx.x; i < nTab; i += kThreads) tab[i] = b.qtable[cd.tableOff + i];
+  if (q.alg == WL_LLOYD) {
+    const uint16_t *gl = b.qlut + (size_t)ci * (kLutCells + 1);
+    for (int i = threadIdx.x; i <= kLutCells; i += kThreads) sLut[i] = gl[i];
+  }
   __syncthreads();
 
   const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
@@ -391,14 +416,14 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
 #pragma unroll
     for (int k = 0; k < kPer / 4; k++) {
       const float4 v = s4[k];
-      bins[4 * k + 0] = quant_value(v.x, q, tab);
-      bins[4 * k + 1] = quant_value(v.y, q, tab);
-      bins[4 * k + 2] = quant_value(v.z, q, tab);
-      bins[4 * k + 3] = quant_value(v.w, q, tab);
+      bins[4 * k + 0] = quant_value(v.x, q, tab, sLut);
+      bins[4 * k + 1] = quant_value(v.y, q, tab, sLut);
+      bins[4 * k + 2] = quant_value(v.z, q, tab, sLut);
+      bins[4 * k + 3] = quant_value(v.w, q, tab, sLut);
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < kPer; k++) bins[k] = p0 + k < len ? quant_value(src[p0 + k], q, tab) : 0;
+    for (int k = 0; k < kPer; k++) bins[k] = p0 + k < len ? quant_value(src[p0 + k], q, tab, sLut) : 0;
   }
   const unsigned valid = p0 >= len ? 0u : (p0 + kPer <= len ? 0xffffu : ((1u << (len - p0)) - 1u));
   unsigned zm = 0;

@@ -37,15 +37,6 @@ __device__ __forceinline__ float ord_dec(unsigned u) {
   return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-__device__ __forceinline__ int find_cubelet(const long long *prefix, int n, long long c) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= c) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // top-2 merge of multisets {a1,a2} and {b1,b2} (a1>=a2, b1>=b2)
 __device__ __forceinline__ void top2_merge(unsigned &a1, unsigned &a2, unsigned b1, unsigned b2) {
   unsigned t1 = max(a1, b1);
@@ -85,7 +76,7 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kSelectBins];
   __shared__ unsigned sMin[kThreads / 32], sMax[kThreads / 32], sA1[kThreads / 32], sA2[kThreads / 32];
   const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
   const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
   const int len = (int)min((long long)kChunk, cd.n - start);
@@ -153,7 +144,7 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
   __shared__ unsigned wCnt[kThreads / 32];
   __shared__ unsigned sBase;
   const long long chunk = blockIdx.x;
-  const int ci = find_cubelet(b.chunkPrefix, b.n, chunk);
+  const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
   const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
   const int len = (int)min((long long)kChunk, cd.n - start);
@@ -335,6 +326,13 @@ __global__ void __launch_bounds__(1024) select_resolve(DevBatch b) {
   for (int i = threadIdx.x; i < kSelectBins; i += 1024) g[i] = 0;
 }
 
+// cubelet index of every chunk, so chunk kernels start with one load
+__global__ void chunk_map_kernel(DevBatch b) {
+  const CubeletDev cd = b.cub[blockIdx.x];
+  for (int j = threadIdx.x; j < cd.nChunks; j += blockDim.x)
+    b.chunkCub[cd.chunkBase + j] = (int)blockIdx.x;
+}
+
 __global__ void select_init(DevBatch b) {
   const int ci = blockIdx.x * blockDim.x + threadIdx.x;
   if (ci >= b.n) return;
@@ -351,6 +349,7 @@ __global__ void select_init(DevBatch b) {
 }  // namespace
 
 void launch_select(DevBatch &b, const float *coef, cudaStream_t s) {
+  chunk_map_kernel<<<b.n, 256, 0, s>>>(b);
   select_init<<<(b.n + 127) / 128, 128, 0, s>>>(b);
   const unsigned chunks = (unsigned)b.totalChunks;
   unsigned *cand = reinterpret_cast<unsigned *>(b.coef2);

@@ -25,7 +25,8 @@ constexpr int kChunk = 4096;            // elements per quantize/encode chunk
 constexpr int kChunkThreads = 256;
 constexpr int kSelectBins = 4096;       // radix-select digit histogram
 constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
-constexpr int kCandSlices = 64;         // CTAs per cubelet over its threshold candidates
+constexpr int kCandSlices = 64;
+constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float order key         // CTAs per cubelet over its threshold candidates
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
 constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
 
@@ -168,6 +169,7 @@ struct DevBatch {
   unsigned *selHist;              // [n][kSelectBins]
   float *lloydHist;               // [n][kLloydBins][2] (count, sum)
   float *qtable;                  // quantizer tables
+  uint16_t *qlut;                 // [n][kLutCells + 1] Lloyd boundaries below each key cell
   float *dqtable;                 // dequant values [n][binCount]
   unsigned long long *hist;       // [n][kMaxSymbols] Huffman counts
   int4 *chunkRun;                 // per chunk: lead, trail, allZero, len
@@ -178,6 +180,7 @@ struct DevBatch {
   int *decode;                    // [n][4*kMaxSymbols]
   uint32_t *words;                // Huffman output
   long long *chunkPrefix;         // [n+1] chunk prefix (== cub[i].chunkBase)
+  int *chunkCub;                  // [totalChunks] cubelet of every chunk
   int4 *logHdr;                   // [n] log table layout from the host
   int *meta;                      // packed decode tables and Lloyd codebooks
   long long totalChunks;
