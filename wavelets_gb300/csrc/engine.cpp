@@ -106,7 +106,7 @@ struct wl_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable, qlut,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, chunkCub, codes, codeLen, decode,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, chunkCub, groupCub, codes, codeLen, decode,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
   HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   cudaEvent_t ev[7] = {};
@@ -421,10 +421,11 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->cub, n * sizeof(CubeletDev)));
   TRY(ensure(ctx, ctx->chunkPrefix, n * sizeof(long long)));
   TRY(ensure(ctx, ctx->chunkCub, chunkTotal * sizeof(int)));
+  TRY(ensure(ctx, ctx->groupCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
   if (anyLloyd) TRY(ensure(ctx, ctx->lloydHist, (size_t)n * kLloydBins * 4));
   TRY(ensure(ctx, ctx->qtable, (size_t)tableTotal * 4));
-  if (anyLloyd) TRY(ensure(ctx, ctx->qlut, (size_t)n * (kLutCells + 1) * 2));
+  if (anyLloyd) TRY(ensure(ctx, ctx->qlut, (size_t)n * kLutStride * 2));
   TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
   TRY(ensure(ctx, ctx->hist, (size_t)n * kMaxSymbols * 8));
   TRY(ensure(ctx, ctx->chunkRun, chunkTotal * sizeof(int4)));
@@ -465,6 +466,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   // ---- descriptors ----
   CubeletDev *hc = H<CubeletDev>(ctx->hCub);
   long long *hp = reinterpret_cast<long long *>(hc + n);
+  long long groupTotal = 0;
   for (int i = 0; i < n; i++) {
     const Plan &pl = plans[i];
     CubeletDev &c = hc[i];
@@ -481,6 +483,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     c.frac = pl.p.threshold_fraction;
     c.lloydIters = pl.p.lloyd_iters > 0 ? pl.p.lloyd_iters : 20;
     c.tableOff = pl.tableOff;
+    c.groupBase = (int)groupTotal;
+    groupTotal += (pl.nChunks + kQuantGroup - 1) / kQuantGroup;
     hp[i] = pl.chunkBase;
   }
   CU(cudaMemcpyAsync(ctx->cub.p, hc, n * sizeof(CubeletDev), cudaMemcpyHostToDevice, s));
@@ -514,6 +518,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.words = P<uint32_t>(ctx->words);
   b.chunkPrefix = P<long long>(ctx->chunkPrefix);
   b.chunkCub = P<int>(ctx->chunkCub);
+  b.groupCub = P<int>(ctx->groupCub);
+  b.totalGroups = groupTotal;
   b.logHdr = P<int4>(ctx->logHdr);
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
@@ -925,7 +931,7 @@ void wl_destroy(wl_ctx *ctx) {
   DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->tokCount,
                    &ctx->state, &ctx->cub,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
-                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix, &ctx->chunkCub,
+                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix, &ctx->chunkCub, &ctx->groupCub,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
                    &ctx->meta};

@@ -27,7 +27,6 @@ namespace wl {
 namespace {
 
 constexpr int kThreads = kChunkThreads;
-constexpr int kPer = kChunk / kThreads;  // 16 consecutive elements per thread
 constexpr int INF = 0x7fffffff;
 
 // greedy split of a zero-bin run (HuffmanDup::dupCount, huffman.h:46-57)
@@ -301,7 +300,7 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
   {
     const float *bnd = b.qtable + cd.tableOff;
     const int nb = st->nBounds;
-    uint16_t *lut = b.qlut + (size_t)ci * (kLutCells + 1);
+    uint16_t *lut = b.qlut + (size_t)ci * kLutStride;
     for (int c = threadIdx.x; c < kLutCells; c += 1024) {
       const float m = cell_min(c);  // NaN cells: never looked up; keep the table monotone
       lut[c] = (uint16_t)(m != m ? (c >= kLutCells / 2 ? nb : 0) : count_lt(bnd, nb, m));
@@ -374,155 +373,204 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 }
 
 // ---- quantize + count + tokens of the chunk ----------------------------------
-// Each thread quantizes 16 consecutive coefficients.  Instead of storing a bin
-// per coefficient, the chunk stores its Huffman tokens in order: every value
-// that is not the zero bin, and the tokens of every zero-bin run that starts
-// and ends inside the chunk.  Runs touching a chunk edge are left to
-// runs_kernel (counts) and the encoder (tokens).
-__global__ void __launch_bounds__(kThreads)
+// Instead of storing a bin per coefficient, a chunk stores its Huffman tokens
+// in order: a token for every value that is not the zero bin, preceded by the
+// tokens of the zero-bin run before it when that run starts inside the chunk.
+// Runs touching a chunk edge are left to runs_kernel (counts) and the encoder
+// (tokens).  A CTA codes kQuantGroup consecutive chunks of one cubelet.
+//
+// Phase 1 (every element): -thr < x < thr is the zero bin for all three
+// quantizers (uniform and log test |x| <= thr first; the codebook has the
+// boundaries -thr and thr around its zero bin and none in between), so an
+// element costs two compares.  The others are candidates, compacted per warp
+// (warp w owns elements [512 w, 512 w + 512); in word j lane l holds element
+// 512 w + 32 j + l, so loads are coalesced).
+// Phase 2 (per candidate): the exact bin; candidates that are not the zero
+// bin become the chunk's value list (position, bin) in position order.
+// Phase 3 (per value): the gap to the previous value is the zero run in
+// between; each thread takes a contiguous slice of the list, counts its
+// tokens, and after a block scan writes them.
+// greedy split of a zero-bin run into dup tokens and single zero-bin tokens
+// (closed form of run_split; the same counts as run_token_count)
+__device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups) {
+  const int q = L >> 10, r = L & 1023, hi = r & ~7, lo = r & 7;
+  const int big = __popc(hi >> 4);
+  if (hi & 8) {
+    dups = q + big + (lo > 0 ? 1 : 0);
+    singles = lo > 0 ? lo : 8;
+  } else {
+    dups = q + big;
+    singles = lo;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 4)
 quantize_kernel(DevBatch b, const float *__restrict__ coef) {
+  constexpr int kWords = kChunk / kThreads;  // 16 words of 32 elements per warp
+  constexpr int kSpan = 32 * kWords;         // elements per warp
+  constexpr int kWarps = kThreads / 32;
   __shared__ unsigned hist[kMaxSymbols + 1];
   extern __shared__ float tab[];  // quantizer table (Lloyd / log), sized by the launch
-  __shared__ int wFirst[kThreads / 32], wLast[kThreads / 32];
-  __shared__ unsigned wCnt[kThreads / 32];
-  __shared__ uint16_t sTok[kChunk];
-  __shared__ uint16_t sBin[kChunk];
-  __shared__ uint16_t sLut[kLutCells + 1];
-  const long long chunk = blockIdx.x;
-  const int ci = b.chunkCub[chunk];
+  __shared__ __align__(16) uint16_t sLut[kLutStride];
+  // candidate values by warp region, then the packed value list
+  __shared__ __align__(16) float sX[kChunk];
+  // candidate positions by warp region, then the chunk's tokens
+  __shared__ uint16_t sPT[kChunk];
+  __shared__ unsigned wVal[kWarps], wTok[kWarps];
+  unsigned *sList = reinterpret_cast<unsigned *>(sX);  // (position << 13) | bin
+  uint16_t *sTok = sPT;
+  const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   const QParams q = load_qparams(cd, st);
   const int dupV = st->dupValue;
   const int B = cd.binCount;
   const int nTab = q.alg == WL_LLOYD ? q.nb : (q.alg == WL_LOG ? q.nPos + q.nNeg : 0);
+  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;  // first chunk of the cubelet
+  const int nc = min(kQuantGroup, cd.nChunks - c0);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int base = w * kSpan;
+  const unsigned ltMask = (1u << lane) - 1u;
+  // zero-bin elements can be skipped only when they are coded as runs
+  const float zlo = dupV >= 0 ? -q.thr : 0.f, zhi = dupV >= 0 ? q.thr : 0.f;
+
   for (int i = threadIdx.x; i < B + 1; i += kThreads) hist[i] = 0;
   for (int i = threadIdx.x; i < nTab; i += kThreads) tab[i] = b.qtable[cd.tableOff + i];
   if (q.alg == WL_LLOYD) {
-    const uint16_t *gl = b.qlut + (size_t)ci * (kLutCells + 1);
-    for (int i = threadIdx.x; i <= kLutCells; i += kThreads) sLut[i] = gl[i];
+    const uint4 *gl = reinterpret_cast<const uint4 *>(b.qlut + (size_t)ci * kLutStride);
+    uint4 *sl = reinterpret_cast<uint4 *>(sLut);
+    for (int i = threadIdx.x; i < kLutStride / 8; i += kThreads) sl[i] = gl[i];
   }
   __syncthreads();
 
-  const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int len = (int)min((long long)kChunk, cd.n - start);
-  const float *src = coef + cd.coefOff + start;
-  const int p0 = threadIdx.x * kPer;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = 0; k < nc; k++) {
+    const long long chunk = cd.chunkBase + c0 + k;
+    const long long start = (long long)(c0 + k) * kChunk;
+    const int len = (int)min((long long)kChunk, cd.n - start);
+    const float *src = coef + cd.coefOff + start;
 
-  int bins[kPer];
-  if (p0 + kPer <= len) {
-    const float4 *s4 = reinterpret_cast<const float4 *>(src + p0);
+    // ---- phase 1: candidates into the warp's region
+    int nCand = 0;  // warp-uniform
+    {
+      float x[kWords];
 #pragma unroll
-    for (int k = 0; k < kPer / 4; k++) {
-      const float4 v = s4[k];
-      bins[4 * k + 0] = quant_value(v.x, q, tab, sLut);
-      bins[4 * k + 1] = quant_value(v.y, q, tab, sLut);
-      bins[4 * k + 2] = quant_value(v.z, q, tab, sLut);
-      bins[4 * k + 3] = quant_value(v.w, q, tab, sLut);
-    }
-  } else {
+      for (int j = 0; j < kWords; j++) {
+        const int pos = base + 32 * j + lane;
+        x[j] = pos < len ? src[pos] : 0.f;
+      }
 #pragma unroll
-    for (int k = 0; k < kPer; k++) bins[k] = p0 + k < len ? quant_value(src[p0 + k], q, tab, sLut) : 0;
-  }
-  const unsigned valid = p0 >= len ? 0u : (p0 + kPer <= len ? 0xffffu : ((1u << (len - p0)) - 1u));
-  unsigned zm = 0;
-#pragma unroll
-  for (int k = 0; k < kPer; k++) zm |= (bins[k] == dupV ? 1u : 0u) << k;
-  zm &= valid;
-  const unsigned nzm = valid & ~zm;
-
-  // next non-zero position after this thread's range, last one before it
-  int nextNZ = INF, prevNZ = -1;
-  if (dupV >= 0) {
-    const int first = nzm ? p0 + __ffs(nzm) - 1 : INF;
-    const int last = nzm ? p0 + 31 - __clz(nzm) : -1;
-    int incMin = first, incMax = last;
-    for (int off = 1; off < 32; off <<= 1) {
-      const int vmin = __shfl_down_sync(0xffffffffu, incMin, off);
-      const int vmax = __shfl_up_sync(0xffffffffu, incMax, off);
-      if (lane + off < 32) incMin = min(incMin, vmin);
-      if (lane >= off) incMax = max(incMax, vmax);
-    }
-    if (lane == 0) wFirst[w] = incMin;
-    if (lane == 31) wLast[w] = incMax;
-    __syncthreads();
-    nextNZ = __shfl_down_sync(0xffffffffu, incMin, 1);
-    if (lane == 31) nextNZ = INF;
-    prevNZ = __shfl_up_sync(0xffffffffu, incMax, 1);
-    if (lane == 0) prevNZ = -1;
-    for (int v = w + 1; v < kThreads / 32; v++) nextNZ = min(nextNZ, wFirst[v]);
-    for (int v = 0; v < w; v++) prevNZ = max(prevNZ, wLast[v]);
-  }
-
-  // Tokens of this thread in position order: a token for every non-zero-bin
-  // value, and the tokens of every run that starts here and ends inside the
-  // chunk.  run start = zero-bin value whose predecessor is not one.
-  unsigned starts = zm & ((nzm << 1) | (prevNZ == p0 - 1 && p0 > 0 ? 1u : 0u));
-  // drop runs that reach the chunk end (trailing) -- they belong to runs_kernel
-  unsigned cnt = __popc(nzm);
-  {
-    unsigned m = starts;
-    while (m) {
-      const int k = __ffs(m) - 1;
-      m &= m - 1;
-      const unsigned later = nzm & ~((2u << k) - 1u);
-      const int end = later ? p0 + __ffs(later) - 1 : ((p0 + kPer >= len) ? INF : nextNZ);
-      if (end == INF) { starts &= ~(1u << k); continue; }
-      cnt += run_token_count(end - (p0 + k));
-    }
-  }
-  // exclusive scan of the per-thread counts
-  unsigned base;
-  {
-    unsigned inc = cnt;
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
-      if (lane >= off) inc += t;
-    }
-    if (lane == 31) wCnt[w] = inc;
-    // stage the bins for the emission loop (dynamic index, shared memory)
-#pragma unroll
-    for (int k = 0; k < kPer; k++) sBin[threadIdx.x * kPer + k] = (uint16_t)bins[k];
-    __syncthreads();
-    unsigned before = 0;
-    for (int v = 0; v < w; v++) before += wCnt[v];
-    base = before + inc - cnt;
-  }
-  {
-    unsigned o = base;
-    unsigned ev = nzm | starts;
-    const uint16_t *mb = sBin + threadIdx.x * kPer;
-    auto put = [&](uint16_t t) {
-      sTok[o++] = t;
-      atomicAdd(&hist[t & 0x1fff], 1u);
-    };
-    while (ev) {
-      const int k = __ffs(ev) - 1;
-      ev &= ev - 1;
-      if (nzm & (1u << k)) {
-        put(make_token(mb[k], 0));
-      } else {
-        const unsigned later = nzm & ~((2u << k) - 1u);
-        const int end = later ? p0 + __ffs(later) - 1 : nextNZ;
-        run_tokens(p0 + k, end, p0 + k, end, B, dupV, put);
+      for (int j = 0; j < kWords; j++) {
+        const int pos = base + 32 * j + lane;
+        const bool cand = pos < len && !(x[j] > zlo && x[j] < zhi);
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        if (cand) {
+          const int l = base + nCand + __popc(m & ltMask);
+          sX[l] = x[j];
+          sPT[l] = (uint16_t)pos;
+        }
+        nCand += __popc(m);
       }
     }
-  }
-  __syncthreads();
-  unsigned total = 0;
-  for (int v = 0; v < kThreads / 32; v++) total += wCnt[v];
-  uint16_t *dst = b.tok + cd.coefOff + start;
-  for (unsigned i = threadIdx.x; i < total; i += kThreads) dst[i] = sTok[i];
-  if (threadIdx.x == 0) {
-    b.chunkTok[chunk] = (int)total;
-    if (dupV >= 0) {
-      int fz = INF, lz = -1;
-      for (int v = 0; v < kThreads / 32; v++) { fz = min(fz, wFirst[v]); lz = max(lz, wLast[v]); }
-      const int lead = fz == INF ? len : fz;
-      const int trail = lz < 0 ? len : len - 1 - lz;
-      b.chunkRun[chunk] = make_int4(lead, trail, lz < 0 ? 1 : 0, len);
+    __syncwarp();
+    // ---- phase 2: exact bins of the warp's candidates
+    unsigned e[kWords];
+    unsigned isv = 0;  // bit r: candidate lane + 32 r is a value
+    int nVal = 0;      // warp-uniform
+#pragma unroll
+    for (int r = 0; r < kWords; r++) {
+      const int l = lane + 32 * r;
+      const bool has = l < nCand;
+      const int bin = has ? quant_value(sX[base + l], q, tab, sLut) : 0;
+      const unsigned pos = has ? sPT[base + l] : 0u;
+      const bool v = has && bin != dupV;
+      e[r] = (pos << 13) | (unsigned)bin;
+      isv |= (v ? 1u : 0u) << r;
+      nVal += __popc(__ballot_sync(0xffffffffu, v));
     }
+    if (lane == 0) wVal[w] = (unsigned)nVal;
+    __syncthreads();  // every warp has read its candidates
+    unsigned total = 0, vo = 0;
+    for (int v = 0; v < kWarps; v++) {
+      if (v < w) vo += wVal[v];
+      total += wVal[v];
+    }
+#pragma unroll
+    for (int r = 0; r < kWords; r++) {
+      const bool v = (isv >> r) & 1u;
+      const unsigned m = __ballot_sync(0xffffffffu, v);
+      if (v) sList[vo + __popc(m & ltMask)] = e[r];
+      vo += __popc(m);
+    }
+    __syncthreads();
+
+    // ---- phase 3: tokens of a contiguous slice of the values
+    const unsigned per = (total + kThreads - 1) / kThreads;
+    const unsigned i0 = min(threadIdx.x * per, total), i1 = min(i0 + per, total);
+    const int prev0 = i0 > 0 ? (int)(sList[i0 - 1] >> 13) : -1;
+    int myTok = 0, singles = 0, dups = 0;
+    {
+      int prev = prev0;
+      for (unsigned i = i0; i < i1; i++) {
+        const int p = (int)(sList[i] >> 13);
+        const int gap = prev >= 0 ? p - prev - 1 : 0;
+        if (gap > 0) {
+          int sg, dp;
+          run_split_closed(gap, sg, dp);
+          myTok += sg + dp;
+          singles += sg;
+          dups += dp;
+        }
+        myTok += 1;
+        prev = p;
+      }
+    }
+    // block exclusive scan of the token counts
+    int inc = myTok;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      singles += __shfl_xor_sync(0xffffffffu, singles, d);
+      dups += __shfl_xor_sync(0xffffffffu, dups, d);
+    }
+    if (lane == 31) wTok[w] = (unsigned)inc;
+    if (lane == 0) {
+      if (singles) atomicAdd(&hist[dupV], (unsigned)singles);
+      if (dups) atomicAdd(&hist[B], (unsigned)dups);
+    }
+    __syncthreads();
+    unsigned o = (unsigned)(inc - myTok), nTok = 0;
+    for (int v = 0; v < kWarps; v++) {
+      if (v < w) o += wTok[v];
+      nTok += wTok[v];
+    }
+    {
+      int prev = prev0;
+      for (unsigned i = i0; i < i1; i++) {
+        const unsigned ev = sList[i];
+        const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
+        if (prev >= 0 && p - prev > 1)
+          run_tokens(prev + 1, p, prev + 1, p, B, dupV, [&](uint16_t t) { sTok[o++] = t; });
+        sTok[o++] = make_token(bin, 0);
+        atomicAdd(&hist[bin], 1u);
+        prev = p;
+      }
+    }
+    __syncthreads();
+    uint16_t *dst = b.tok + cd.coefOff + start;
+    for (unsigned i = threadIdx.x; i < nTok; i += kThreads) dst[i] = sTok[i];
+    if (threadIdx.x == 0) {
+      b.chunkTok[chunk] = (int)nTok;
+      if (dupV >= 0) {
+        const int lead = total ? (int)(sList[0] >> 13) : len;
+        const int trail = total ? len - 1 - (int)(sList[total - 1] >> 13) : len;
+        b.chunkRun[chunk] = make_int4(lead, trail, total ? 0 : 1, len);
+      }
+    }
+    __syncthreads();  // the buffers are reused by the next chunk
   }
   unsigned long long *gh = b.hist + (size_t)ci * kMaxSymbols;
   for (int i = threadIdx.x; i <= B; i += kThreads)
@@ -681,7 +729,7 @@ void launch_quantize(DevBatch &b, const float *coef, int maxTable, cudaStream_t 
   const int smem = maxTable * (int)sizeof(float);
   cudaFuncSetAttribute(quantize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        smem > 0 ? smem : 1);
-  quantize_kernel<<<(unsigned)b.totalChunks, kThreads, smem, s>>>(b, coef);
+  quantize_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b, coef);
 }
 
 void launch_runs(DevBatch &b, cudaStream_t s) { runs_kernel<<<b.n, 1024, 0, s>>>(b); }

@@ -326,11 +326,15 @@ __global__ void __launch_bounds__(1024) select_resolve(DevBatch b) {
   for (int i = threadIdx.x; i < kSelectBins; i += 1024) g[i] = 0;
 }
 
-// cubelet index of every chunk, so chunk kernels start with one load
+// cubelet index of every chunk (and quantize group), so chunk kernels start
+// with one load
 __global__ void chunk_map_kernel(DevBatch b) {
   const CubeletDev cd = b.cub[blockIdx.x];
   for (int j = threadIdx.x; j < cd.nChunks; j += blockDim.x)
     b.chunkCub[cd.chunkBase + j] = (int)blockIdx.x;
+  const int groups = (cd.nChunks + kQuantGroup - 1) / kQuantGroup;
+  for (int j = threadIdx.x; j < groups; j += blockDim.x)
+    b.groupCub[cd.groupBase + j] = (int)blockIdx.x;
 }
 
 __global__ void select_init(DevBatch b) {

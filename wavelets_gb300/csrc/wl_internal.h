@@ -26,7 +26,9 @@ constexpr int kChunkThreads = 256;
 constexpr int kSelectBins = 4096;       // radix-select digit histogram
 constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
 constexpr int kCandSlices = 64;
-constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float order key         // CTAs per cubelet over its threshold candidates
+constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float order key
+constexpr int kLutStride = kLutCells + 8;  // per-cubelet table stride (16-byte rows)
+constexpr int kQuantGroup = 4;          // chunks per quantize CTA         // CTAs per cubelet over its threshold candidates
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
 constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
 
@@ -154,7 +156,7 @@ struct CubeletDev {
   int lloydIters;
   int tableOff;           // offset into per-cubelet quantizer tables (floats)
   int nTable;             // entries in the table (log: boundaries; lloyd: boundaries)
-  int pad_;
+  int groupBase;          // first quantize group (kQuantGroup chunks per group)
 };
 
 // Device workspace for one batch.
@@ -169,7 +171,7 @@ struct DevBatch {
   unsigned *selHist;              // [n][kSelectBins]
   float *lloydHist;               // [n][kLloydBins][2] (count, sum)
   float *qtable;                  // quantizer tables
-  uint16_t *qlut;                 // [n][kLutCells + 1] Lloyd boundaries below each key cell
+  uint16_t *qlut;                 // [n][kLutStride] Lloyd boundaries below each key cell
   float *dqtable;                 // dequant values [n][binCount]
   unsigned long long *hist;       // [n][kMaxSymbols] Huffman counts
   int4 *chunkRun;                 // per chunk: lead, trail, allZero, len
@@ -181,6 +183,8 @@ struct DevBatch {
   uint32_t *words;                // Huffman output
   long long *chunkPrefix;         // [n+1] chunk prefix (== cub[i].chunkBase)
   int *chunkCub;                  // [totalChunks] cubelet of every chunk
+  int *groupCub;                  // [totalGroups] cubelet of every quantize group
+  long long totalGroups;
   int4 *logHdr;                   // [n] log table layout from the host
   int *meta;                      // packed decode tables and Lloyd codebooks
   long long totalChunks;
