@@ -596,7 +596,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   mark(ctx, 8);
   CU(cudaGetLastError());
   CU(cudaEventRecord(ctx->ev[4], s));
-  launch_encode(b, s);
+  launch_encode(b, maxS, s);
   launch_pack_meta(b, s);
   ctx->launches += 6;
   mark(ctx, 9);

@@ -299,20 +299,36 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, un
   return before + inc - v;
 }
 
+// Bits of a chunk: its stored tokens straight from global memory, plus the
+// tokens of the zero runs crossing its edges (thread 0).
 __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
   __shared__ uint8_t sLen[kMaxSymbols + 3];
-  __shared__ uint16_t list[kMaxChunkTokens];
-  __shared__ int sCount[2];
   __shared__ unsigned long long sh[kThreads / 32];
   const long long chunk = blockIdx.x;
   const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
-  const int dupV = b.state[ci].dupValue;
+  const int dupV = b.state[ci].dupValue, dupKey = cd.binCount;
   const int S = cd.binCount + 1;
   for (int i = threadIdx.x; i < S; i += kThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
-  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);
+  const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
+  const int nInt = b.chunkTok[chunk];
+  const uint16_t *src = b.tok + cd.coefOff + cstart;
+  __syncthreads();
   unsigned long long s = 0;
-  for (int i = threadIdx.x; i < n; i += kThreads) s += token_len(list[i], sLen, cd.binCount);
+  for (int i = threadIdx.x; i < nInt; i += kThreads) s += token_len(src[i], sLen, dupKey);
+  if (threadIdx.x == 0 && dupV >= 0) {
+    const int4 cr = b.chunkRun[chunk];  // lead, trail, allZero, len
+    const long long runIn = b.chunkRunCtx[2 * chunk], runOut = b.chunkRunCtx[2 * chunk + 1];
+    auto add = [&](uint16_t t) { s += token_len(t, sLen, dupKey); };
+    if (cr.x > 0) {
+      const long long e = cr.z ? runOut : cstart + cr.x;
+      run_tokens(runIn, e, cstart, cstart + (cr.z ? cr.w : cr.x), dupKey, dupV, add);
+    }
+    if (!cr.z && cr.y > 0) {
+      const long long s0 = cstart + cr.w - cr.y;
+      run_tokens(s0, runOut, s0, cstart + cr.w, dupKey, dupV, add);
+    }
+  }
   s = block_sum(s, sh);
   if (threadIdx.x == 0) b.chunkBits[chunk] = s;
 }
@@ -398,15 +414,19 @@ __global__ void encode_zero_kernel(DevBatch b) {
   w[(end - 1) >> 5] = 0;
 }
 
-constexpr int kMaxChunkWords = (kChunk * (kMaxCodeBits + 3) + 31) / 32 + 2;
+// Chunk words staged in shared memory; a chunk longer than this (only with
+// very long codes) ORs its bits straight into global memory instead.
+constexpr int kWriteWords = 2048;
+
+__host__ __device__ inline size_t write_smem_bytes(int S) {
+  return (size_t)S * 8 + (((size_t)S + 15) & ~(size_t)15) + (size_t)kWriteWords * 4;
+}
 
 __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
-  __shared__ uint8_t sLen[kMaxSymbols + 3];
-  __shared__ unsigned long long sCode[kMaxSymbols];
   __shared__ uint16_t list[kMaxChunkTokens];
   __shared__ int sCount[2];
   __shared__ unsigned shs[kThreads / 32];
-  extern __shared__ uint32_t sw[];
+  extern __shared__ unsigned long long wsm[];
   const long long chunk = blockIdx.x;
   const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
@@ -414,6 +434,10 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   if (st->error) return;
   const int dupV = st->dupValue, dupKey = cd.binCount;
   const int S = cd.binCount + 1;
+  // tables sized for this cubelet's alphabet (the launch sizes for the largest)
+  unsigned long long *sCode = wsm;
+  uint8_t *sLen = reinterpret_cast<uint8_t *>(sCode + S);
+  uint32_t *sw = reinterpret_cast<uint32_t *>(sLen + ((S + 15) & ~15));
   for (int i = threadIdx.x; i < S; i += kThreads) {
     sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
     sCode[i] = b.codes[(size_t)ci * kMaxSymbols + i];
@@ -423,8 +447,17 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
                                           ? b.chunkBits[chunk + 1] : st->totalBits;
   const int shift = (int)(chunkOff & 31);
   const int nW = (int)((shift + (chunkEnd - chunkOff) + 31) >> 5);
-  for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
-  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);
+  uint32_t *gw = b.words + st->wordsBase + (chunkOff >> 5);
+  const bool staged = nW <= kWriteWords;
+  if (staged) {
+    for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
+  } else {
+    // interior words belong to this chunk alone; the edge words were zeroed
+    // by encode_zero_kernel and are shared with the neighbours
+    for (int i = 1 + threadIdx.x; i < nW - 1; i += kThreads) gw[i] = 0;
+  }
+  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);  // has barriers
+  uint32_t *dstw = staged ? sw : gw;
   // each thread takes a contiguous slice of the tokens
   const int per = (n + kThreads - 1) / kThreads;
   const int t0 = min(n, (int)threadIdx.x * per), t1 = min(n, t0 + per);
@@ -448,14 +481,14 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
       const int o = p & 31;
       const int take = min(l, 32 - o);
       const unsigned part = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
-      atomicOr(&sw[p >> 5], part << o);
+      atomicOr(&dstw[p >> 5], part << o);
       v >>= take;
       p += take;
       l -= take;
     }
   }
+  if (!staged) return;
   __syncthreads();
-  uint32_t *gw = b.words + st->wordsBase + (chunkOff >> 5);
   for (int i = threadIdx.x; i < nW; i += kThreads) {
     if (i == 0 || i == nW - 1) {
       if (sw[i]) atomicOr(&gw[i], sw[i]);
@@ -475,13 +508,14 @@ void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s) {
 
 void launch_pack_meta(DevBatch &b, cudaStream_t s) { pack_meta_kernel<<<b.n, 256, 0, s>>>(b); }
 
-void launch_encode(DevBatch &b, cudaStream_t s) {
+void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const unsigned chunks = (unsigned)b.totalChunks;
   encode_count_kernel<<<chunks, kThreads, 0, s>>>(b);
   encode_scan_kernel<<<b.n, 1024, 0, s>>>(b);
   cubelet_offsets_kernel<<<1, 1, 0, s>>>(b);
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);
-  const int smem = kMaxChunkWords * 4;
+  const int smem = (int)write_smem_bytes(maxSymbols);
+  // static + dynamic above 48 KB needs the opt-in
   cudaFuncSetAttribute(encode_write_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   encode_write_kernel<<<chunks, kThreads, smem, s>>>(b);
 }

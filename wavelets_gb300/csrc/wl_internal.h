@@ -214,7 +214,7 @@ void launch_runs(DevBatch &b, cudaStream_t s);
 
 // launchers (huffman.cu)
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);
-void launch_encode(DevBatch &b, cudaStream_t s);
+void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s);
 void launch_pack_meta(DevBatch &b, cudaStream_t s);
 
 // GPU Huffman decoding (decode.cu)
