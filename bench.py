@@ -294,8 +294,13 @@ def main():
         return float(t.item())
 
     # ---- device-resident batched path (value) ----
+    # Results are released as in steady use (the previous batch's results
+    # live while the next batch runs), so the library's page-locked result
+    # storage is recycled rather than allocated inside a timed step.
+    out = None
     for _ in range(args.warmup):
-        ref_out = ctx.compress_batch(dev_items, on_device=True)
+        out = ctx.compress_batch(dev_items, on_device=True)
+    ref_words = [c.words.copy() for c in out]
     ctx.set_profiling(True)
     kt = {k: 0.0 for k in ctx.KERNEL_GROUPS}
     dev_ms = []
@@ -314,36 +319,8 @@ def main():
     ctx.set_profiling(False)
     step_ms = gmax(statistics.mean(dev_ms))
     comp_bytes = sum(c.compressed_bytes for c in out)
-    same = all(np.array_equal(a.words, b.words) for a, b in zip(out, ref_out))
+    same = all(np.array_equal(a.words, b) for a, b in zip(out, ref_words))
     value = world * in_bytes / (step_ms / 1e3) / 1e9
-
-    # ---- end to end through the public API (pinned host inputs) ----
-    barrier()
-    e2e_t = []
-    for _ in range(max(1, args.steps)):
-        t = time.perf_counter()
-        outh = ctx.compress_batch(host_items, raw=True)
-        e2e_t.append(time.perf_counter() - t)
-    barrier()
-    e2e_ms = gmax(statistics.mean(e2e_t) * 1e3)
-    same_h = all(np.array_equal(a.words, b.words) for a, b in zip(outh, out))
-    d2h = sum(c.compressed_bytes + c.decode.nbytes + c.boundaries.nbytes + c.values.nbytes
-              for c in outh)
-
-    # ---- plain: one cubelet per call ----
-    plain = None
-    if not args.no_plain and len(items) > 1:
-        for it in dev_items[:8]:
-            ctx.compress_batch([it], on_device=True)
-        pt = []
-        single = []
-        for it in dev_items:
-            single.append(ctx.compress_batch([it], on_device=True)[0])
-            pt.append(ctx.timings()[5])
-        plain_ms = sum(pt)
-        plain = {"value": in_bytes / (plain_ms / 1e3) / 1e9, "ms_per_step": plain_ms,
-                 "identical_to_batched": all(np.array_equal(a.words, b.words)
-                                             for a, b in zip(single, out))}
 
     # ---- PSNR on a sample (equal for batched and plain: identical streams) ----
     psnrs = []
@@ -354,6 +331,40 @@ def main():
                                                   else float(x.max() - x.min()))
         mse = float(np.mean((back - x) ** 2))
         psnrs.append(10 * np.log10(peak * peak / mse) if mse > 0 else 999.0)
+    out_words = [c.words.copy() for c in out]
+    del out
+
+    # ---- end to end through the public API (pinned host inputs) ----
+    outh = None
+    for _ in range(2):
+        outh = ctx.compress_batch(host_items, raw=True)
+    barrier()
+    e2e_t = []
+    for _ in range(max(1, args.steps)):
+        t = time.perf_counter()
+        outh = ctx.compress_batch(host_items, raw=True)
+        e2e_t.append(time.perf_counter() - t)
+    barrier()
+    e2e_ms = gmax(statistics.mean(e2e_t) * 1e3)
+    same_h = all(np.array_equal(a.words, b) for a, b in zip(outh, out_words))
+    d2h = sum(c.compressed_bytes + c.decode.nbytes + c.boundaries.nbytes + c.values.nbytes
+              for c in outh)
+    del outh
+
+    # ---- plain: one cubelet per call ----
+    plain = None
+    if not args.no_plain and len(items) > 1:
+        for it in dev_items[:8]:
+            ctx.compress_batch([it], on_device=True)
+        pt = []
+        single = []
+        for it in dev_items:
+            single.append(ctx.compress_batch([it], on_device=True)[0].words.copy())
+            pt.append(ctx.timings()[5])
+        plain_ms = sum(pt)
+        plain = {"value": in_bytes / (plain_ms / 1e3) / 1e9, "ms_per_step": plain_ms,
+                 "identical_to_batched": all(np.array_equal(a, b)
+                                             for a, b in zip(single, out_words))}
 
     # ---- roofline ----
     hbm, peak_kind = peaks()

@@ -90,6 +90,8 @@ typedef struct {
   int32_t *decode;
   int n_boundaries, n_values; /* codebook (Lloyd only) */
   float *boundaries, *values;
+  void *owner;              /* library-internal: shared storage of the arrays
+                               (NULL: each array is its own malloc block) */
 } wl_result;
 
 void wl_result_free(wl_result *r);

@@ -11,12 +11,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "cubelet_io.h"
@@ -74,6 +76,64 @@ bool use_cols(int Xp, int Yp, int Zp, bool identity, const wl_params &p) {
 using PassGroups = std::map<int, std::vector<PassDesc>>;
 int group_key(bool cols, int dtype, int L) {
   return ((cols ? 1 : 0) << 12) | (dtype << 8) | (cols ? ceil_log2_int(L) : 0);
+}
+
+// ---- result storage ------------------------------------------------------------
+// The arrays of all results of one compression call live in one page-locked
+// slab that the device copies into directly (no host-side copy).  Every
+// result holds a reference; the slab returns to a process-wide pool when the
+// last one is released.
+struct ResultSlab {
+  std::atomic<int> refs{0};
+  char *base = nullptr;
+  size_t cap = 0;
+};
+
+class SlabPool {
+ public:
+  ResultSlab *acquire(size_t bytes) {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      int bi = -1;
+      for (int i = 0; i < (int)free_.size(); i++)
+        if (free_[i]->cap >= bytes && (bi < 0 || free_[i]->cap < free_[bi]->cap)) bi = i;
+      if (bi >= 0) {
+        ResultSlab *s = free_[bi];
+        free_.erase(free_.begin() + bi);
+        return s;
+      }
+    }
+    ResultSlab *s = new ResultSlab;
+    const size_t cap = std::max<size_t>(bytes + bytes / 4, (size_t)1 << 20);
+    if (cudaHostAlloc(reinterpret_cast<void **>(&s->base), cap, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      delete s;
+      return nullptr;
+    }
+    s->cap = cap;
+    return s;
+  }
+  void release(ResultSlab *s) {
+    std::lock_guard<std::mutex> g(mu_);
+    free_.push_back(s);
+    while (free_.size() > kKeep) {
+      ResultSlab *o = free_.front();
+      free_.erase(free_.begin());
+      cudaFreeHost(o->base);
+      delete o;
+    }
+  }
+
+ private:
+  static constexpr size_t kKeep = 4;  // free slabs kept for reuse
+  std::mutex mu_;
+  std::vector<ResultSlab *> free_;
+};
+
+// never destroyed: results may be released during process teardown
+SlabPool &slab_pool() {
+  static SlabPool *p = new SlabPool;
+  return *p;
 }
 
 int dtype_size(int dt) {
@@ -453,8 +513,23 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   if (onDevice) {
     for (int i = 0; i < n; i++) dIn[i] = plans[i].data;
   } else {
-    TRY(ensure(ctx, ctx->input, inBytes));
+    // Page-locked host inputs are read in place by the first transform pass
+    // (the GPU reaches pinned memory directly); pageable ones are copied.
+    bool staged = false;
     for (int i = 0; i < n; i++) {
+      cudaPointerAttributes attr;
+      if (cudaPointerGetAttributes(&attr, plans[i].data) == cudaSuccess &&
+          attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+        dIn[i] = attr.devicePointer;
+      } else {
+        cudaGetLastError();
+        dIn[i] = nullptr;
+        staged = true;
+      }
+    }
+    if (staged) TRY(ensure(ctx, ctx->input, inBytes));
+    for (int i = 0; i < n; i++) {
+      if (dIn[i]) continue;
       const Plan &pl = plans[i];
       char *dst = P<char>(ctx->input) + pl.inOff;
       CU(cudaMemcpyAsync(dst, pl.data, (size_t)pl.X * pl.Y * pl.Z * dtype_size(pl.dtype),
@@ -615,23 +690,35 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
                   i, hs[i].error);
     totalWords += hs[i].nWords;
   }
-  TRY(ensure_host(ctx, ctx->hWords, (size_t)totalWords * 4));
   size_t metaInts = 0;
   for (int i = 0; i < n; i++)
     metaInts += hs[i].nDecode + (plans[i].p.quant_alg == WL_LLOYD ? hs[i].nBounds + hs[i].nValues : 0);
-  TRY(ensure_host(ctx, ctx->hDecode, metaInts * 4 + 16));
-  if (totalWords)
-    CU(cudaMemcpyAsync(ctx->hWords.p, b.words, (size_t)totalWords * 4, cudaMemcpyDeviceToHost, s));
-  if (metaInts)
-    CU(cudaMemcpyAsync(ctx->hDecode.p, b.meta, metaInts * 4, cudaMemcpyDeviceToHost, s));
-  int *hd = H<int>(ctx->hDecode);
+  // words, then the packed decode tables and codebooks, straight into the slab
+  const size_t wordsBytes = ((size_t)totalWords * 4 + 15) & ~(size_t)15;
+  ResultSlab *slab = slab_pool().acquire(wordsBytes + metaInts * 4 + 16);
+  if (!slab) return fail(ctx, WL_ENOMEM, "cannot allocate %zu bytes of page-locked result storage",
+                         wordsBytes + metaInts * 4 + 16);
+  uint32_t *hw = reinterpret_cast<uint32_t *>(slab->base);
+  int *hd = reinterpret_cast<int *>(slab->base + wordsBytes);
+  if (totalWords) {
+    const cudaError_t e = cudaMemcpyAsync(hw, b.words, (size_t)totalWords * 4, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+  }
+  if (metaInts) {
+    const cudaError_t e = cudaMemcpyAsync(hd, b.meta, metaInts * 4, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+  }
   std::vector<size_t> decOff(n), cbOff(n, 0);
   for (int i = 0; i < n; i++) {
     decOff[i] = (size_t)hs[i].metaBase;
     cbOff[i] = (size_t)hs[i].metaBase + hs[i].nDecode;
   }
-  CU(cudaEventRecord(ctx->ev[6], s));
-  CU(cudaStreamSynchronize(s));
+  {
+    cudaError_t e = cudaEventRecord(ctx->ev[6], s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+  }
+  slab->refs.store(n);
 
   float t[6];
   cudaEventElapsedTime(&t[0], ctx->ev[0], ctx->ev[1]);
@@ -644,7 +731,6 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   if (ctx->profiling)
     for (int g = 0; g < 9; g++) cudaEventElapsedTime(&ctx->ktimes[g], ctx->pev[g], ctx->pev[g + 1]);
 
-  const uint32_t *hw = H<uint32_t>(ctx->hWords);
   for (int i = 0; i < n; i++) {
     const Plan &pl = plans[i];
     const CubeletState &st = hs[i];
@@ -667,19 +753,16 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     r.dup_value = st.dupValue;
     r.dup_key = st.dupValue >= 0 ? pl.p.bin_count : -1;
     r.longest_code = st.longest;
+    r.owner = slab;
     r.n_words = st.nWords;
-    r.words = (uint32_t *)malloc((size_t)std::max(1, st.nWords) * 4);
-    memcpy(r.words, hw + st.wordsBase, (size_t)st.nWords * 4);
+    r.words = hw + st.wordsBase;
     r.n_decode = st.nDecode;
-    r.decode = (int32_t *)malloc((size_t)std::max(1, st.nDecode) * 4);
-    memcpy(r.decode, hd + decOff[i], (size_t)st.nDecode * 4);
+    r.decode = hd + decOff[i];
     if (pl.p.quant_alg == WL_LLOYD) {
       r.n_boundaries = st.nBounds;
       r.n_values = st.nValues;
-      r.boundaries = (float *)malloc((size_t)std::max(1, st.nBounds) * 4);
-      r.values = (float *)malloc((size_t)std::max(1, st.nValues) * 4);
-      memcpy(r.boundaries, hd + cbOff[i], (size_t)st.nBounds * 4);
-      memcpy(r.values, hd + cbOff[i] + st.nBounds, (size_t)st.nValues * 4);
+      r.boundaries = reinterpret_cast<float *>(hd + cbOff[i]);
+      r.values = reinterpret_cast<float *>(hd + cbOff[i] + st.nBounds);
     }
   }
   return WL_OK;
@@ -894,10 +977,15 @@ void wl_params_default(wl_params *p) {
 
 void wl_result_free(wl_result *r) {
   if (!r) return;
-  free(r->words);
-  free(r->decode);
-  free(r->boundaries);
-  free(r->values);
+  if (r->owner) {
+    ResultSlab *s = static_cast<ResultSlab *>(r->owner);
+    if (s->refs.fetch_sub(1) == 1) slab_pool().release(s);
+  } else {
+    free(r->words);
+    free(r->decode);
+    free(r->boundaries);
+    free(r->values);
+  }
   memset(r, 0, sizeof *r);
 }
 

@@ -51,7 +51,8 @@ class WlResult(ctypes.Structure):
                 ("n_decode", ctypes.c_int), ("decode", ctypes.POINTER(ctypes.c_int32)),
                 ("n_boundaries", ctypes.c_int), ("n_values", ctypes.c_int),
                 ("boundaries", ctypes.POINTER(ctypes.c_float)),
-                ("values", ctypes.POINTER(ctypes.c_float))]
+                ("values", ctypes.POINTER(ctypes.c_float)),
+                ("owner", ctypes.c_void_p)]
 
 
 class WlCubelet(ctypes.Structure):
@@ -171,7 +172,9 @@ class Compressed:
         def arr(ptr, n, dt):
             if n <= 0 or not ptr:
                 return np.zeros(0, dt)
-            return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt, copy=True)
+            a = np.empty(n, dt)
+            ctypes.memmove(a.ctypes.data, ctypes.cast(ptr, ctypes.c_void_p).value, a.nbytes)
+            return a
         return cls(tuple(r.size), tuple(r.original_size), r.original_dtype, tuple(r.steps),
                    r.wavelet, r.quant_alg, r.bin_count, r.threshold_fraction,
                    r.threshold_value, r.max_value, r.min_coef, r.max_coef, r.zero_bin,
@@ -218,6 +221,81 @@ def _size_of(arr: np.ndarray):
     a = arr if arr.ndim == 3 else arr.reshape((1,) * (3 - arr.ndim) + arr.shape)
     Z, Y, X = a.shape
     return (X, Y, Z)
+
+
+class _ResultsOwner:
+    """Releases the library results whose arrays numpy views point into."""
+
+    def __init__(self, lib, outs, n):
+        self.lib, self.outs, self.n = lib, outs, n
+
+    def __del__(self):
+        try:
+            for i in range(self.n):
+                self.lib.wl_result_free(ctypes.byref(self.outs[i]))
+        except Exception:
+            pass
+
+
+def _result_dtype():
+    """numpy mirror of WlResult for vectorised field access."""
+    names, formats, offsets = [], [], []
+    for name, ct in WlResult._fields_:
+        f = getattr(WlResult, name)
+        if name in ("words", "decode", "boundaries", "values", "owner"):
+            fmt = np.uint64
+        elif isinstance(ct, type) and issubclass(ct, ctypes.Array):
+            fmt = (np.int32, (ct._length_,))
+        elif ct is ctypes.c_float:
+            fmt = np.float32
+        else:
+            fmt = np.int32
+        names.append(name)
+        formats.append(fmt)
+        offsets.append(f.offset)
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                     "itemsize": ctypes.sizeof(WlResult)})
+
+
+_RESULT_DT = None
+
+
+def adopt_results(lib, outs, n) -> List["Compressed"]:
+    """Compressed objects over the results' arrays without copying them.  The
+    library keeps a batch's arrays in one block; the numpy views hold a
+    reference that releases the results when the last view goes away."""
+    global _RESULT_DT
+    if _RESULT_DT is None:
+        _RESULT_DT = _result_dtype()
+    rec = np.frombuffer(outs, _RESULT_DT, count=n)
+    ptrs = np.stack([rec["words"], rec["decode"], rec["boundaries"], rec["values"]], 1)
+    cnts = np.stack([rec["n_words"], rec["n_decode"], rec["n_boundaries"], rec["n_values"]],
+                    1).astype(np.int64)
+    used = (cnts > 0) & (ptrs != 0)
+    if n == 0 or not used.any() or not (rec["owner"] != 0).all():
+        res = [Compressed.from_struct(outs[i]) for i in range(n)]
+        for i in range(n):
+            lib.wl_result_free(ctypes.byref(outs[i]))
+        return res
+    lo = int(ptrs[used].min())
+    hi = int((ptrs + 4 * cnts.astype(np.uint64))[used].max())
+    buf = (ctypes.c_char * (hi - lo)).from_address(lo)
+    buf._owner = _ResultsOwner(lib, outs, n)
+    base = np.frombuffer(buf, np.uint8)
+    rel = np.where(used, ptrs - np.uint64(lo), 0).astype(np.int64).tolist()
+    cl = np.where(used, cnts, 0).tolist()
+    dts = (np.uint32, np.int32, np.float32, np.float32)
+    res = []
+    for i, r in enumerate(rec.tolist()):
+        arrs = [base[o:o + 4 * c].view(dt) for o, c, dt in zip(rel[i], cl[i], dts)]
+        d = dict(zip(_RESULT_DT.names, r))
+        res.append(Compressed(tuple(int(v) for v in d["size"]),
+                              tuple(int(v) for v in d["original_size"]), d["original_dtype"],
+                              tuple(int(v) for v in d["steps"]), d["wavelet"], d["quant_alg"], d["bin_count"],
+                              d["threshold_fraction"], d["threshold_value"], d["max_value"],
+                              d["min_coef"], d["max_coef"], d["zero_bin"], d["dup_key"],
+                              d["dup_value"], d["longest_code"], *arrs))
+    return res
 
 
 class Context:
@@ -268,9 +346,7 @@ class Context:
                                           1 if on_device else 0, ctypes.byref(make_params(params)),
                                           ctypes.byref(res))
         self._check(st)
-        out = Compressed.from_struct(res)
-        self.lib.wl_result_free(ctypes.byref(res))
-        return out
+        return adopt_results(self.lib, (WlResult * 1)(res), 1)[0]
 
     def compress_batch(self, items: Sequence, params=None, on_device: bool = False,
                        raw: bool = False) -> List[Compressed]:
@@ -297,10 +373,7 @@ class Context:
         outs = (WlResult * n)()
         st = self.lib.wl_compress_batch(self.h, cubs, n, 1 if on_device else 0, outs)
         self._check(st)
-        res = [Compressed.from_struct(outs[i]) for i in range(n)]
-        for i in range(n):
-            self.lib.wl_result_free(ctypes.byref(outs[i]))
-        return res
+        return adopt_results(self.lib, outs, n)
 
     def decompress(self, c: Compressed, dtype=None) -> np.ndarray:
         """Restore a cubelet; dtype defaults to the original."""
