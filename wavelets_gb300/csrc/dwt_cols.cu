@@ -250,6 +250,36 @@ __device__ __forceinline__ void haar_seg(float *x, int P, int i0, int i1, bool i
   }
 }
 
+// 8- and 16-bit rows read from host memory: each lane loads 16 bytes (V
+// elements) of the row's first n real elements when the row is 16-byte
+// aligned (few large requests suit the host link; from device memory the
+// per-element loads are faster), and stores them into the transposed tile in
+// V steps.  Lane l starts at element rot = l V / 32 (mod V) of its vector,
+// which puts the 32 stores of a step in 32 different banks.  Returns how many
+// leading elements were loaded.
+template <typename InT>
+__device__ __forceinline__ int load_row_vec(float *trow, const InT *src, int n, int lane) {
+  constexpr int V = 16 / (int)sizeof(InT);
+  if ((reinterpret_cast<size_t>(src) & 15) != 0) return 0;
+  const int nv = n / V;
+  const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+  const int rot = (lane * V / 32) & (V - 1);
+  for (int v = lane; v < nv; v += 32) {
+    const uint4 q = s4[v];
+    float *dst = trow + v * V * kP;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+      const int idx = (k + rot) & (V - 1);
+      constexpr int perWord = 4 / (int)sizeof(InT);
+      const int wi = idx / perWord, sh = (idx % perWord) * 8 * (int)sizeof(InT);
+      const unsigned word = (wi & 2) ? ((wi & 1) ? q.w : q.z) : ((wi & 1) ? q.y : q.x);
+      const unsigned e = (word >> sh) & (sizeof(InT) == 1 ? 0xffu : 0xffffu);
+      dst[idx * kP] = (float)e;
+    }
+  }
+  return nv * V;
+}
+
 // lane group for rows of `len` elements moved `len`-wide
 __device__ __forceinline__ int group_width(int len) {
   if (len >= 32) return 32;
@@ -258,7 +288,7 @@ __device__ __forceinline__ int group_width(int len) {
   return G;
 }
 
-template <typename InT, typename OutT, bool INV>
+template <typename InT, typename OutT, bool INV, bool VEC>
 __global__ void __launch_bounds__(kThreadsC)
 dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                 int nPasses) {
@@ -337,7 +367,9 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       float *trow = tile + rr;
       if (!INV) {
         const int cl = min(L, d.clampL) - 1;
-        for (int c = sub; c < L; c += G) stage(trow + c * kP, src + min(c, cl));
+        int c0 = 0;
+        if (VEC && G == 32) c0 = load_row_vec(trow, src, cl + 1, lane);
+        for (int c = c0 + sub; c < L; c += G) stage(trow + c * kP, src + min(c, cl));
       } else {
         for (int p = sub; p < L; p += G) {
           int lev;
@@ -428,9 +460,9 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   }
 }
 
-template <typename InT, typename OutT, bool INV>
+template <typename InT, typename OutT, bool INV, bool VEC = false>
 void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, cudaStream_t s) {
-  auto k = dwt_cols_kernel<InT, OutT, INV>;
+  auto k = dwt_cols_kernel<InT, OutT, INV, VEC>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   k<<<tiles, kThreadsC, smem, s>>>(p, tp, n);
@@ -443,11 +475,17 @@ int dwt_cols_tile_rows() { return kRows; }
 int dwt_cols_smem_bytes(int L) { return L * kP * (int)sizeof(float); }
 
 void launch_dwt_cols(const PassDesc *p, const int *tp, int n, int tiles, int smem, int inType,
-                     int outType, bool inverse, cudaStream_t s) {
+                     int outType, bool inverse, bool vecLoad, cudaStream_t s) {
   if (!inverse) {
     switch (inType) {
-      case WL_U8: launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, s); break;
-      case WL_U16: launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, s); break;
+      case WL_U8:
+        if (vecLoad) launch_t<uint8_t, float, false, true>(p, tp, n, tiles, smem, s);
+        else launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, s);
+        break;
+      case WL_U16:
+        if (vecLoad) launch_t<uint16_t, float, false, true>(p, tp, n, tiles, smem, s);
+        else launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, s);
+        break;
       case WL_I32: launch_t<int32_t, float, false>(p, tp, n, tiles, smem, s); break;
       default: launch_t<float, float, false>(p, tp, n, tiles, smem, s); break;
     }

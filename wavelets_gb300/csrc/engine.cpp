@@ -74,8 +74,9 @@ bool use_cols(int Xp, int Yp, int Zp, bool identity, const wl_params &p) {
 // length class): a launch's shared memory is sized for its longest row, so
 // rows of very different lengths go to different launches.
 using PassGroups = std::map<int, std::vector<PassDesc>>;
-int group_key(bool cols, int dtype, int L) {
-  return ((cols ? 1 : 0) << 12) | (dtype << 8) | (cols ? ceil_log2_int(L) : 0);
+int group_key(bool cols, int dtype, int L, bool vec = false) {
+  return ((vec ? 1 : 0) << 13) | ((cols ? 1 : 0) << 12) | (dtype << 8) |
+         (cols ? ceil_log2_int(L) : 0);
 }
 
 // ---- result storage ------------------------------------------------------------
@@ -261,7 +262,7 @@ wl_status check_params(wl_ctx *ctx, const wl_params &p) {
 // z pass z-x-y in place (a-b-c lists axes from fastest to slowest).  Rows
 // are numbered so that neighbouring rows are neighbours in memory on every
 // side whose element stride is not 1.
-void forward_passes_cols(const Plan &pl, const void *in, float *coef, float *coef2,
+void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
                          PassGroups &xs, PassGroups &ys, PassGroups &zs) {
   const int big = 0x7fffffff;
   const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
@@ -274,6 +275,7 @@ void forward_passes_cols(const Plan &pl, const void *in, float *coef, float *coe
   d.wavelet = pl.p.wavelet;
   // x pass: rows (a = y, b = z), REPEAT padding by clamping
   d.in = in;
+  d.vecLoad = hostIn ? 1 : 0;
   d.inSA = pl.X; d.inSB = (long long)pl.X * pl.Y; d.inSC = 1;
   d.clampL = pl.X; d.clampA = pl.Y; d.clampB = pl.Z;
   d.L = pl.Xp; d.B = pl.Zp; d.rows = (int)(Yp * Zp);
@@ -281,10 +283,11 @@ void forward_passes_cols(const Plan &pl, const void *in, float *coef, float *coe
   d.outSA = Zp; d.outSB = 1; d.outSC = Zp * Yp;
   d.steps = pl.sx;
   d.T = T; d.tiles = (d.rows + T - 1) / T;
-  xs[group_key(true, pl.dtype, d.L)].push_back(d);
+  xs[group_key(true, pl.dtype, d.L, hostIn && dtype_size(pl.dtype) < 4)].push_back(d);
   // y pass: rows (a = x, b = z) of z-y-x -> z-x-y
   PassDesc e = d;
   e.clampL = e.clampB = e.clampA = big;
+  e.vecLoad = 0;
   e.in = o2;
   e.inSA = Zp * Yp; e.inSB = 1; e.inSC = Zp;
   e.L = pl.Yp; e.B = pl.Zp; e.rows = (int)(Zp * Xp);
@@ -306,10 +309,10 @@ void forward_passes_cols(const Plan &pl, const void *in, float *coef, float *coe
   zs[group_key(true, WL_F32, f.L)].push_back(f);
 }
 
-void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
+void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
                     PassGroups &xs, PassGroups &ys, PassGroups &zs) {
   if (pl.cols) {
-    forward_passes_cols(pl, in, coef, coef2, xs, ys, zs);
+    forward_passes_cols(pl, in, hostIn, coef, coef2, xs, ys, zs);
     return;
   }
   const int big = 0x7fffffff;
@@ -371,7 +374,8 @@ void forward_passes(const Plan &pl, const void *in, float *coef, float *coef2,
 
 // Upload a group of passes (descriptor + tile prefix) and launch it.
 wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
-                    int inType, int outType, bool inverse, bool cols = false) {
+                    int inType, int outType, bool inverse, bool cols = false,
+                    bool vecLoad = false) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int) + 64;
@@ -394,7 +398,7 @@ wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
   const PassDesc *dp = reinterpret_cast<const PassDesc *>(d);
   const int *dtp = reinterpret_cast<const int *>(d + n * sizeof(PassDesc));
   if (cols)
-    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
+    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, vecLoad, ctx->stream);
   else
     launch_dwt_pass(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
   CU(cudaGetLastError());
@@ -405,9 +409,9 @@ wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
 wl_status run_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int outType,
                      bool inverse) {
   for (const auto &kv : gs) {
-    const bool cols = (kv.first >> 12) & 1;
+    const bool cols = (kv.first >> 12) & 1, vec = (kv.first >> 13) & 1;
     const int dt = (kv.first >> 8) & 15;
-    TRY(run_group(ctx, kv.second, hoff, inverse ? WL_F32 : dt, outType, inverse, cols));
+    TRY(run_group(ctx, kv.second, hoff, inverse ? WL_F32 : dt, outType, inverse, cols, vec));
   }
   return WL_OK;
 }
@@ -510,6 +514,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
 
   // ---- inputs ----
   std::vector<const void *> dIn(n);
+  std::vector<char> hostIn(n, 0);  // input read in place from page-locked host memory
   if (onDevice) {
     for (int i = 0; i < n; i++) dIn[i] = plans[i].data;
   } else {
@@ -521,6 +526,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       if (cudaPointerGetAttributes(&attr, plans[i].data) == cudaSuccess &&
           attr.type == cudaMemoryTypeHost && attr.devicePointer) {
         dIn[i] = attr.devicePointer;
+        hostIn[i] = 1;
       } else {
         cudaGetLastError();
         dIn[i] = nullptr;
@@ -603,7 +609,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   ctx->launches = 0;
   PassGroups xs, ys, zs;
   for (int i = 0; i < n; i++)
-    forward_passes(plans[i], dIn[i], b.coef, b.coef2, xs, ys, zs);
+    forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs, ys, zs);
   size_t hoff = 0;
   mark(ctx, 0);
   TRY(run_groups(ctx, xs, hoff, WL_F32, false));

@@ -102,6 +102,7 @@ struct PassDesc {
   int exact;      // reference float order (filter bank) instead of lifting
   int clampL, clampB, clampA;  // forward load: source sizes (REPEAT padding)
   int cropL, cropB, cropA;     // inverse store: destination sizes (crop)
+  int vecLoad;                 // source is page-locked host memory: 16-byte row loads
 };
 
 // Per-cubelet state written by the kernels and read back by the host.
@@ -199,7 +200,8 @@ int dwt_smem_bytes(int L, int T, bool exact);
 // column-tile passes (dwt_cols.cu): lifting / Haar, rows up to kColsMaxL
 constexpr int kColsMaxL = 512;
 void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int tiles,
-                     int smem, int inType, int outType, bool inverse, cudaStream_t s);
+                     int smem, int inType, int outType, bool inverse, bool vecLoad,
+                     cudaStream_t s);
 int dwt_cols_tile_rows();
 int dwt_cols_smem_bytes(int L);
 

@@ -283,18 +283,23 @@ def adopt_results(lib, outs, n) -> List["Compressed"]:
     buf._owner = _ResultsOwner(lib, outs, n)
     base = np.frombuffer(buf, np.uint8)
     rel = np.where(used, ptrs - np.uint64(lo), 0).astype(np.int64).tolist()
-    cl = np.where(used, cnts, 0).tolist()
-    dts = (np.uint32, np.int32, np.float32, np.float32)
+    ends = (np.where(used, ptrs - np.uint64(lo), 0).astype(np.int64)
+            + 4 * np.where(used, cnts, 0)).tolist()
+    f = {k: rec[k].tolist() for k in _RESULT_DT.names if k not in ("words", "decode",
+                                                                    "boundaries", "values", "owner")}
+    e32, ef = np.zeros(0, np.float32), np.zeros(0, np.float32)
     res = []
-    for i, r in enumerate(rec.tolist()):
-        arrs = [base[o:o + 4 * c].view(dt) for o, c, dt in zip(rel[i], cl[i], dts)]
-        d = dict(zip(_RESULT_DT.names, r))
-        res.append(Compressed(tuple(int(v) for v in d["size"]),
-                              tuple(int(v) for v in d["original_size"]), d["original_dtype"],
-                              tuple(int(v) for v in d["steps"]), d["wavelet"], d["quant_alg"], d["bin_count"],
-                              d["threshold_fraction"], d["threshold_value"], d["max_value"],
-                              d["min_coef"], d["max_coef"], d["zero_bin"], d["dup_key"],
-                              d["dup_value"], d["longest_code"], *arrs))
+    for i in range(n):
+        o, z = rel[i], ends[i]
+        res.append(Compressed(
+            tuple(f["size"][i]), tuple(f["original_size"][i]), f["original_dtype"][i],
+            tuple(f["steps"][i]), f["wavelet"][i], f["quant_alg"][i], f["bin_count"][i],
+            f["threshold_fraction"][i], f["threshold_value"][i], f["max_value"][i],
+            f["min_coef"][i], f["max_coef"][i], f["zero_bin"][i], f["dup_key"][i],
+            f["dup_value"][i], f["longest_code"][i],
+            base[o[0]:z[0]].view(np.uint32), base[o[1]:z[1]].view(np.int32),
+            base[o[2]:z[2]].view(np.float32) if z[2] > o[2] else e32,
+            base[o[3]:z[3]].view(np.float32) if z[3] > o[3] else ef))
     return res
 
 
