@@ -11,9 +11,13 @@
 // segments of pairs, which gives the SM four times the warps a one-warp tile
 // would at the same shared memory.
 //
-// Tile layout in shared memory: element p of tile row r at tile[p * 33 + r].
-// Lanes reading one position of their 32 rows hit 32 banks; a warp walking
-// the positions of one row (stride 33 words) also hits 32 banks.  Each side
+// Rows of at most 64 elements use 128-row tiles instead: each warp sweeps 32
+// rows whole, with no halos and no barriers between levels.
+//
+// Tile layout in shared memory: element p of tile row r at tile[p * (R+1) + r]
+// for an R-row tile.  Lanes reading one position of 32 neighbouring rows hit
+// 32 banks; a warp walking the positions of one row (odd stride) also hits
+// 32 banks.  Each side
 // of a pass picks its access pattern from the strides of the global layout:
 //   - rows consecutive in memory (element stride != 1): every lane moves its
 //     own row, so a warp access covers one element of 32 neighbouring rows
@@ -41,7 +45,6 @@ namespace {
 using namespace dwtc;
 
 constexpr int kRows = 32;         // rows per tile (one per lane)
-constexpr int kP = kRows + 1;     // words between consecutive positions of a row
 constexpr int kSeg = 4;           // warps per CTA = segments per level
 constexpr int kThreadsC = 32 * kSeg;
 
@@ -258,7 +261,8 @@ __device__ __forceinline__ void haar_seg(float *x, int P, int i0, int i1, bool i
 // which puts the 32 stores of a step in 32 different banks.  Returns how many
 // leading elements were loaded.
 template <typename InT>
-__device__ __forceinline__ int load_row_vec(float *trow, const InT *src, int n, int lane) {
+__device__ __forceinline__ int load_row_vec(float *trow, const InT *src, int n, int lane,
+                                            int pitch) {
   constexpr int V = 16 / (int)sizeof(InT);
   if ((reinterpret_cast<size_t>(src) & 15) != 0) return 0;
   const int nv = n / V;
@@ -266,7 +270,7 @@ __device__ __forceinline__ int load_row_vec(float *trow, const InT *src, int n, 
   const int rot = (lane * V / 32) & (V - 1);
   for (int v = lane; v < nv; v += 32) {
     const uint4 q = s4[v];
-    float *dst = trow + v * V * kP;
+    float *dst = trow + v * V * pitch;
 #pragma unroll
     for (int k = 0; k < V; k++) {
       const int idx = (k + rot) & (V - 1);
@@ -274,7 +278,7 @@ __device__ __forceinline__ int load_row_vec(float *trow, const InT *src, int n, 
       const int wi = idx / perWord, sh = (idx % perWord) * 8 * (int)sizeof(InT);
       const unsigned word = (wi & 2) ? ((wi & 1) ? q.w : q.z) : ((wi & 1) ? q.y : q.x);
       const unsigned e = (word >> sh) & (sizeof(InT) == 1 ? 0xffu : 0xffffu);
-      dst[idx * kP] = (float)e;
+      dst[idx * pitch] = (float)e;
     }
   }
   return nv * V;
@@ -288,13 +292,19 @@ __device__ __forceinline__ int group_width(int len) {
   return G;
 }
 
-template <typename InT, typename OutT, bool INV, bool VEC>
+// ROWS = 32: the four warps share the tile's 32 rows and split every level
+// into segments (long rows).  ROWS = 128: every warp owns 32 rows of the
+// tile and sweeps them whole, with no halos and no barriers between levels
+// (rows of at most 64 elements, where segments would be mostly halo).
+template <typename InT, typename OutT, bool INV, bool VEC, int ROWS>
 __global__ void __launch_bounds__(kThreadsC)
 dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                 int nPasses) {
+  constexpr int kP = ROWS + 1;                 // words between positions of a row
+  constexpr int kSegs = ROWS == kRows ? kSeg : 1;
   extern __shared__ float4 smem4[];
   float *tile = reinterpret_cast<float *>(smem4);
-  __shared__ long long rowIn[kRows], rowOut[kRows];
+  __shared__ long long rowIn[ROWS], rowOut[ROWS];
   __shared__ float scaleTab[32];
 
   const int bid = blockIdx.x;
@@ -306,14 +316,17 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   const PassDesc &d = passes[lo];
   const int L = d.L, S = d.steps;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int r0 = (bid - tilePrefix[lo]) * kRows;
-  const int nr = min(kRows, d.rows - r0);
+  const int r0 = (bid - tilePrefix[lo]) * ROWS;
+  const int nr = min(ROWS, d.rows - r0);
+  // the row this thread moves and computes, and its share of the elements
+  const int me = ROWS == kRows ? lane : (int)threadIdx.x;
+  const int cFirst = ROWS == kRows ? warp : 0, cStep = ROWS == kRows ? kSeg : 1;
   // exact-order CDF 9/7 passes never come here (they run in dwt.cu)
   const bool lifting = d.wavelet == WL_CDF97;
-  if (warp == 0) {
-    const int r = r0 + lane;
+  if ((int)threadIdx.x < ROWS) {
+    const int r = r0 + threadIdx.x;
     long long bi = 0, bo = -1;
-    if (lane < nr) {
+    if ((int)threadIdx.x < nr) {
       const int a = r / d.B, b = r - a * d.B;
       if (!INV)
         bi = (long long)min(a, d.clampA - 1) * d.inSA + (long long)min(b, d.clampB - 1) * d.inSB;
@@ -321,31 +334,31 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
         bi = (long long)a * d.inSA + (long long)b * d.inSB;
       if (a < d.cropA && b < d.cropB) bo = (long long)a * d.outSA + (long long)b * d.outSB;
     }
-    rowIn[lane] = bi;
-    rowOut[lane] = bo;
-  } else if (warp == 1 && lane <= S) {
-    scaleTab[lane] = lifting ? lifting_scale(lane, S) : 1.0f;
+    rowIn[threadIdx.x] = bi;
+    rowOut[threadIdx.x] = bo;
   }
+  if (threadIdx.x >= kThreadsC - 32 && lane <= S)
+    scaleTab[lane] = lifting ? lifting_scale(lane, S) : 1.0f;
   __syncthreads();
 
   // ---- load ----------------------------------------------------------------
   const InT *in = static_cast<const InT *>(d.in);
   const long long inSC = d.inSC;
   if (inSC != 1) {
-    // own row: lanes cover one element of 32 neighbouring rows; the warps
-    // take every fourth element
-    if (lane < nr) {
-      const InT *src = in + rowIn[lane];
-      float *col = tile + lane;
+    // own row: lanes cover one element of 32 neighbouring rows (with 32 rows
+    // the warps take every fourth element)
+    if (me < nr) {
+      const InT *src = in + rowIn[me];
+      float *col = tile + me;
       if (!INV) {
         const int cl = min(L, d.clampL) - 1;
-        for (int c = warp; c < L; c += kSeg)
+        for (int c = cFirst; c < L; c += cStep)
           stage(col + c * kP, src + (long long)min(c, cl) * inSC);
       } else {
         // band order -> in-place positions, undoing the deferred scale
         const int nLow = L >> S;
         const float sl = scaleTab[S];
-        for (int q = warp; q < nLow; q += kSeg)
+        for (int q = cFirst; q < nLow; q += cStep)
           col[(q << S) * kP] = load_as_float(src + q * inSC) / sl;
         for (int t = 0; t < S; t++) {
           const int qs = L >> (t + 1);
@@ -353,7 +366,7 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
           const InT *sb = src + (long long)qs * inSC;
           float *cb = col + (1 << t) * kP;
           const int step = (2 << t) * kP;
-          for (int k = warp; k < qs; k += kSeg) cb[k * step] = load_as_float(sb + k * inSC) / st;
+          for (int k = cFirst; k < qs; k += cStep) cb[k * step] = load_as_float(sb + k * inSC) / st;
         }
       }
     }
@@ -368,7 +381,7 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       if (!INV) {
         const int cl = min(L, d.clampL) - 1;
         int c0 = 0;
-        if (VEC && G == 32) c0 = load_row_vec(trow, src, cl + 1, lane);
+        if (VEC && G == 32) c0 = load_row_vec(trow, src, cl + 1, lane, kP);
         for (int c = c0 + sub; c < L; c += G) stage(trow + c * kP, src + min(c, cl));
       } else {
         for (int p = sub; p < L; p += G) {
@@ -383,12 +396,13 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   __syncthreads();
 
   // ---- levels --------------------------------------------------------------
-  float *x = tile + lane;
-  const bool rowOk = lane < nr;
+  float *x = tile + me;
+  const bool rowOk = me < nr;
   for (int it = 0; it < S; it++) {
     const int lev = INV ? S - 1 - it : it;
     const int h = (L >> lev) >> 1, P = (1 << lev) * kP;
-    const int i0 = (warp * h) / kSeg, i1 = ((warp + 1) * h) / kSeg;
+    const int i0 = kSegs == 1 ? 0 : (warp * h) / kSegs;
+    const int i1 = kSegs == 1 ? h : ((warp + 1) * h) / kSegs;
     if (!lifting) {
       if (rowOk) haar_seg(x, P, i0, i1, INV);
     } else if (h == 1) {
@@ -401,28 +415,31 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
         }
       }
     } else {
-      Halo hb;
-      if (rowOk && i0 < i1) capture_halo(x, h, P, i0, i1, hb);
-      __syncthreads();
+      Halo hb = {};
+      if (kSegs > 1) {
+        if (rowOk && i0 < i1) capture_halo(x, h, P, i0, i1, hb);
+        __syncthreads();
+      }
       if (rowOk && i0 < i1) {
         if (!INV) lift_fwd_seg(x, h, P, i0, i1, hb);
         else lift_inv_seg(x, h, P, i0, i1, hb);
       }
     }
-    __syncthreads();
+    if (kSegs > 1) __syncthreads();
   }
+  if (kSegs == 1) __syncthreads();
 
   // ---- store ---------------------------------------------------------------
   OutT *out = static_cast<OutT *>(d.out);
   const long long outSC = d.outSC;
   if (outSC != 1) {
-    if (lane < nr && rowOut[lane] >= 0) {
-      OutT *dst = out + rowOut[lane];
-      const float *col = tile + lane;
+    if (me < nr && rowOut[me] >= 0) {
+      OutT *dst = out + rowOut[me];
+      const float *col = tile + me;
       if (!INV) {
         const int nLow = L >> S;
         const float sl = scaleTab[S];
-        for (int q = warp; q < nLow; q += kSeg)
+        for (int q = cFirst; q < nLow; q += cStep)
           store_from_float(dst + q * outSC, col[(q << S) * kP] * sl);
         for (int t = 0; t < S; t++) {
           const int qs = L >> (t + 1);
@@ -430,12 +447,12 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
           OutT *db = dst + (long long)qs * outSC;
           const float *cb = col + (1 << t) * kP;
           const int step = (2 << t) * kP;
-          for (int k = warp; k < qs; k += kSeg)
+          for (int k = cFirst; k < qs; k += cStep)
             store_from_float(db + k * outSC, cb[k * step] * st);
         }
       } else {
         const int Lc = min(L, d.cropL);
-        for (int c = warp; c < Lc; c += kSeg) store_from_float(dst + c * outSC, col[c * kP]);
+        for (int c = cFirst; c < Lc; c += cStep) store_from_float(dst + c * outSC, col[c * kP]);
       }
     }
   } else {
@@ -461,8 +478,10 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
 }
 
 template <typename InT, typename OutT, bool INV, bool VEC = false>
-void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, cudaStream_t s) {
-  auto k = dwt_cols_kernel<InT, OutT, INV, VEC>;
+void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
+              cudaStream_t s) {
+  auto k = rows == kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows>
+                         : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   k<<<tiles, kThreadsC, smem, s>>>(p, tp, n);
@@ -470,31 +489,32 @@ void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, cuda
 
 }  // namespace
 
-int dwt_cols_tile_rows() { return kRows; }
+// rows of at most 64 elements: 128-row tiles swept whole by each warp
+int dwt_cols_tile_rows(int L) { return L <= 64 ? 4 * kRows : kRows; }
 
-int dwt_cols_smem_bytes(int L) { return L * kP * (int)sizeof(float); }
+int dwt_cols_smem_bytes(int L) { return L * (dwt_cols_tile_rows(L) + 1) * (int)sizeof(float); }
 
-void launch_dwt_cols(const PassDesc *p, const int *tp, int n, int tiles, int smem, int inType,
-                     int outType, bool inverse, bool vecLoad, cudaStream_t s) {
+void launch_dwt_cols(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
+                     int inType, int outType, bool inverse, bool vecLoad, cudaStream_t s) {
   if (!inverse) {
     switch (inType) {
       case WL_U8:
-        if (vecLoad) launch_t<uint8_t, float, false, true>(p, tp, n, tiles, smem, s);
-        else launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, s);
+        if (vecLoad) launch_t<uint8_t, float, false, true>(p, tp, n, tiles, smem, rows, s);
+        else launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, rows, s);
         break;
       case WL_U16:
-        if (vecLoad) launch_t<uint16_t, float, false, true>(p, tp, n, tiles, smem, s);
-        else launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, s);
+        if (vecLoad) launch_t<uint16_t, float, false, true>(p, tp, n, tiles, smem, rows, s);
+        else launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, rows, s);
         break;
-      case WL_I32: launch_t<int32_t, float, false>(p, tp, n, tiles, smem, s); break;
-      default: launch_t<float, float, false>(p, tp, n, tiles, smem, s); break;
+      case WL_I32: launch_t<int32_t, float, false>(p, tp, n, tiles, smem, rows, s); break;
+      default: launch_t<float, float, false>(p, tp, n, tiles, smem, rows, s); break;
     }
   } else {
     switch (outType) {
-      case WL_U8: launch_t<float, uint8_t, true>(p, tp, n, tiles, smem, s); break;
-      case WL_U16: launch_t<float, uint16_t, true>(p, tp, n, tiles, smem, s); break;
-      case WL_I32: launch_t<float, int32_t, true>(p, tp, n, tiles, smem, s); break;
-      default: launch_t<float, float, true>(p, tp, n, tiles, smem, s); break;
+      case WL_U8: launch_t<float, uint8_t, true>(p, tp, n, tiles, smem, rows, s); break;
+      case WL_U16: launch_t<float, uint16_t, true>(p, tp, n, tiles, smem, rows, s); break;
+      case WL_I32: launch_t<float, int32_t, true>(p, tp, n, tiles, smem, rows, s); break;
+      default: launch_t<float, float, true>(p, tp, n, tiles, smem, rows, s); break;
     }
   }
 }

@@ -268,7 +268,6 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
   float *o = coef + pl.coefOff;
   float *o2 = coef2 + pl.coefOff;
-  const int T = dwt_cols_tile_rows();
   PassDesc d;
   memset(&d, 0, sizeof d);
   d.cropL = d.cropB = d.cropA = big;
@@ -282,7 +281,7 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   d.out = o2;
   d.outSA = Zp; d.outSB = 1; d.outSC = Zp * Yp;
   d.steps = pl.sx;
-  d.T = T; d.tiles = (d.rows + T - 1) / T;
+  d.T = dwt_cols_tile_rows(d.L); d.tiles = (d.rows + d.T - 1) / d.T;
   xs[group_key(true, pl.dtype, d.L, hostIn && dtype_size(pl.dtype) < 4)].push_back(d);
   // y pass: rows (a = x, b = z) of z-y-x -> z-x-y
   PassDesc e = d;
@@ -294,7 +293,7 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   e.out = o;
   e.outSA = Zp; e.outSB = 1; e.outSC = Zp * Xp;
   e.steps = pl.sy;
-  e.tiles = (e.rows + T - 1) / T;
+  e.T = dwt_cols_tile_rows(e.L); e.tiles = (e.rows + e.T - 1) / e.T;
   ys[group_key(true, WL_F32, e.L)].push_back(e);
   if (pl.sz == 0) return;
   // z pass: rows (a = y, b = x) of z-x-y, in place
@@ -305,7 +304,7 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   f.out = o;
   f.outSA = Zp * Xp; f.outSB = Zp; f.outSC = 1;
   f.steps = pl.sz;
-  f.tiles = (f.rows + T - 1) / T;
+  f.T = dwt_cols_tile_rows(f.L); f.tiles = (f.rows + f.T - 1) / f.T;
   zs[group_key(true, WL_F32, f.L)].push_back(f);
 }
 
@@ -398,7 +397,8 @@ wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
   const PassDesc *dp = reinterpret_cast<const PassDesc *>(d);
   const int *dtp = reinterpret_cast<const int *>(d + n * sizeof(PassDesc));
   if (cols)
-    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, vecLoad, ctx->stream);
+    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, g[0].T, inType, outType, inverse, vecLoad,
+                    ctx->stream);
   else
     launch_dwt_pass(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
   CU(cudaGetLastError());
@@ -812,13 +812,12 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
   wp.wavelet = wavelet;
   if (use_cols(Xp, Yp, Zp, identity, wp)) {
     // column-tile layouts, the forward passes in reverse
-    const int T = dwt_cols_tile_rows();
     if (steps[2] > 0) {  // z pass in place on z-x-y, rows (a = y, b = x)
       PassDesc a = mk();
       a.in = c1; a.inSA = (long long)Zp * Xp; a.inSB = Zp; a.inSC = 1;
       a.out = c1; a.outSA = (long long)Zp * Xp; a.outSB = Zp; a.outSC = 1;
       a.L = Zp; a.B = Xp; a.rows = Xp * Yp; a.steps = steps[2];
-      a.T = T; a.tiles = (a.rows + T - 1) / T;
+      a.T = dwt_cols_tile_rows(a.L); a.tiles = (a.rows + a.T - 1) / a.T;
       TRY(run_group(ctx, {a}, hoff, WL_F32, WL_F32, true, true));
     }
     // y pass z-x-y -> z-y-x, rows (a = x, b = z)
@@ -826,7 +825,7 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
     e.in = c1; e.inSA = Zp; e.inSB = 1; e.inSC = (long long)Zp * Xp;
     e.out = c2; e.outSA = (long long)Zp * Yp; e.outSB = 1; e.outSC = Zp;
     e.L = Yp; e.B = Zp; e.rows = Zp * Xp; e.steps = steps[1];
-    e.T = T; e.tiles = (e.rows + T - 1) / T;
+    e.T = dwt_cols_tile_rows(e.L); e.tiles = (e.rows + e.T - 1) / e.T;
     TRY(run_group(ctx, {e}, hoff, WL_F32, WL_F32, true, true));
     // x pass z-y-x -> x-y-z + crop + dtype, rows (a = y, b = z)
     PassDesc x = mk();
@@ -834,7 +833,7 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
     x.out = dst; x.outSA = X; x.outSB = (long long)X * Y; x.outSC = 1;
     x.cropL = X; x.cropA = Y; x.cropB = Z;
     x.L = Xp; x.B = Zp; x.rows = Yp * Zp; x.steps = steps[0];
-    x.T = T; x.tiles = (x.rows + T - 1) / T;
+    x.T = dwt_cols_tile_rows(x.L); x.tiles = (x.rows + x.T - 1) / x.T;
     TRY(run_group(ctx, {x}, hoff, WL_F32, outType, true, true));
     if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));

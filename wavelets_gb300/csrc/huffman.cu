@@ -368,15 +368,42 @@ __global__ void __launch_bounds__(1024) encode_scan_kernel(DevBatch b) {
   }
 }
 
-// packed word and metadata offsets of every cubelet (one thread; n is small)
-__global__ void cubelet_offsets_kernel(DevBatch b) {
-  long long off = 0, moff = 0;
-  for (int i = 0; i < b.n; i++) {
-    CubeletState *st = b.state + i;
-    st->wordsBase = off;
-    off += st->error ? 0 : st->nWords;
-    st->metaBase = moff;
-    moff += st->nDecode + (b.cub[i].quantAlg == WL_LLOYD ? st->nBounds + st->nValues : 0);
+// packed word and metadata offsets of every cubelet: exclusive scans over
+// the cubelets, 1024 at a time
+__global__ void __launch_bounds__(1024) cubelet_offsets_kernel(DevBatch b) {
+  __shared__ long long sw[32], sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long carryW = 0, carryM = 0;
+  for (int base = 0; base < b.n; base += 1024) {
+    const int i = base + threadIdx.x;
+    long long vw = 0, vm = 0;
+    if (i < b.n) {
+      const CubeletState *st = b.state + i;
+      vw = st->error ? 0 : st->nWords;
+      vm = st->nDecode + (b.cub[i].quantAlg == WL_LLOYD ? st->nBounds + st->nValues : 0);
+    }
+    long long iw = vw, im = vm;
+    for (int off = 1; off < 32; off <<= 1) {
+      const long long tw = __shfl_up_sync(0xffffffffu, iw, off);
+      const long long tm = __shfl_up_sync(0xffffffffu, im, off);
+      if (lane >= off) { iw += tw; im += tm; }
+    }
+    if (lane == 31) { sw[w] = iw; sm[w] = im; }
+    __syncthreads();
+    long long bw = 0, bm = 0, tw = 0, tm = 0;
+    for (int v = 0; v < 32; v++) {
+      if (v < w) { bw += sw[v]; bm += sm[v]; }
+      tw += sw[v];
+      tm += sm[v];
+    }
+    if (i < b.n) {
+      CubeletState *st = b.state + i;
+      st->wordsBase = carryW + bw + iw - vw;
+      st->metaBase = carryM + bm + im - vm;
+    }
+    carryW += tw;
+    carryM += tm;
+    __syncthreads();
   }
 }
 
@@ -512,7 +539,7 @@ void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const unsigned chunks = (unsigned)b.totalChunks;
   encode_count_kernel<<<chunks, kThreads, 0, s>>>(b);
   encode_scan_kernel<<<b.n, 1024, 0, s>>>(b);
-  cubelet_offsets_kernel<<<1, 1, 0, s>>>(b);
+  cubelet_offsets_kernel<<<1, 1024, 0, s>>>(b);
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);
   const int smem = (int)write_smem_bytes(maxSymbols);
   // static + dynamic above 48 KB needs the opt-in

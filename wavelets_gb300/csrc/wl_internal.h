@@ -200,9 +200,9 @@ int dwt_smem_bytes(int L, int T, bool exact);
 // column-tile passes (dwt_cols.cu): lifting / Haar, rows up to kColsMaxL
 constexpr int kColsMaxL = 512;
 void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int tiles,
-                     int smem, int inType, int outType, bool inverse, bool vecLoad,
+                     int smem, int rows, int inType, int outType, bool inverse, bool vecLoad,
                      cudaStream_t s);
-int dwt_cols_tile_rows();
+int dwt_cols_tile_rows(int L);
 int dwt_cols_smem_bytes(int L);
 
 // launchers (select.cu)
