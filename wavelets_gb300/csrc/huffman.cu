@@ -226,15 +226,20 @@ constexpr int kMaxChunkTokens = kChunk + 2 * kMaxEdgeTokens;
 
 // Build the ordered token list of a chunk in shared memory: the tokens of
 // the run entering the chunk, the chunk's stored tokens, the tokens of the
-// run leaving it.  Returns the count.  Collective (two barriers).
+// run leaving it.  The stored tokens go to list[kMaxEdgeTokens...] while
+// thread 0 works out the edge runs, whose entering tokens end right before
+// them.  Returns the count; *first = index of the first token.  Collective
+// (one barrier).
 __device__ int chunk_tokens(const DevBatch &b, long long chunk, const CubeletDev &cd,
-                            int dupV, uint16_t *list, int *sCount) {
+                            int dupV, uint16_t *list, int *sCount, int *first) {
   const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
   const int nInt = b.chunkTok[chunk];
   const uint16_t *src = b.tok + cd.coefOff + cstart;
+  for (int i = threadIdx.x; i < nInt; i += kThreads) list[kMaxEdgeTokens + i] = src[i];
   if (threadIdx.x == 0) {
     int nPre = 0, nPost = 0;
-    uint16_t pre[kMaxEdgeTokens], post[kMaxEdgeTokens];
+    uint16_t pre[kMaxEdgeTokens];
+    uint16_t *post = list + kMaxEdgeTokens + nInt;
     if (dupV >= 0) {
       const int4 cr = b.chunkRun[chunk];  // lead, trail, allZero, len
       const long long runIn = b.chunkRunCtx[2 * chunk], runOut = b.chunkRunCtx[2 * chunk + 1];
@@ -250,15 +255,12 @@ __device__ int chunk_tokens(const DevBatch &b, long long chunk, const CubeletDev
                    [&](uint16_t t) { if (nPost < kMaxEdgeTokens) post[nPost++] = t; });
       }
     }
-    for (int i = 0; i < nPre; i++) list[i] = pre[i];
-    for (int i = 0; i < nPost; i++) list[nPre + nInt + i] = post[i];
-    sCount[0] = nPre;
+    for (int i = 0; i < nPre; i++) list[kMaxEdgeTokens - nPre + i] = pre[i];
+    sCount[0] = kMaxEdgeTokens - nPre;
     sCount[1] = nPre + nInt + nPost;
   }
   __syncthreads();
-  const int nPre = sCount[0];
-  for (int i = threadIdx.x; i < nInt; i += kThreads) list[nPre + i] = src[i];
-  __syncthreads();
+  *first = sCount[0];
   return sCount[1];
 }
 
@@ -454,11 +456,12 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   __shared__ int sCount[2];
   __shared__ unsigned shs[kThreads / 32];
   extern __shared__ unsigned long long wsm[];
-  const long long chunk = blockIdx.x;
-  const int ci = b.chunkCub[chunk];
+  const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   if (st->error) return;
+  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
+  const int nc = min(kQuantGroup, cd.nChunks - c0);
   const int dupV = st->dupValue, dupKey = cd.binCount;
   const int S = cd.binCount + 1;
   // tables sized for this cubelet's alphabet (the launch sizes for the largest)
@@ -469,58 +472,65 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
     sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
     sCode[i] = b.codes[(size_t)ci * kMaxSymbols + i];
   }
-  const unsigned long long chunkOff = b.chunkBits[chunk];
-  const unsigned long long chunkEnd = (chunk + 1 < cd.chunkBase + cd.nChunks)
-                                          ? b.chunkBits[chunk + 1] : st->totalBits;
-  const int shift = (int)(chunkOff & 31);
-  const int nW = (int)((shift + (chunkEnd - chunkOff) + 31) >> 5);
-  uint32_t *gw = b.words + st->wordsBase + (chunkOff >> 5);
-  const bool staged = nW <= kWriteWords;
-  if (staged) {
-    for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
-  } else {
-    // interior words belong to this chunk alone; the edge words were zeroed
-    // by encode_zero_kernel and are shared with the neighbours
-    for (int i = 1 + threadIdx.x; i < nW - 1; i += kThreads) gw[i] = 0;
-  }
-  const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount);  // has barriers
-  uint32_t *dstw = staged ? sw : gw;
-  // each thread takes a contiguous slice of the tokens
-  const int per = (n + kThreads - 1) / kThreads;
-  const int t0 = min(n, (int)threadIdx.x * per), t1 = min(n, t0 + per);
-  unsigned mine = 0;
-  for (int i = t0; i < t1; i++) mine += token_len(list[i], sLen, dupKey);
-  unsigned total;
-  unsigned pos = block_excl_scan(mine, shs, total) + shift;
-  for (int i = t0; i < t1; i++) {
-    const uint16_t t = list[i];
-    const int sym = t & 0x1fff;
-    int l = sLen[sym];
-    unsigned long long v = sCode[sym];
-    if (sym == dupKey) {
-      v |= (unsigned long long)(t >> 13) << l;
-      l += 3;
-    }
-    unsigned p = pos;
-    pos += l;
-    // up to 61 bits starting anywhere in a word: at most 3 words
-    while (l > 0) {
-      const int o = p & 31;
-      const int take = min(l, 32 - o);
-      const unsigned part = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
-      atomicOr(&dstw[p >> 5], part << o);
-      v >>= take;
-      p += take;
-      l -= take;
-    }
-  }
-  if (!staged) return;
-  __syncthreads();
-  for (int i = threadIdx.x; i < nW; i += kThreads) {
-    if (i == 0 || i == nW - 1) {
-      if (sw[i]) atomicOr(&gw[i], sw[i]);
+  for (int k = 0; k < nc; k++) {
+    const long long chunk = cd.chunkBase + c0 + k;
+    const unsigned long long chunkOff = b.chunkBits[chunk];
+    const unsigned long long chunkEnd = (chunk + 1 < cd.chunkBase + cd.nChunks)
+                                            ? b.chunkBits[chunk + 1] : st->totalBits;
+    const int shift = (int)(chunkOff & 31);
+    const int nW = (int)((shift + (chunkEnd - chunkOff) + 31) >> 5);
+    uint32_t *gw = b.words + st->wordsBase + (chunkOff >> 5);
+    const bool staged = nW <= kWriteWords;
+    if (staged) {
+      for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
     } else {
-      gw[i] = sw[i];
+      // interior words belong to this chunk alone; the edge words were zeroed
+      // by encode_zero_kernel and are shared with the neighbours
+      for (int i = 1 + threadIdx.x; i < nW - 1; i += kThreads) gw[i] = 0;
+    }
+    int first;
+    const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount, &first);  // has a barrier
+    const uint16_t *tl = list + first;
+    uint32_t *dstw = staged ? sw : gw;
+    // each thread takes a contiguous slice of the tokens
+    const int per = (n + kThreads - 1) / kThreads;
+    const int t0 = min(n, (int)threadIdx.x * per), t1 = min(n, t0 + per);
+    unsigned mine = 0;
+    for (int i = t0; i < t1; i++) mine += token_len(tl[i], sLen, dupKey);
+    unsigned total;
+    unsigned pos = block_excl_scan(mine, shs, total) + shift;
+    for (int i = t0; i < t1; i++) {
+      const uint16_t t = tl[i];
+      const int sym = t & 0x1fff;
+      int l = sLen[sym];
+      unsigned long long v = sCode[sym];
+      if (sym == dupKey) {
+        v |= (unsigned long long)(t >> 13) << l;
+        l += 3;
+      }
+      unsigned p = pos;
+      pos += l;
+      // up to 61 bits starting anywhere in a word: at most 3 words
+      while (l > 0) {
+        const int o = p & 31;
+        const int take = min(l, 32 - o);
+        const unsigned part = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
+        atomicOr(&dstw[p >> 5], part << o);
+        v >>= take;
+        p += take;
+        l -= take;
+      }
+    }
+    __syncthreads();
+    if (staged) {
+      for (int i = threadIdx.x; i < nW; i += kThreads) {
+        if (i == 0 || i == nW - 1) {
+          if (sw[i]) atomicOr(&gw[i], sw[i]);
+        } else {
+          gw[i] = sw[i];
+        }
+      }
+      __syncthreads();  // sw and the token list are reused by the next chunk
     }
   }
 }
@@ -544,7 +554,7 @@ void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const int smem = (int)write_smem_bytes(maxSymbols);
   // static + dynamic above 48 KB needs the opt-in
   cudaFuncSetAttribute(encode_write_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  encode_write_kernel<<<chunks, kThreads, smem, s>>>(b);
+  encode_write_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b);
 }
 
 }  // namespace wl

@@ -70,33 +70,43 @@ __device__ __forceinline__ void load_chunk(const float *src, int len, float (&v)
 }
 
 // First digit (bits 31..20 of |c|) plus min, max and the two largest |c|.
-// Each thread loads its four float4 of the chunk before using any of them.
+// A CTA takes kQuantGroup consecutive chunks of one cubelet (one histogram
+// flush per group) and loads the next chunk while it counts the current one.
 __global__ void __launch_bounds__(kThreads)
 select_pass0(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kSelectBins];
   __shared__ unsigned sMin[kThreads / 32], sMax[kThreads / 32], sA1[kThreads / 32], sA2[kThreads / 32];
-  const long long chunk = blockIdx.x;
-  const int ci = b.chunkCub[chunk];
+  const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
-  const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int len = (int)min((long long)kChunk, cd.n - start);
-  const float *src = coef + cd.coefOff + start;
+  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
+  const int nc = min(kQuantGroup, cd.nChunks - c0);
   CubeletState *st = b.state + ci;
+  auto chunk_len = [&](int k) {
+    return (int)min((long long)kChunk, cd.n - (long long)(c0 + k) * kChunk);
+  };
+  auto chunk_src = [&](int k) { return coef + cd.coefOff + (long long)(c0 + k) * kChunk; };
 
   for (int i = threadIdx.x; i < kSelectBins; i += kThreads) hist[i] = 0;
   float v[kPerThread];
-  load_chunk(src, len, v);
+  load_chunk(chunk_src(0), chunk_len(0), v);
   __syncthreads();
 
   unsigned mn = 0xffffffffu, mx = 0u, a1 = 0u, a2 = 0u;
+  for (int k = 0; k < nc; k++) {
+    const int len = chunk_len(k);
+    float vn[kPerThread];
+    if (k + 1 < nc) load_chunk(chunk_src(k + 1), chunk_len(k + 1), vn);
 #pragma unroll
-  for (int k = 0; k < kPerThread; k++) {
-    if (chunk_index(k) >= len) continue;
-    const unsigned a = __float_as_uint(v[k]) & 0x7fffffffu;
-    atomicAdd(&hist[a >> 20], 1u);
-    mn = min(mn, ord_enc(v[k]));
-    mx = max(mx, ord_enc(v[k]));
-    top2_merge(a1, a2, a, 0u);
+    for (int j = 0; j < kPerThread; j++) {
+      if (chunk_index(j) >= len) continue;
+      const unsigned a = __float_as_uint(v[j]) & 0x7fffffffu;
+      atomicAdd(&hist[a >> 20], 1u);
+      mn = min(mn, ord_enc(v[j]));
+      mx = max(mx, ord_enc(v[j]));
+      top2_merge(a1, a2, a, 0u);
+    }
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++) v[j] = vn[j];
   }
   for (int off = 16; off > 0; off >>= 1) {
     mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
@@ -137,60 +147,68 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
 // Second full pass: compact the coefficients of the threshold bucket
 // (|c| >> 20 == prefix) into the cubelet's candidate region, and add every
 // |c| above the bucket to the Lloyd histogram (those are above the threshold
-// whatever its low 20 bits turn out to be).
+// whatever its low 20 bits turn out to be).  Chunk groups as in pass 0.
 __global__ void __launch_bounds__(kThreads)
 select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict__ cand) {
   __shared__ unsigned lh[kLloydBins];
   __shared__ unsigned wCnt[kThreads / 32];
   __shared__ unsigned sBase;
-  const long long chunk = blockIdx.x;
-  const int ci = b.chunkCub[chunk];
+  const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
-  const long long start = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int len = (int)min((long long)kChunk, cd.n - start);
-  const float *src = coef + cd.coefOff + start;
+  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
+  const int nc = min(kQuantGroup, cd.nChunks - c0);
   CubeletState *st = b.state + ci;
   const unsigned prefix = st->prefix;
   const bool lloyd = cd.quantAlg == WL_LLOYD && !st->lloydDeferred;
   const unsigned lbase = st->lloydBase, lhi = st->lloydHiBits;
   const int lshift = st->lloydShift;
+  auto chunk_len = [&](int k) {
+    return (int)min((long long)kChunk, cd.n - (long long)(c0 + k) * kChunk);
+  };
+  auto chunk_src = [&](int k) { return coef + cd.coefOff + (long long)(c0 + k) * kChunk; };
   if (lloyd)
     for (int i = threadIdx.x; i < kLloydBins; i += kThreads) lh[i] = 0;
   float v[kPerThread];
-  load_chunk(src, len, v);
+  load_chunk(chunk_src(0), chunk_len(0), v);
   __syncthreads();
 
-  unsigned m = 0;  // candidates among this thread's values
-#pragma unroll
-  for (int k = 0; k < kPerThread; k++) {
-    const unsigned a = __float_as_uint(v[k]) & 0x7fffffffu;
-    const bool in = chunk_index(k) < len;
-    if (in && (a >> 20) == prefix) m |= 1u << k;
-    if (lloyd && in && (a >> 20) > prefix && a <= lhi) atomicAdd(&lh[(a - lbase) >> lshift], 1u);
-  }
-  // block-wide exclusive count of candidates, one reservation per block
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const unsigned cnt = __popc(m);
-  unsigned inc = cnt;
-  for (int off = 1; off < 32; off <<= 1) {
-    const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
-    if (lane >= off) inc += t;
-  }
-  if (lane == 31) wCnt[w] = inc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned tot = 0;
-    for (int i = 0; i < kThreads / 32; i++) tot += wCnt[i];
-    sBase = tot ? atomicAdd(&st->candCount, tot) : 0u;
-  }
-  __syncthreads();
-  unsigned o = sBase + inc - cnt;
-  for (int i = 0; i < w; i++) o += wCnt[i];
   unsigned *dst = cand + cd.coefOff;
-  while (m) {
-    const int k = __ffs(m) - 1;
-    m &= m - 1;
-    dst[o++] = __float_as_uint(v[k]) & 0x7fffffffu;
+  for (int k = 0; k < nc; k++) {
+    const int len = chunk_len(k);
+    float vn[kPerThread];
+    if (k + 1 < nc) load_chunk(chunk_src(k + 1), chunk_len(k + 1), vn);
+    unsigned m = 0;  // candidates among this thread's values
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++) {
+      const unsigned a = __float_as_uint(v[j]) & 0x7fffffffu;
+      const bool in = chunk_index(j) < len;
+      if (in && (a >> 20) == prefix) m |= 1u << j;
+      if (lloyd && in && (a >> 20) > prefix && a <= lhi) atomicAdd(&lh[(a - lbase) >> lshift], 1u);
+    }
+    // block-wide exclusive count of candidates, one reservation per chunk
+    const unsigned cnt = __popc(m);
+    unsigned inc = cnt;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += t;
+    }
+    if (lane == 31) wCnt[w] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned tot = 0;
+      for (int i = 0; i < kThreads / 32; i++) tot += wCnt[i];
+      sBase = tot ? atomicAdd(&st->candCount, tot) : 0u;
+    }
+    __syncthreads();
+    unsigned o = sBase + inc - cnt;
+    for (int i = 0; i < w; i++) o += wCnt[i];
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++)
+      if ((m >> j) & 1u) dst[o++] = __float_as_uint(v[j]) & 0x7fffffffu;
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++) v[j] = vn[j];
+    __syncthreads();  // wCnt and sBase are reused by the next chunk
   }
   if (lloyd) {
     unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
@@ -357,9 +375,10 @@ void launch_select(DevBatch &b, const float *coef, cudaStream_t s) {
   select_init<<<(b.n + 127) / 128, 128, 0, s>>>(b);
   const unsigned chunks = (unsigned)b.totalChunks;
   unsigned *cand = reinterpret_cast<unsigned *>(b.coef2);
-  select_pass0<<<chunks, kThreads, 0, s>>>(b, coef);
+  const unsigned groups = (unsigned)b.totalGroups;
+  select_pass0<<<groups, kThreads, 0, s>>>(b, coef);
   select_resolve<0><<<b.n, 1024, 0, s>>>(b);
-  select_compact<<<chunks, kThreads, 0, s>>>(b, coef, cand);
+  select_compact<<<groups, kThreads, 0, s>>>(b, coef, cand);
   cand_hist<1><<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, cand);
   select_resolve<1><<<b.n, 1024, 0, s>>>(b);
   cand_hist<2><<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, cand);
