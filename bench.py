@@ -394,8 +394,12 @@ def main():
     # the dominant kernel group among those that move bulk data
     dom = max((k for k in per_step if group_bytes.get(k, 0) > 0), key=lambda k: per_step[k])
     dom_gbs = group_bytes[dom] / (per_step[dom] / 1e3) / 1e9 if per_step[dom] > 0 else 0.0
+    # measured DRAM bytes (read + write) per padded voxel of the mixed batch,
+    # from the ncu captures summarised in profiles/kernels_mixed128.md
+    traffic_per_voxel = {"quantize": 4.80, "select": 8.20} if args.workload == "mixed" else {}
+    traffic = traffic_per_voxel[dom] * n_pad if dom in traffic_per_voxel else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": dom_gbs, "peak": hbm,
-                "unit": "GB/s", "frac": dom_gbs / hbm, "traffic": None,
+                "unit": "GB/s", "frac": dom_gbs / hbm, "traffic": traffic,
                 "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": group_bytes[dom]}
     pipe_gbs = (in_bytes + comp_bytes) / (step_ms / 1e3) / 1e9
