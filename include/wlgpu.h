@@ -168,6 +168,58 @@ wl_status wl_last_timings(const wl_ctx *ctx, float out[6]);
 /* Synchronize the context's stream. */
 wl_status wl_sync(wl_ctx *ctx);
 
+/* ---- Serving -------------------------------------------------------------
+ * No reference counterpart (the reference compresses one file per process).
+ * A server runs a request loop over several lanes, each a context (stream and
+ * buffers) driven by its own host thread: compress and decompress requests of
+ * any size are admitted as they arrive, compress requests waiting together
+ * are batched onto the next free lane (continuous batching), admission is
+ * gated by a device working-memory budget, and batches on different lanes
+ * overlap on the GPU.  Compress inputs may be device, page-locked or pageable
+ * host pointers; they, and a decompress request's input and output, must stay
+ * valid until the request is waited for. */
+enum { WL_REQ_COMPRESS = 1, WL_REQ_DECOMPRESS = 2 };
+
+typedef struct {
+  int lanes;                /* concurrent batches on the device (default 2) */
+  size_t memory_budget;     /* device working bytes admitted at once (default 16 GiB) */
+  int max_batch;            /* requests per batch (default 1024) */
+} wl_serve_config;
+
+typedef struct {
+  int kind;                 /* WL_REQ_COMPRESS or WL_REQ_DECOMPRESS */
+  wl_cubelet cubelet;       /* compress: the input */
+  const wl_result *compressed; /* decompress: the input */
+  int out_dtype;            /* decompress: output element type */
+  void *out;                /* decompress: original_size elements of out_dtype */
+  int out_on_device;
+} wl_request;
+
+typedef struct {
+  int status;               /* wl_status of the request */
+  double queue_ms;          /* submit -> its batch started */
+  double service_ms;        /* batch start -> done */
+  double total_ms;          /* submit -> done */
+  int batch_size;           /* requests in the batch that served it */
+  int lane;
+} wl_request_info;
+
+typedef struct wl_server wl_server;
+
+void wl_serve_config_default(wl_serve_config *cfg);
+wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out);
+/* Queue a request; *ticket identifies it for wl_serve_wait. */
+wl_status wl_serve_submit(wl_server *srv, const wl_request *req, unsigned long long *ticket);
+/* Wait up to timeout_ms (0 polls, negative waits without limit).  Returns
+ * WL_ETIMEOUT while the request is pending; otherwise the request's own
+ * status, fills *info (may be NULL) and, for compress, *out (owns its arrays;
+ * release with wl_result_free), and retires the ticket. */
+wl_status wl_serve_wait(wl_server *srv, unsigned long long ticket, int timeout_ms,
+                        wl_result *out, wl_request_info *info);
+const char *wl_serve_last_error(const wl_server *srv);
+/* Finishes the running batches; requests still queued fail with WL_EINVAL. */
+void wl_serve_destroy(wl_server *srv);
+
 /* Device memory helpers for callers that keep inputs resident on the GPU. */
 void *wl_device_alloc(size_t bytes);
 void wl_device_free(void *p);

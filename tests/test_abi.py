@@ -69,3 +69,23 @@ def test_init_without_gpu_fails_cleanly(lib):
     h = ctypes.c_void_p()
     lib.wl_init.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
     assert lib.wl_init(0, ctypes.byref(h)) != 0
+
+
+def test_serve_create_without_gpu_fails_cleanly(lib):
+    """No GPU: the server reports an error instead of starting lanes."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("GPU present")
+    except ImportError:
+        pass
+    from wavelets_gb300 import lib as L
+    cfg = L.WlServeConfig()
+    lib.wl_serve_config_default.argtypes = [ctypes.POINTER(L.WlServeConfig)]
+    lib.wl_serve_config_default(ctypes.byref(cfg))
+    assert cfg.lanes == 2 and cfg.memory_budget == 16 << 30 and cfg.max_batch == 1024
+    h = ctypes.c_void_p()
+    lib.wl_serve_create.argtypes = [ctypes.c_int, ctypes.POINTER(L.WlServeConfig),
+                                    ctypes.POINTER(ctypes.c_void_p)]
+    assert lib.wl_serve_create(0, ctypes.byref(cfg), ctypes.byref(h)) != 0
+    assert not h.value

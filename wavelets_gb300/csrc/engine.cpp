@@ -519,14 +519,17 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     for (int i = 0; i < n; i++) dIn[i] = plans[i].data;
   } else {
     // Page-locked host inputs are read in place by the first transform pass
-    // (the GPU reaches pinned memory directly); pageable ones are copied.
+    // (the GPU reaches pinned memory directly); pageable ones are copied;
+    // device (or managed) pointers are used as they are.
     bool staged = false;
     for (int i = 0; i < n; i++) {
       cudaPointerAttributes attr;
-      if (cudaPointerGetAttributes(&attr, plans[i].data) == cudaSuccess &&
-          attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+      const bool known = cudaPointerGetAttributes(&attr, plans[i].data) == cudaSuccess;
+      if (known && attr.type == cudaMemoryTypeHost && attr.devicePointer) {
         dIn[i] = attr.devicePointer;
         hostIn[i] = 1;
+      } else if (known && (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)) {
+        dIn[i] = plans[i].data;
       } else {
         cudaGetLastError();
         dIn[i] = nullptr;

@@ -1,0 +1,329 @@
+// Serving: a request loop over several lanes.
+//
+// Each lane is an ordinary context (its own stream and grow-only buffers)
+// driven by its own host thread, so a batch on one lane overlaps on the GPU
+// with batches and decompressions on the others.  Requests wait in one FIFO
+// queue.  A free lane takes either the decompress request at the head of the
+// queue, or every compress request at the head that fits (continuous
+// batching: whatever arrived while the lanes were busy forms the next batch).
+// Admission is gated by an estimate of each request's device working memory
+// against the configured budget; a request larger than the whole budget runs
+// alone once nothing else is in flight.
+#include <chrono>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "wlgpu.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+int ceil_log2(unsigned x) {  // ceilLog2 (dwt_cpu.cc:75-78)
+  if (x == 0) return 0;
+  int n = 0;
+  unsigned v = x - 1;
+  while (v) { n++; v >>= 1; }
+  return n;
+}
+
+long long padded(int len, int steps) {  // dwt_padded_length (dwt_cpu.cc:212-219)
+  const long long mod = 1ll << steps;
+  return mod * ((len - 1) / mod + 1);
+}
+
+int dtype_bytes(int dt) {
+  switch (dt) {
+    case WL_U8: return 1;
+    case WL_U16: return 2;
+    default: return 4;
+  }
+}
+
+// Device working bytes of one request: two float coefficient buffers, the
+// token slots and per-chunk records, staging of the input or output, plus a
+// fixed allowance for tables.
+double estimate(const wl_request &r) {
+  if (r.kind == WL_REQ_COMPRESS) {
+    const wl_cubelet &c = r.cubelet;
+    long long n = 1;
+    for (int a = 0; a < 3; a++) {
+      const int m = ceil_log2((unsigned)c.size[a]);
+      const int s = (c.params.steps[a] < 0 || c.params.steps[a] > m) ? m : c.params.steps[a];
+      n *= padded(c.size[a], s);
+    }
+    const double in = (double)c.size[0] * c.size[1] * c.size[2] * dtype_bytes(c.dtype);
+    return 12.0 * n + in + (1 << 20);
+  }
+  const wl_result *x = r.compressed;
+  const double n = (double)x->size[0] * x->size[1] * x->size[2];
+  const double out = (double)x->original_size[0] * x->original_size[1] * x->original_size[2] *
+                     dtype_bytes(r.out_dtype);
+  return 12.0 * n + 4.0 * x->n_words + out + (1 << 20);
+}
+
+struct Job {
+  unsigned long long id = 0;
+  wl_request req;
+  double est = 0;
+  Clock::time_point submitted, started, finished;
+  bool done = false;
+  wl_status st = WL_OK;
+  wl_result res;
+  int batchSize = 0, lane = -1;
+};
+
+}  // namespace
+
+struct wl_server {
+  int device = 0;
+  wl_serve_config cfg;
+  std::mutex mu;
+  std::condition_variable cvWork, cvDone;
+  std::deque<Job *> pending;
+  std::unordered_map<unsigned long long, Job *> jobs;
+  double inflight = 0;
+  bool stop = false;
+  unsigned long long nextId = 1;
+  std::vector<wl_ctx *> ctxs;
+  std::vector<std::thread> workers;
+  std::string err;
+};
+
+namespace {
+
+wl_status serve_fail(wl_server *s, wl_status st, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (s) {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->err = buf;
+  }
+  return st;
+}
+
+// Can the request at the head of the queue start now?
+bool head_fits(const wl_server *s) {
+  if (s->pending.empty()) return false;
+  const Job *j = s->pending.front();
+  return s->inflight == 0 || s->inflight + j->est <= (double)s->cfg.memory_budget;
+}
+
+void worker(wl_server *s, int lane) {
+  wl_ctx *ctx = s->ctxs[lane];
+  std::vector<Job *> batch;
+  std::vector<wl_cubelet> items;
+  std::vector<wl_result> outs;
+  for (;;) {
+    batch.clear();
+    double est = 0;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cvWork.wait(lk, [&] { return s->stop || head_fits(s); });
+      if (s->stop && s->pending.empty()) return;
+      if (!head_fits(s)) continue;
+      const double budget = (double)s->cfg.memory_budget;
+      if (s->pending.front()->req.kind == WL_REQ_DECOMPRESS) {
+        batch.push_back(s->pending.front());
+        s->pending.pop_front();
+        est = batch[0]->est;
+      } else {
+        while (!s->pending.empty() && (int)batch.size() < s->cfg.max_batch) {
+          Job *j = s->pending.front();
+          if (j->req.kind != WL_REQ_COMPRESS) break;
+          if (!batch.empty() && s->inflight + est + j->est > budget) break;
+          if (batch.empty() && s->inflight > 0 && s->inflight + j->est > budget) break;
+          batch.push_back(j);
+          est += j->est;
+          s->pending.pop_front();
+        }
+      }
+      s->inflight += est;
+      const Clock::time_point now = Clock::now();
+      for (Job *j : batch) {
+        j->started = now;
+        j->batchSize = (int)batch.size();
+        j->lane = lane;
+      }
+      // more work may fit beside this batch
+      if (head_fits(s)) s->cvWork.notify_one();
+    }
+
+    if (batch[0]->req.kind == WL_REQ_DECOMPRESS) {
+      Job *j = batch[0];
+      j->st = wl_decompress_cubelet(ctx, j->req.compressed, j->req.out_dtype, j->req.out,
+                                    j->req.out_on_device);
+    } else {
+      const int n = (int)batch.size();
+      items.resize(n);
+      outs.assign(n, wl_result());
+      for (int i = 0; i < n; i++) items[i] = batch[i]->req.cubelet;
+      const wl_status st = wl_compress_batch(ctx, items.data(), n, 0, outs.data());
+      for (int i = 0; i < n; i++) {
+        batch[i]->st = st;
+        if (st == WL_OK) batch[i]->res = outs[i];
+      }
+    }
+
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      const Clock::time_point now = Clock::now();
+      for (Job *j : batch) {
+        j->finished = now;
+        j->done = true;
+        if (j->st != WL_OK) s->err = wl_last_error(ctx);
+      }
+      s->inflight -= est;
+      if (s->inflight < 1.0) s->inflight = 0;
+    }
+    s->cvDone.notify_all();
+    s->cvWork.notify_all();
+  }
+}
+
+double ms(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+void wl_serve_config_default(wl_serve_config *cfg) {
+  if (!cfg) return;
+  cfg->lanes = 2;
+  cfg->memory_budget = (size_t)16 << 30;
+  cfg->max_batch = 1024;
+}
+
+wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out) {
+  if (!out) return WL_EINVAL;
+  *out = nullptr;
+  wl_server *s = new wl_server;
+  s->device = device;
+  wl_serve_config_default(&s->cfg);
+  if (cfg) s->cfg = *cfg;
+  if (s->cfg.lanes < 1) s->cfg.lanes = 1;
+  if (s->cfg.max_batch < 1) s->cfg.max_batch = 1;
+  for (int i = 0; i < s->cfg.lanes; i++) {
+    wl_ctx *c = nullptr;
+    const wl_status st = wl_init(device, &c);
+    if (st != WL_OK) {
+      for (wl_ctx *x : s->ctxs) wl_destroy(x);
+      delete s;
+      return st;
+    }
+    s->ctxs.push_back(c);
+  }
+  for (int i = 0; i < s->cfg.lanes; i++) s->workers.emplace_back(worker, s, i);
+  *out = s;
+  return WL_OK;
+}
+
+wl_status wl_serve_submit(wl_server *s, const wl_request *req, unsigned long long *ticket) {
+  if (!s || !req || !ticket) return WL_EINVAL;
+  if (req->kind == WL_REQ_COMPRESS) {
+    if (!req->cubelet.data) return serve_fail(s, WL_EINVAL, "compress request without data");
+    for (int a = 0; a < 3; a++)
+      if (req->cubelet.size[a] < 1) return serve_fail(s, WL_EINVAL, "empty cubelet size");
+  } else if (req->kind == WL_REQ_DECOMPRESS) {
+    if (!req->compressed || !req->out)
+      return serve_fail(s, WL_EINVAL, "decompress request without input or output");
+  } else {
+    return serve_fail(s, WL_EINVAL, "unknown request kind %d", req->kind);
+  }
+  Job *j = new Job;
+  j->req = *req;
+  memset(&j->res, 0, sizeof j->res);
+  j->est = estimate(*req);
+  j->submitted = Clock::now();
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->stop) {
+      delete j;
+      return WL_EINVAL;
+    }
+    j->id = s->nextId++;
+    s->jobs[j->id] = j;
+    s->pending.push_back(j);
+    *ticket = j->id;
+  }
+  s->cvWork.notify_one();
+  return WL_OK;
+}
+
+wl_status wl_serve_wait(wl_server *s, unsigned long long ticket, int timeout_ms, wl_result *out,
+                        wl_request_info *info) {
+  if (!s) return WL_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) {
+    s->err = "unknown or already retired ticket";
+    return WL_EINVAL;
+  }
+  Job *j = it->second;
+  if (timeout_ms < 0) {
+    s->cvDone.wait(lk, [&] { return j->done; });
+  } else if (!j->done) {
+    s->cvDone.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return j->done; });
+  }
+  if (!j->done) return WL_ETIMEOUT;
+  s->jobs.erase(it);
+  lk.unlock();
+  if (info) {
+    info->status = j->st;
+    info->queue_ms = ms(j->submitted, j->started);
+    info->service_ms = ms(j->started, j->finished);
+    info->total_ms = ms(j->submitted, j->finished);
+    info->batch_size = j->batchSize;
+    info->lane = j->lane;
+  }
+  const wl_status st = j->st;
+  if (j->req.kind == WL_REQ_COMPRESS) {
+    if (out) *out = j->res;
+    else wl_result_free(&j->res);
+  }
+  delete j;
+  return st;
+}
+
+const char *wl_serve_last_error(const wl_server *s) {
+  return s ? s->err.c_str() : "null server";
+}
+
+void wl_serve_destroy(wl_server *s) {
+  if (!s) return;
+  std::deque<Job *> dropped;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+    dropped.swap(s->pending);
+    for (Job *j : dropped) {
+      j->st = WL_EINVAL;
+      j->done = true;
+    }
+  }
+  s->cvWork.notify_all();
+  s->cvDone.notify_all();
+  for (std::thread &t : s->workers) t.join();
+  for (auto &kv : s->jobs) {
+    if (kv.second->req.kind == WL_REQ_COMPRESS && kv.second->st == WL_OK)
+      wl_result_free(&kv.second->res);
+    delete kv.second;
+  }
+  for (wl_ctx *c : s->ctxs) wl_destroy(c);
+  delete s;
+}
+
+}  // extern "C"

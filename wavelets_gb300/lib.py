@@ -60,6 +60,26 @@ class WlCubelet(ctypes.Structure):
                 ("size", ctypes.c_int * 3), ("params", WlParams)]
 
 
+REQ_COMPRESS, REQ_DECOMPRESS = 1, 2
+
+
+class WlServeConfig(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("memory_budget", ctypes.c_size_t),
+                ("max_batch", ctypes.c_int)]
+
+
+class WlRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("cubelet", WlCubelet),
+                ("compressed", ctypes.POINTER(WlResult)), ("out_dtype", ctypes.c_int),
+                ("out", ctypes.c_void_p), ("out_on_device", ctypes.c_int)]
+
+
+class WlRequestInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("queue_ms", ctypes.c_double),
+                ("service_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("batch_size", ctypes.c_int), ("lane", ctypes.c_int)]
+
+
 EXPORTS = {
     "wl_params_default": (None, [ctypes.POINTER(WlParams)]),
     "wl_result_free": (None, [ctypes.POINTER(WlResult)]),
@@ -102,6 +122,15 @@ EXPORTS = {
                                                    ctypes.c_void_p]),
     "wl_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "wl_host_free": (None, [ctypes.c_void_p]),
+    "wl_serve_config_default": (None, [ctypes.POINTER(WlServeConfig)]),
+    "wl_serve_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(WlServeConfig),
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "wl_serve_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlRequest),
+                                       ctypes.POINTER(ctypes.c_ulonglong)]),
+    "wl_serve_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int,
+                                     ctypes.POINTER(WlResult), ctypes.POINTER(WlRequestInfo)]),
+    "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "wl_serve_destroy": (None, [ctypes.c_void_p]),
 }
 
 _lib = None
@@ -524,5 +553,84 @@ class PinnedBuffer:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """The serving loop of libwlgpu: compress and decompress requests admitted
+    as they arrive, batched continuously onto `lanes` concurrent lanes, gated
+    by a device working-memory budget.  Inputs and outputs are kept alive here
+    until their request has been waited for."""
+
+    def __init__(self, lanes: int = 2, memory_budget: int = 16 << 30, max_batch: int = 1024,
+                 device: int = 0):
+        self.lib = load()
+        cfg = WlServeConfig()
+        self.lib.wl_serve_config_default(ctypes.byref(cfg))
+        cfg.lanes, cfg.memory_budget, cfg.max_batch = lanes, memory_budget, max_batch
+        h = ctypes.c_void_p()
+        st = self.lib.wl_serve_create(device, ctypes.byref(cfg), ctypes.byref(h))
+        if st != WL_OK:
+            raise WlError(st, f"wl_serve_create(device={device}) failed")
+        self.h = h
+        self._keep = {}
+
+    def _submit(self, req, keep):
+        t = ctypes.c_ulonglong()
+        st = self.lib.wl_serve_submit(self.h, ctypes.byref(req), ctypes.byref(t))
+        if st != WL_OK:
+            raise WlError(st, self.lib.wl_serve_last_error(self.h).decode())
+        self._keep[t.value] = (req, keep)
+        return t.value
+
+    def submit_compress(self, arr=None, params=None, ptr=None, dtype=None, size=None) -> int:
+        """Compress a numpy array (host) or a raw (ptr, wl dtype, size) input."""
+        req = WlRequest()
+        req.kind = REQ_COMPRESS
+        keep = None
+        if arr is not None:
+            keep = np.ascontiguousarray(arr)
+            ptr, dtype, size = keep.ctypes.data, NP_TO_WL[keep.dtype], _size_of(keep)
+        req.cubelet.data = ptr
+        req.cubelet.dtype = dtype
+        req.cubelet.size[:] = size
+        req.cubelet.params = make_params(params)
+        return self._submit(req, keep)
+
+    def submit_decompress(self, c: "Compressed", out: np.ndarray) -> int:
+        """Restore `c` into the host array `out` (original size, any dtype)."""
+        req = WlRequest()
+        req.kind = REQ_DECOMPRESS
+        r = c.to_struct()
+        req.compressed = ctypes.pointer(r)
+        req.out_dtype = NP_TO_WL[out.dtype]
+        req.out = out.ctypes.data
+        req.out_on_device = 0
+        return self._submit(req, (c, r, out))
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(Compressed or None, info dict); None while a poll finds it pending."""
+        res = (WlResult * 1)()
+        info = WlRequestInfo()
+        st = self.lib.wl_serve_wait(self.h, ticket, timeout_ms, res, ctypes.byref(info))
+        if st == WL_ETIMEOUT:
+            return None, None
+        req, _ = self._keep.pop(ticket)
+        if st != WL_OK:
+            raise WlError(st, self.lib.wl_serve_last_error(self.h).decode())
+        d = {k: getattr(info, k) for k, _ in WlRequestInfo._fields_}
+        if req.kind == REQ_COMPRESS:
+            return adopt_results(self.lib, res, 1)[0], d
+        return None, d
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wl_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
