@@ -16,6 +16,10 @@ Printed JSON line (rank 0):
               page-locked host memory in place) and the device->host read of
               the compressed streams inside the timed region (wall clock)
   plain_value the same 512 cubelets compressed one cubelet per call
+  serving     a Poisson stream of 2,000 requests/s (80% compress, 20%
+              decompress; axes log-uniform 16..512, CDF 9/7 3,3,3, log 256)
+              through the serving loop for --serve-seconds: p50/p99 latency
+              and served GB/s
   roofline    the dominant kernel group: its compulsory bytes / its time
   pipeline_roofline  (input + compressed bytes) / whole-step device time
   cpu_baseline the oracle (CPU restatement of the reference path) on a
@@ -233,6 +237,99 @@ def run_reference(args, items, desc, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ serving
+def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=2, budget=16 << 30, device=0):
+    """Poisson stream of requests (80% compress, 20% decompress) against the
+    library's serving loop: payloads with axes log-uniform in 16..512 (at most
+    256 MiB each), uint8/uint16/float32 in equal parts, CDF 9/7 with 3 steps
+    per axis, log quantizer with 256 bins.  Compress inputs are read in place
+    from page-locked host memory; decompressed volumes land in page-locked
+    host buffers.  Returns latency percentiles and served GB/s."""
+    import queue
+    from wavelets_gb300 import synth
+    rng = np.random.default_rng(seed)
+    pool = synth.serving_pool(seed, 64)
+    prm = P.Params(steps=(3, 3, 3), wavelet=P.CDF97, quant_alg=P.LOG, bin_count=256)
+    offs, off = [], 0
+    for a in pool:
+        offs.append(off)
+        off += (a.nbytes + 255) // 256 * 256
+    pin = lib.PinnedBuffer(off)
+    host = pin.array(np.uint8, (off,))
+    for a, o in zip(pool, offs):
+        host[o:o + a.nbytes] = a.view(np.uint8).ravel()
+    reqs = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), a.nbytes)
+            for a, o in zip(pool, offs)]
+    # decompress sources: a third of the pool, compressed once up front
+    ctx = lib.Context(device)
+    srcs = [(ctx.compress(a, prm), a) for a in pool[::3]]
+    ctx.close()
+    nslot = 16
+    outs = [[lib.PinnedBuffer(a.nbytes) for _ in range(nslot)] for _, a in srcs]
+    out_views = [[b.array(a.dtype, a.shape) for b in bufs] for bufs, (_, a) in zip(outs, srcs)]
+
+    n = int(rng.poisson(rate * seconds))
+    times = np.sort(rng.uniform(0.0, seconds, n))
+    is_comp = rng.uniform(size=n) < 0.8
+    which = rng.integers(0, 1 << 30, n)
+    srv = lib.Server(lanes=lanes, memory_budget=budget)
+    # warm the lanes' buffers with one request of every payload
+    for ptr, dt, size, _ in reqs:
+        srv.wait(srv.submit_compress(ptr=ptr, dtype=dt, size=size, params=prm))
+    q = queue.Queue()
+    lat = {"compress": [], "decompress": []}
+    done_bytes = [0]
+    t_last = [0.0]
+    errors = []
+
+    def waiter():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            t, kind, nbytes = item
+            try:
+                _, info = srv.wait(t)
+            except Exception as e:  # keep draining; report the failure
+                errors.append(str(e))
+                continue
+            lat[kind].append(info["total_ms"])
+            done_bytes[0] += nbytes
+            t_last[0] = time.perf_counter()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    for k in range(n):
+        dt_wait = t0 + times[k] - time.perf_counter()
+        if dt_wait > 0:
+            time.sleep(dt_wait)
+        if is_comp[k]:
+            ptr, dt, size, nb = reqs[which[k] % len(reqs)]
+            q.put((srv.submit_compress(ptr=ptr, dtype=dt, size=size, params=prm), "compress", nb))
+        else:
+            j = which[k] % len(srcs)
+            c, a = srcs[j]
+            q.put((srv.submit_decompress(c, out_views[j][k % nslot]), "decompress", a.nbytes))
+    q.put(None)
+    th.join()
+    elapsed = max(t_last[0], time.perf_counter()) - t0
+    srv.close()
+    allv = np.array(lat["compress"] + lat["decompress"])
+
+    def pct(v, p_):
+        return float(np.percentile(v, p_)) if len(v) else None
+
+    return {"requests": n, "failed": len(errors), "seconds": seconds, "rate_per_s": rate,
+            "lanes": lanes, "memory_budget_gib": budget / (1 << 30),
+            "value": done_bytes[0] / elapsed / 1e9, "unit": "GB/s",
+            "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+            "compress_p50_ms": pct(lat["compress"], 50), "compress_p99_ms": pct(lat["compress"], 99),
+            "decompress_p50_ms": pct(lat["decompress"], 50),
+            "decompress_p99_ms": pct(lat["decompress"], 99),
+            "mean_request_mb": float(np.mean([r[3] for r in reqs]) / 1e6)}
+
+
 # ------------------------------------------------------------------ GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -244,6 +341,8 @@ def main():
     ap.add_argument("--cubelets", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the serving measurement (0: skip)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -403,6 +502,10 @@ def main():
                 "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": group_bytes[dom]}
     pipe_gbs = (in_bytes + comp_bytes) / (step_ms / 1e3) / 1e9
+    # ---- serving: Poisson request stream, p50/p99 latency ----
+    serving = None
+    if rank == 0 and args.serve_seconds > 0 and args.workload == "mixed":
+        serving = serve_run(lib, args.serve_seconds, device=local)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(items)
@@ -428,6 +531,7 @@ def main():
             "pipeline_roofline": {"achieved": pipe_gbs, "peak": hbm, "unit": "GB/s",
                                   "frac": pipe_gbs / hbm,
                                   "bytes": "input + compressed output per step"},
+            "serving": serving,
             "kernel_ms_per_step": per_step,
             "gpu_launches": launches,
             "clocks": clk.summary(),

@@ -327,8 +327,7 @@ dwt_pass_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
 template <typename InT, typename OutT, bool INV>
 void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, cudaStream_t s) {
   auto k = dwt_pass_kernel<InT, OutT, INV>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (smem > 32 * 1024) raise_smem_limit(k, smem);  // static + dynamic may pass 48 KB
   k<<<tiles, kThreads, smem, s>>>(p, tp, n);
 }
 

@@ -482,8 +482,7 @@ void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, int 
               cudaStream_t s) {
   auto k = rows == kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows>
                          : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (smem > 32 * 1024) raise_smem_limit(k, smem);  // static + dynamic may pass 48 KB
   k<<<tiles, kThreadsC, smem, s>>>(p, tp, n);
 }
 

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <string>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <vector>
 
@@ -161,6 +162,20 @@ int padded_length(int len, int steps) {  // dwt_padded_length (dwt_cpu.cc:212-21
 }
 
 }  // namespace
+
+namespace wl {
+void raise_smem_limit(const void *func, int bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void *, int> *limits = new std::unordered_map<const void *, int>;
+  std::lock_guard<std::mutex> g(mu);
+  int &cur = (*limits)[func];
+  if (bytes <= cur) return;
+  if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+    cur = bytes;
+  else
+    cudaGetLastError();  // the launch reports the error
+}
+}  // namespace wl
 
 struct wl_ctx {
   int device = 0;

@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
 
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const size_t smem = build_smem_bytes(maxSymbols);
-  cudaFuncSetAttribute(huffman_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  raise_smem_limit(huffman_build_kernel, (int)smem);
   huffman_build_kernel<<<b.n, 1024, smem, s>>>(b);
 }
 
@@ -553,7 +553,7 @@ void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);
   const int smem = (int)write_smem_bytes(maxSymbols);
   // static + dynamic above 48 KB needs the opt-in
-  cudaFuncSetAttribute(encode_write_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  raise_smem_limit(encode_write_kernel, smem);
   encode_write_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b);
 }
 

@@ -721,14 +721,13 @@ void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
   lloyd_cand_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(
       b, reinterpret_cast<const unsigned *>(b.coef2));
   lloyd_deferred_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, coef);
-  cudaFuncSetAttribute(lloyd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kLloydSmem);
+  raise_smem_limit(lloyd_solve_kernel, kLloydSmem);
   lloyd_solve_kernel<<<b.n, 1024, kLloydSmem, s>>>(b);
 }
 
 void launch_quantize(DevBatch &b, const float *coef, int maxTable, cudaStream_t s) {
   const int smem = maxTable * (int)sizeof(float);
-  cudaFuncSetAttribute(quantize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       smem > 0 ? smem : 1);
+  raise_smem_limit(quantize_kernel, smem > 0 ? smem : 1);
   quantize_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b, coef);
 }
 

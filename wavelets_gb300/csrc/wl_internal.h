@@ -192,6 +192,14 @@ struct DevBatch {
 };
 
 // launchers (dwt.cu)
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`.  The
+// limit is per kernel and process-wide; it only ever grows here, so a launch
+// on one host thread cannot be undercut by a smaller setting from another.
+void raise_smem_limit(const void *func, int bytes);
+template <class F> inline void raise_smem_limit(F *func, int bytes) {
+  raise_smem_limit(reinterpret_cast<const void *>(func), bytes);
+}
+
 void launch_dwt_pass(const PassDesc *d_passes, const int *d_tilePrefix,
                      int nPasses, int totalTiles, int smemBytes, int inType,
                      int outType, bool inverse, cudaStream_t s);

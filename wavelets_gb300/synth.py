@@ -136,3 +136,36 @@ def small_cases(seed: int = 7):
         a = scaled_blob_cubelet(rng, shape, dt)
         cases.append((f"{dt.__name__}_{'x'.join(map(str, shape))}", a))
     return cases
+
+
+def serving_pool(seed: int = 20261207, count: int = 64, cap_bytes: int = 256 << 20,
+                 base_size: int = 128):
+    """Request payloads for the serving workload: every axis log-uniform in
+    16..512, dtypes uint8 / uint16 / float32 in equal parts, input at most
+    cap_bytes (redrawn otherwise).  Contents are mirrored crops of one blob
+    volume, scaled to the dtype range (cheap to make at any size)."""
+    rng = np.random.default_rng(seed)
+    base = np.zeros((base_size,) * 3, np.float32)
+    add_blobs(base, rng, 40, (2.0, base_size / 2.0), (-1.0, 1.0))
+    base += rng.normal(0.0, 0.01, base.shape).astype(np.float32)
+    lo, hi = float(base.min()), float(base.max())
+    span = hi - lo if hi > lo else 1.0
+    dtypes = (np.uint8, np.uint16, np.float32)
+    out = []
+    for i in range(count):
+        dt = dtypes[i % 3]
+        while True:
+            shape = tuple(int(np.exp(rng.uniform(np.log(16), np.log(512)))) for _ in range(3))
+            if int(np.prod(shape)) * np.dtype(dt).itemsize <= cap_bytes:
+                break
+        idx = []
+        for n in shape:  # mirrored walk through the base volume from a random start
+            k = (rng.integers(0, base_size) + np.arange(n)) % (2 * base_size)
+            idx.append(np.where(k < base_size, k, 2 * base_size - 1 - k))
+        v = base[np.ix_(*idx)]
+        if dt == np.float32:
+            out.append(np.ascontiguousarray(v))
+        else:
+            top = 255.0 if dt == np.uint8 else 65535.0
+            out.append(np.clip(np.rint((v - lo) / span * top), 0, top).astype(dt))
+    return out
