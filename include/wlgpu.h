@@ -116,6 +116,11 @@ typedef struct {
   int dtype;
   int size[3];
   wl_params params;
+  /* Elements between consecutive rows (y) and slices (z) of the source; 0
+   * means dense (X and X*Y).  A sub-volume of a larger array -- a cubelet of
+   * a split volume (cube split, cubelet_convert.cc:424-562) -- is passed in
+   * place this way, without copying it out first. */
+  long long row_pitch, slice_pitch;
 } wl_cubelet;
 
 /* Compress n cubelets of any sizes/dtypes/parameters in one pass of batched

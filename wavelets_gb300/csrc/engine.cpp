@@ -62,6 +62,7 @@ struct Plan {
   int tableOff;
   bool identity;       // all steps zero: no transform, no axis rotation
   bool cols;           // transform runs on the column-tile kernel
+  long long pitchY, pitchZ;  // source elements between rows / slices
 };
 
 // Column-tile kernel for every lifting / Haar cubelet whose padded axes fit
@@ -290,7 +291,7 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   // x pass: rows (a = y, b = z), REPEAT padding by clamping
   d.in = in;
   d.vecLoad = hostIn ? 1 : 0;
-  d.inSA = pl.X; d.inSB = (long long)pl.X * pl.Y; d.inSC = 1;
+  d.inSA = pl.pitchY; d.inSB = pl.pitchZ; d.inSC = 1;
   d.clampL = pl.X; d.clampA = pl.Y; d.clampB = pl.Z;
   d.L = pl.Xp; d.B = pl.Zp; d.rows = (int)(Yp * Zp);
   d.out = o2;
@@ -339,8 +340,8 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
   d.cropL = d.cropB = d.cropA = big;
   // x pass: rows (z, y) of the source, REPEAT padding by clamping
   d.in = in;
-  d.inSA = (long long)pl.X * pl.Y;
-  d.inSB = pl.X;
+  d.inSA = pl.pitchZ;
+  d.inSB = pl.pitchY;
   d.inSC = 1;
   d.clampL = pl.X; d.clampB = pl.Y; d.clampA = pl.Z;
   d.L = pl.Xp; d.B = pl.Yp; d.rows = (int)(Yp * Zp);
@@ -457,6 +458,11 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     pl.X = it.size[0]; pl.Y = it.size[1]; pl.Z = it.size[2];
     if (pl.X < 1 || pl.Y < 1 || pl.Z < 1)
       return fail(ctx, WL_EINVAL, "cubelet %d: empty size %dx%dx%d", i, pl.X, pl.Y, pl.Z);
+    pl.pitchY = it.row_pitch ? it.row_pitch : pl.X;
+    pl.pitchZ = it.slice_pitch ? it.slice_pitch : pl.pitchY * pl.Y;
+    if (pl.pitchY < pl.X || pl.pitchZ < pl.pitchY * pl.Y)
+      return fail(ctx, WL_EINVAL, "cubelet %d: pitches %lld, %lld smaller than its rows/slices",
+                  i, pl.pitchY, pl.pitchZ);
     pl.p = it.params;
     // setWaveletSteps (test_compress_common.cc:362-374)
     int m;
@@ -554,10 +560,22 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     if (staged) TRY(ensure(ctx, ctx->input, inBytes));
     for (int i = 0; i < n; i++) {
       if (dIn[i]) continue;
-      const Plan &pl = plans[i];
+      Plan &pl = plans[i];
       char *dst = P<char>(ctx->input) + pl.inOff;
-      CU(cudaMemcpyAsync(dst, pl.data, (size_t)pl.X * pl.Y * pl.Z * dtype_size(pl.dtype),
-                         cudaMemcpyHostToDevice, s));
+      const size_t es = dtype_size(pl.dtype);
+      if (pl.pitchY == pl.X && pl.pitchZ == (long long)pl.X * pl.Y) {
+        CU(cudaMemcpyAsync(dst, pl.data, (size_t)pl.X * pl.Y * pl.Z * es,
+                           cudaMemcpyHostToDevice, s));
+      } else {
+        // a sub-volume of a pageable array: gathered dense, slice by slice
+        for (int z = 0; z < pl.Z; z++)
+          CU(cudaMemcpy2DAsync(dst + (size_t)z * pl.X * pl.Y * es, (size_t)pl.X * es,
+                               static_cast<const char *>(pl.data) + (size_t)z * pl.pitchZ * es,
+                               (size_t)pl.pitchY * es, (size_t)pl.X * es, pl.Y,
+                               cudaMemcpyHostToDevice, s));
+        pl.pitchY = pl.X;
+        pl.pitchZ = (long long)pl.X * pl.Y;
+      }
       dIn[i] = dst;
     }
   }
@@ -1063,6 +1081,7 @@ wl_status wl_compress_cubelet(wl_ctx *ctx, const void *data, int dtype, const in
                               int onDevice, const wl_params *params, wl_result *out) {
   if (!ctx || !data || !size || !params || !out) return fail(ctx, WL_EINVAL, "null argument");
   wl_cubelet it;
+  memset(&it, 0, sizeof it);
   it.data = data;
   it.dtype = dtype;
   it.size[0] = size[0]; it.size[1] = size[1]; it.size[2] = size[2];
@@ -1187,6 +1206,7 @@ wl_status wl_forward_transform(wl_ctx *ctx, const void *data, int dtype, const i
   if (!ctx || !data || !size || !params || !coeffs || !stored)
     return fail(ctx, WL_EINVAL, "null argument");
   wl_cubelet it;
+  memset(&it, 0, sizeof it);
   it.data = data;
   it.dtype = dtype;
   it.size[0] = size[0]; it.size[1] = size[1]; it.size[2] = size[2];

@@ -57,7 +57,8 @@ class WlResult(ctypes.Structure):
 
 class WlCubelet(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int),
-                ("size", ctypes.c_int * 3), ("params", WlParams)]
+                ("size", ctypes.c_int * 3), ("params", WlParams),
+                ("row_pitch", ctypes.c_longlong), ("slice_pitch", ctypes.c_longlong)]
 
 
 REQ_COMPRESS, REQ_DECOMPRESS = 1, 2
@@ -391,7 +392,9 @@ class Context:
         keep = []
         for i, it in enumerate(items):
             if raw or on_device:
-                ptr, dt, size, prm = it
+                ptr, dt, size, prm = it[:4]
+                if len(it) > 4:  # (row pitch, slice pitch) of a sub-volume
+                    cubs[i].row_pitch, cubs[i].slice_pitch = it[4]
             else:
                 if isinstance(it, tuple):
                     a, prm = it
@@ -408,6 +411,27 @@ class Context:
         st = self.lib.wl_compress_batch(self.h, cubs, n, 1 if on_device else 0, outs)
         self._check(st)
         return adopt_results(self.lib, outs, n)
+
+    def compress_split(self, volume, cube=(128, 128, 128), overlap=8, params=None,
+                       ptr=None, on_device=False):
+        """Split a (Z, Y, X) volume into overlapping cubelets (the reference's
+        `cube split`) and compress them in one batch, reading each cubelet in
+        place from the volume (numpy array, or `ptr` to device / page-locked
+        memory holding it).  Returns (grid, results) in the reference's
+        cubelet order; grid holds (offset, size) in x, y, z order."""
+        from wavelets_gb300.split import split_grid
+        a = volume
+        Z, Y, X = a.shape
+        es = a.dtype.itemsize
+        if ptr is None and not a.flags.c_contiguous:
+            raise ValueError("volume must be C-contiguous")
+        base = ptr if ptr is not None else a.ctypes.data
+        grid = split_grid((X, Y, Z), cube, overlap)
+        items = []
+        for (ox, oy, oz), size in grid:
+            off = (ox + X * (oy + Y * oz)) * es
+            items.append((base + off, NP_TO_WL[a.dtype], size, params, (X, X * Y)))
+        return grid, self.compress_batch(items, on_device=on_device, raw=not on_device)
 
     def decompress(self, c: Compressed, dtype=None) -> np.ndarray:
         """Restore a cubelet; dtype defaults to the original."""
