@@ -83,11 +83,26 @@ def plain2d_workload(seed, count):
     return [(img, p)]
 
 
+def split_workload(seed, count):
+    """The 1024^3 uint16 ellipsoid phantom split into 128^3 cubelets with
+    8-voxel overlap (729 cubelets, read in place from the volume)."""
+    from wavelets_gb300.split import split_grid
+    vol = synth.phantom_u16(seed=seed, size=1024)
+    p = P.Params(steps=(4, 4, 4), wavelet=P.CDF97, threshold_fraction=0.97, quant_alg=P.LOG,
+                 bin_count=512)
+    Z, Y, X = vol.shape
+    grid = split_grid((X, Y, Z), (128, 128, 128), 8)
+    split_workload.volume, split_workload.grid = vol, grid
+    return [(vol[oz:oz + sz, oy:oy + sy, ox:ox + sx], p) for (ox, oy, oz), (sx, sy, sz) in grid]
+
+
 WORKLOADS = {
     "mixed": (mixed_workload, "512 mixed cubelets (axes 16..256, u8/u16/f32, Haar|CDF9/7, "
                               "Lloyd 256, keep 10%)"),
     "volume": (volume_workload, "256^3 float32, CDF9/7 3,3,3, keep 5%, uniform 1024"),
     "plain2d": (plain2d_workload, "2048x2048 uint8, CDF9/7 11,11,0, keep 10%, log 256"),
+    "split1024": (split_workload, "1024^3 uint16 phantom split 128^3 / overlap 8 (729 cubelets, "
+                                  "in place), CDF9/7 4,4,4, keep 3%, log 512"),
 }
 
 
@@ -152,7 +167,8 @@ def _cpu_compress_one(args):
     from oracle import oracle
     qalg = {P.UNIFORM: oracle.UNIFORM, P.LOG: oracle.LOG, P.LLOYD: oracle.LLOYD}[p.quant_alg]
     t = time.perf_counter()
-    oracle.compress_volume(arr, p.steps, p.wavelet, p.threshold_fraction, p.bin_count, qalg,
+    oracle.compress_volume(np.ascontiguousarray(arr), p.steps, p.wavelet, p.threshold_fraction,
+                           p.bin_count, qalg,
                            p.compress_zeros, None)
     return arr.nbytes, time.perf_counter() - t
 
@@ -365,21 +381,39 @@ def main():
     from wavelets_gb300 import lib
 
     ctx = lib.Context(local)
-    in_bytes = sum(a.nbytes for a, _ in items)
-    # device-resident inputs (256-byte aligned) and pinned host copies
-    offs, off = [], 0
-    for a, _ in items:
-        offs.append(off)
-        off += (a.nbytes + 255) // 256 * 256
-    dev = lib.DeviceBuffer(off)
-    pin = lib.PinnedBuffer(off)
-    for (a, _), o in zip(items, offs):
-        dev.upload(a, o)
-        pin.array(np.uint8, (off,))[o:o + a.nbytes] = a.view(np.uint8).ravel()
-    dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
-                 for (a, p), o in zip(items, offs)]
-    host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
-                  for (a, p), o in zip(items, offs)]
+    split_vol = getattr(gen, "volume", None)
+    if split_vol is not None:
+        # one volume in device / pinned memory; every cubelet is read in place
+        # through the volume's row and slice pitches
+        Zv, Yv, Xv = split_vol.shape
+        es = split_vol.dtype.itemsize
+        in_bytes = split_vol.nbytes
+        dev = lib.DeviceBuffer(in_bytes)
+        dev.upload(split_vol)
+        pin = lib.PinnedBuffer(in_bytes)
+        pin.array(split_vol.dtype, split_vol.shape)[...] = split_vol
+        pitch = (Xv, Xv * Yv)
+        offs = [(ox + Xv * (oy + Yv * oz)) * es for (ox, oy, oz), _ in gen.grid]
+        dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p, pitch)
+                     for (a, p), o in zip(items, offs)]
+        host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p, pitch)
+                      for (a, p), o in zip(items, offs)]
+    else:
+        in_bytes = sum(a.nbytes for a, _ in items)
+        # device-resident inputs (256-byte aligned) and pinned host copies
+        offs, off = [], 0
+        for a, _ in items:
+            offs.append(off)
+            off += (a.nbytes + 255) // 256 * 256
+        dev = lib.DeviceBuffer(off)
+        pin = lib.PinnedBuffer(off)
+        for (a, _), o in zip(items, offs):
+            dev.upload(a, o)
+            pin.array(np.uint8, (off,))[o:o + a.nbytes] = a.view(np.uint8).ravel()
+        dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                     for (a, p), o in zip(items, offs)]
+        host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                      for (a, p), o in zip(items, offs)]
 
     def barrier():
         if dist:
@@ -424,7 +458,20 @@ def main():
 
     # ---- PSNR on a sample (equal for batched and plain: identical streams) ----
     psnrs = []
-    for (a, p), c in list(zip(items, out))[:: max(1, len(items) // 32)]:
+    if split_vol is not None:
+        # whole volume: every cubelet restores its part, overlaps overwritten
+        back = np.zeros(split_vol.shape, np.float32)
+        for ((ox, oy, oz), (sx, sy, sz)), c in zip(gen.grid, out):
+            back[oz:oz + sz, oy:oy + sy, ox:ox + sx] = ctx.decompress(c)
+        sq = 0.0
+        for z0 in range(0, split_vol.shape[0], 64):
+            d = back[z0:z0 + 64].astype(np.float64) - split_vol[z0:z0 + 64]
+            sq += float(np.sum(d * d))
+        mse = sq / split_vol.size
+        psnrs.append(10 * np.log10(65535.0 ** 2 / mse) if mse > 0 else 999.0)
+        del back
+    for (a, p), c in ([] if split_vol is not None else
+                      list(zip(items, out))[:: max(1, len(items) // 32)]):
         back = ctx.decompress(c).astype(np.float64)
         x = a.astype(np.float64)
         peak = 255.0 if a.dtype == np.uint8 else (65535.0 if a.dtype == np.uint16

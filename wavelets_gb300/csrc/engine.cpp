@@ -20,6 +20,7 @@
 #include <map>
 #include <unordered_map>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "cubelet_io.h"
@@ -679,16 +680,35 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     const CubeletState *hs = H<CubeletState>(ctx->hState);
     float *tab = H<float>(ctx->hTab);
     int4 *lh = H<int4>(ctx->hLogHdr);
+    // one table per log cubelet, independent: spread over host threads
+    std::vector<int> logIdx;
     for (int i = 0; i < n; i++) {
       lh[i] = make_int4(0, 0, 0, 0);
-      if (plans[i].p.quant_alg != WL_LOG) continue;
-      LogTable t;
-      log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
-      if (t.nPos + t.nNeg > 2 * plans[i].p.bin_count)
-        return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)", i);
-      lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
-      std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
+      if (plans[i].p.quant_alg == WL_LOG) logIdx.push_back(i);
     }
+    std::atomic<int> next{0}, bad{-1};
+    auto work = [&]() {
+      LogTable t;
+      for (int k; (k = next.fetch_add(1)) < (int)logIdx.size();) {
+        const int i = logIdx[k];
+        log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
+        if (t.nPos + t.nNeg > 2 * plans[i].p.bin_count) {
+          bad.store(i);
+          continue;
+        }
+        lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
+        std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
+      }
+    };
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nThreads = std::min<int>({hw, 16, ((int)logIdx.size() + 7) / 8});
+    std::vector<std::thread> pool;
+    for (int k = 1; k < nThreads; k++) pool.emplace_back(work);
+    work();
+    for (std::thread &th : pool) th.join();
+    if (bad.load() >= 0)
+      return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)",
+                  bad.load());
     CU(cudaMemcpyAsync(ctx->qtable.p, tab, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(ctx->logHdr.p, lh, n * sizeof(int4), cudaMemcpyHostToDevice, s));
   }

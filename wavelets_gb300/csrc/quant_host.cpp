@@ -77,17 +77,18 @@ template <class P> uint32_t first_true_guess(uint32_t lo, uint32_t hi, double gu
   if (!(guess > 0) || !std::isfinite(guess)) return first_true(lo, hi, pred);
   const uint32_t ug = float_to_bits((float)guess);
   if (ug <= lo || ug >= hi) return first_true(lo, hi, pred);
-  uint32_t step = 64, a, b;
+  // the double-precision guess is usually within a few ulps of the answer
+  uint32_t step = 4, a, b;
   for (;;) {  // a: lo or a point where pred is false
     a = ug - lo > step ? ug - step : lo;
     if (a == lo || !pred(a)) break;
-    step *= 4;
+    step *= 8;
   }
-  step = 64;
+  step = 4;
   for (;;) {  // b: hi or a point where pred is true
     b = hi - ug > step ? ug + step : hi;
     if (b == hi || pred(b)) break;
-    step *= 4;
+    step *= 8;
   }
   return first_true(a, b, pred);
 }
