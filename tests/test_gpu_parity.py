@@ -327,3 +327,41 @@ def test_plain_2d_u8_full_size(ctx):
     mse = float(np.mean((back.astype(np.float64) - arr) ** 2))
     psnr = 10 * np.log10(255.0 ** 2 / mse)
     assert psnr > 25, psnr
+
+
+FP64_RTOL = 2e-6  # max|gpu - fp64 lifting| / max|fp64| (the reference itself: <= 4.6e-7)
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_ids(MANIFEST["cases"]))
+def test_transform_error_against_float64_lifting(ctx, case):
+    """The GPU transform (default lifting mode) against the float64 lifting
+    yardstick: within FP64_RTOL of the largest coefficient."""
+    from oracle import lifting64
+    p = _params(case)
+    coeffs, _ = ctx.forward_transform(_input(case), p)
+    ref, _ = lifting64.forward(_input(case), p.steps, p.wavelet)
+    scale = float(np.abs(ref).max())
+    if scale == 0:
+        assert np.abs(coeffs).max() == 0
+        return
+    assert float(np.abs(coeffs - ref).max()) / scale <= FP64_RTOL
+
+
+@pytest.mark.parametrize("shape,steps,wavelet", [((256, 256, 256), (3, 3, 3), P.CDF97),
+                                                 ((1, 2048, 2048), (11, 11, 0), P.CDF97),
+                                                 ((96, 128, 48), (-1, -1, -1), P.HAAR)])
+def test_full_size_transform_error_against_float64_lifting(ctx, shape, steps, wavelet):
+    """Full-size volumes of the benchmark workloads: error stated and bounded."""
+    from oracle import lifting64
+    if shape[0] == 1:
+        a = synth.plain_2d()
+    elif shape == (256, 256, 256):
+        a = synth.volume_f32()
+    else:
+        a = synth.scaled_blob_cubelet(np.random.default_rng(3), shape, np.uint16)
+    p = P.Params(steps=steps, wavelet=wavelet)
+    coeffs, _ = ctx.forward_transform(a, p)
+    ref, _ = lifting64.forward(a, steps, wavelet)
+    err = float(np.abs(coeffs - ref).max()) / float(np.abs(ref).max())
+    print(f"transform error vs float64 lifting, {shape} {steps}: {err:.3e}")
+    assert err <= FP64_RTOL

@@ -88,3 +88,23 @@ def test_reference_cli_flags_rejected_like_reference(tmp_path):
     inp = os.path.join(GOLDEN, MANIFEST["cases"][0]["input"])
     assert oracle.main(["-thresh", "1.5", inp, str(tmp_path / "x.cube")]) != 0
     assert oracle.main(["-qalg", "count", inp, str(tmp_path / "x.cube")]) != 0
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=_case_ids())
+def test_float64_lifting_agrees_with_reference_coefficients(case):
+    """The float64 lifting yardstick reproduces the reference's own float32
+    coefficients to float32 rounding (pins the yardstick before it measures
+    the GPU transform)."""
+    from oracle import lifting64
+    from wavelets_gb300 import params as P
+    p, _, _ = P.parse_flags(MANIFEST["params"][case["params"]])
+    a = cubefile.read_file(os.path.join(GOLDEN, case["input"]))[0].array()
+    got, st = lifting64.forward(a, p.steps, p.wavelet)
+    assert [int(s) for s in case["stats"]["steps"]] == list(st)
+    ref = np.fromfile(os.path.join(GOLDEN, case["coeffs"]), np.float32).astype(np.float64)
+    assert got.shape == ref.shape
+    scale = float(np.abs(got).max())
+    if scale == 0:
+        assert np.abs(ref).max() == 0
+        return
+    assert float(np.abs(got - ref).max()) / scale <= 2e-6
