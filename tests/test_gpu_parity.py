@@ -365,3 +365,4 @@ def test_full_size_transform_error_against_float64_lifting(ctx, shape, steps, wa
     err = float(np.abs(coeffs - ref).max()) / float(np.abs(ref).max())
     print(f"transform error vs float64 lifting, {shape} {steps}: {err:.3e}")
     assert err <= FP64_RTOL
+

@@ -307,20 +307,33 @@ def adopt_results(lib, outs, n) -> List["Compressed"]:
         for i in range(n):
             lib.wl_result_free(ctypes.byref(outs[i]))
         return res
-    lo = int(ptrs[used].min())
-    hi = int((ptrs + 4 * cnts.astype(np.uint64))[used].max())
-    buf = (ctypes.c_char * (hi - lo)).from_address(lo)
-    buf._owner = _ResultsOwner(lib, outs, n)
-    base = np.frombuffer(buf, np.uint8)
-    rel = np.where(used, ptrs - np.uint64(lo), 0).astype(np.int64).tolist()
-    ends = (np.where(used, ptrs - np.uint64(lo), 0).astype(np.int64)
+    # one numpy view per storage block (a pipelined batch has several); all
+    # views share the owner that releases the batch's results
+    owner = _ResultsOwner(lib, outs, n)
+    slab = rec["owner"]
+    ends_abs = ptrs + 4 * cnts.astype(np.uint64)
+    bases, lo_of = {}, {}
+    for sid in np.unique(slab).tolist():
+        sel = used & (slab == sid)[:, None]
+        if not sel.any():
+            continue
+        lo = int(ptrs[sel].min())
+        buf = (ctypes.c_char * (int(ends_abs[sel].max()) - lo)).from_address(lo)
+        buf._owner = owner
+        bases[sid], lo_of[sid] = np.frombuffer(buf, np.uint8), lo
+    slab_l = slab.tolist()
+    lo_row = np.array([lo_of.get(x, 0) for x in slab_l], np.uint64)[:, None]
+    rel = np.where(used, ptrs - lo_row, 0).astype(np.int64).tolist()
+    ends = (np.where(used, ptrs - lo_row, 0).astype(np.int64)
             + 4 * np.where(used, cnts, 0)).tolist()
+    empty_base = np.zeros(0, np.uint8)
     f = {k: rec[k].tolist() for k in _RESULT_DT.names if k not in ("words", "decode",
                                                                     "boundaries", "values", "owner")}
     e32, ef = np.zeros(0, np.float32), np.zeros(0, np.float32)
     res = []
     for i in range(n):
         o, z = rel[i], ends[i]
+        base = bases.get(slab_l[i], empty_base)
         res.append(Compressed(
             tuple(f["size"][i]), tuple(f["original_size"][i]), f["original_dtype"][i],
             tuple(f["steps"][i]), f["wavelet"][i], f["quant_alg"][i], f["bin_count"][i],
