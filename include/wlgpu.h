@@ -241,6 +241,48 @@ int wl_last_launch_count(const wl_ctx *ctx);
 wl_status wl_set_profiling(wl_ctx *ctx, int on);
 wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
 
+/* ---- Tile autotuner ------------------------------------------------------
+ * No reference counterpart (the reference's GPU transform has fixed block
+ * shapes, dwt_gpu.cu).  The column-tile transform runs the rows of each size
+ * class -- pass (0 forward x, 1 forward y, 2 forward z, 3 inverse z,
+ * 4 inverse y, 5 inverse x), element type of the pass's global side (0 u8,
+ * 1 u16, 2 i32, 3 f32; +4 for 8/16-bit input read from page-locked host
+ * memory) and row-length class k (rows of 2^(k-1)+1 .. 2^k elements) -- in
+ * tiles of 32, 64 or 128 rows: 32-row tiles split every level into four
+ * segments over four warps, 64-row tiles into two, 128-row tiles sweep each
+ * row whole.  wl_autotune times every height that fits on a synthetic batch
+ * of about 2^24 elements per class on ctx's device (rows up to max_len
+ * elements, 0 = 512; reps timed launches per candidate, 0 = 5) and keeps the
+ * fastest in a process-wide table that every context uses from its next
+ * call.  Untuned classes use 128-row tiles for rows of up to 64 elements and
+ * 32-row tiles above.  The tile height changes speed only: every height does
+ * the same arithmetic on every element, so results are bit-identical.
+ *
+ * The table as text (wl_tune_export; *len = bytes without the NUL, buf may be
+ * NULL to ask for the length): one line per tuned class,
+ * "pass type class rows us32 us64 us128" with the measured microseconds per
+ * launch (0 = not measured).  wl_tune_import reads the same lines (the times
+ * are optional); wl_tune_reset returns every class to the default. */
+wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps);
+wl_status wl_tune_export(char *buf, size_t cap, size_t *len);
+wl_status wl_tune_import(const char *text);
+void wl_tune_reset(void);
+
+/* ---- CUDA graphs ---------------------------------------------------------
+ * mode 1 (default): a batch whose geometry (count, element types, sizes,
+ * pitches, parameters, kind of input memory) repeats the previous call's is
+ * captured as a CUDA graph, and every later call with that geometry replays
+ * it (up to 4 geometries per context); input addresses and per-call tables
+ * reach the graph through page-locked upload buffers, so results are those
+ * of the direct launches.  Batches that never repeat (serving) launch
+ * directly and pay no capture.  mode 0: always launch directly.
+ * wl_graph_stats: {direct segment runs, captures, replays, failed captures};
+ * a failed capture turns graphs off for the context and wl_graph_error
+ * names the reason. */
+wl_status wl_set_graph_mode(wl_ctx *ctx, int mode);
+wl_status wl_graph_stats(const wl_ctx *ctx, long long out[4]);
+const char *wl_graph_error(const wl_ctx *ctx);
+
 /* Threshold selection that allocates nothing.  This entry point has no
  * counterpart in the reference.  It is for callers that may not call
  * cudaMalloc: code running while a stream is being captured (allocation is

@@ -89,3 +89,20 @@ def test_serve_create_without_gpu_fails_cleanly(lib):
                                     ctypes.POINTER(ctypes.c_void_p)]
     assert lib.wl_serve_create(0, ctypes.byref(cfg), ctypes.byref(h)) != 0
     assert not h.value
+
+
+def test_tile_table_round_trip(lib):
+    """The tile table needs no GPU: lines imported come back exported, bad
+    lines are refused, reset empties it."""
+    from wavelets_gb300 import lib as L
+    L.tune_reset()
+    assert L.tune_table() == ""
+    L.tune_load("0 0 6 64 10.5 9.25 11\n3 3 9 32\n\n")
+    rows = L.tune_rows(L.tune_table())
+    assert rows[(0, 0, 6)] == (64, (10.5, 9.25, 11.0))
+    assert rows[(3, 3, 9)][0] == 32
+    for bad in ("0 0 6 48\n", "6 0 6 32\n", "0 8 6 32\n", "0 0 10 32\n", "0 0\n"):
+        with pytest.raises(L.WlError):
+            L.tune_load(bad)
+    L.tune_reset()
+    assert L.tune_table() == ""

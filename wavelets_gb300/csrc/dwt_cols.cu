@@ -1,5 +1,5 @@
-// Column-tile wavelet passes: a CTA of four warps per tile of 32 rows; every
-// lane owns one row of the tile.
+// Column-tile wavelet passes: a CTA of four warps per tile of 32, 64 or 128
+// rows; every lane owns one row of the tile.
 //
 // The row-cooperative kernel (dwt.cu) spreads a row over the lanes of a warp
 // and pays index arithmetic and a warp barrier for every lifting step of
@@ -7,12 +7,14 @@
 // streaming sweep that keeps a two-pair window in registers and applies all
 // four lifting steps (or the Haar butterfly) on the way, so an element costs
 // one shared load, one shared store and four float operations per level.
-// The four warps of the CTA split every level of the 32 rows into four
-// segments of pairs, which gives the SM four times the warps a one-warp tile
-// would at the same shared memory.
-//
-// Rows of at most 64 elements use 128-row tiles instead: each warp sweeps 32
-// rows whole, with no halos and no barriers between levels.
+// The warps that share 32 rows split every level into segments of pairs:
+// four segments for a 32-row tile, two for a 64-row tile, and none for a
+// 128-row tile, where each warp sweeps its 32 rows whole with no halos and no
+// barriers between levels.  More segments give the SM more warps per byte of
+// shared memory; fewer spend less on halos and barriers.  The tile height of
+// each row-length class is chosen by measurement (the tile autotuner in the
+// engine); the default is 128 rows for rows of at most 64 elements and 32
+// rows above.
 //
 // Tile layout in shared memory: element p of tile row r at tile[p * (R+1) + r]
 // for an R-row tile.  Lanes reading one position of 32 neighbouring rows hit
@@ -292,16 +294,15 @@ __device__ __forceinline__ int group_width(int len) {
   return G;
 }
 
-// ROWS = 32: the four warps share the tile's 32 rows and split every level
-// into segments (long rows).  ROWS = 128: every warp owns 32 rows of the
-// tile and sweeps them whole, with no halos and no barriers between levels
-// (rows of at most 64 elements, where segments would be mostly halo).
+// ROWS = 32, 64 or 128: warp w owns rows 32 (w / kSegs) .. +31 of the tile
+// and segment w % kSegs of every level of them, kSegs = 128 / ROWS.
 template <typename InT, typename OutT, bool INV, bool VEC, int ROWS>
 __global__ void __launch_bounds__(kThreadsC)
 dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                 int nPasses) {
+  static_assert(ROWS == kRows || ROWS == 2 * kRows || ROWS == 4 * kRows, "tile height");
   constexpr int kP = ROWS + 1;                 // words between positions of a row
-  constexpr int kSegs = ROWS == kRows ? kSeg : 1;
+  constexpr int kSegs = kSeg * kRows / ROWS;   // warps per 32 rows = segments per level
   extern __shared__ float4 smem4[];
   float *tile = reinterpret_cast<float *>(smem4);
   __shared__ long long rowIn[ROWS], rowOut[ROWS];
@@ -319,8 +320,9 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   const int r0 = (bid - tilePrefix[lo]) * ROWS;
   const int nr = min(ROWS, d.rows - r0);
   // the row this thread moves and computes, and its share of the elements
-  const int me = ROWS == kRows ? lane : (int)threadIdx.x;
-  const int cFirst = ROWS == kRows ? warp : 0, cStep = ROWS == kRows ? kSeg : 1;
+  const int seg = warp % kSegs;
+  const int me = (warp / kSegs) * kRows + lane;
+  const int cFirst = seg, cStep = kSegs;
   // exact-order CDF 9/7 passes never come here (they run in dwt.cu)
   const bool lifting = d.wavelet == WL_CDF97;
   if ((int)threadIdx.x < ROWS) {
@@ -401,8 +403,8 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   for (int it = 0; it < S; it++) {
     const int lev = INV ? S - 1 - it : it;
     const int h = (L >> lev) >> 1, P = (1 << lev) * kP;
-    const int i0 = kSegs == 1 ? 0 : (warp * h) / kSegs;
-    const int i1 = kSegs == 1 ? h : ((warp + 1) * h) / kSegs;
+    const int i0 = kSegs == 1 ? 0 : (seg * h) / kSegs;
+    const int i1 = kSegs == 1 ? h : ((seg + 1) * h) / kSegs;
     if (!lifting) {
       if (rowOk) haar_seg(x, P, i0, i1, INV);
     } else if (h == 1) {
@@ -480,18 +482,27 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
 template <typename InT, typename OutT, bool INV, bool VEC = false>
 void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
               cudaStream_t s) {
-  auto k = rows == kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows>
-                         : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows>;
+  auto k = rows == kRows       ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows>
+           : rows == 2 * kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, 2 * kRows>
+                               : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows>;
   if (smem > 32 * 1024) raise_smem_limit(k, smem);  // static + dynamic may pass 48 KB
   k<<<tiles, kThreadsC, smem, s>>>(p, tp, n);
 }
 
 }  // namespace
 
-// rows of at most 64 elements: 128-row tiles swept whole by each warp
+// default tile height: rows of at most 64 elements in 128-row tiles swept
+// whole by each warp, longer rows in 32-row tiles of four segments
 int dwt_cols_tile_rows(int L) { return L <= 64 ? 4 * kRows : kRows; }
 
-int dwt_cols_smem_bytes(int L) { return L * (dwt_cols_tile_rows(L) + 1) * (int)sizeof(float); }
+int dwt_cols_smem_bytes(int L, int rows) { return L * (rows + 1) * (int)sizeof(float); }
+
+// dynamic shared memory available beside the kernel's static arrays
+bool dwt_cols_rows_fit(int L, int rows) {
+  if (rows != kRows && rows != 2 * kRows && rows != 4 * kRows) return false;
+  const int kStatic = 2 * 4 * kRows * 8 + 32 * 4 + 1024;  // row bases, scales, reserve
+  return dwt_cols_smem_bytes(L, rows) <= 227 * 1024 - kStatic;
+}
 
 void launch_dwt_cols(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
                      int inType, int outType, bool inverse, bool vecLoad, cudaStream_t s) {

@@ -179,14 +179,41 @@ void raise_smem_limit(const void *func, int bytes) {
 }
 }  // namespace wl
 
+namespace {
+// A captured compression of one batch geometry: the launch sequence, grids
+// and kernel arguments are functions of the geometry (key) and of the
+// context's buffers (gen); what changes from call to call -- input
+// addresses, thresholds' host tables -- travels through the page-locked
+// upload block and tables that the graph's copy nodes read at launch time.
+struct GraphEntry {
+  std::vector<long long> key;
+  unsigned long long gen = 0;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  int launches[2] = {0, 0};  // kernels in each segment
+  unsigned long long lastUse = 0;
+};
+constexpr size_t kGraphCache = 4;
+}  // namespace
+
 struct wl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  DevBuf input, coef, coef2, bins, tokCount, state, cub, selHist, lloydHist, qtable, dqtable, qlut,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkPrefix, chunkCub, groupCub, codes, codeLen, decode,
+  DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
-  HostBuf hState, hWords, hDecode, hPasses, hCub, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
+  HostBuf hState, hWords, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
+  // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
+  // and replay it from then on
+  int graphMode = 1;
+  bool capturing = false;
+  unsigned long long gen = 0;  // bumped whenever a buffer is reallocated
+  unsigned long long useClock = 0;
+  std::vector<GraphEntry> graphs;
+  std::vector<long long> lastKey;
+  unsigned long long lastGen = ~0ull;
+  long long graphStats[4] = {0, 0, 0, 0};  // direct runs, captures, replays, capture failures
+  std::string graphErr;
   cudaEvent_t ev[7] = {};
   float timings[6] = {0, 0, 0, 0, 0, 0};
   bool profiling = false;
@@ -220,6 +247,7 @@ wl_status ensure(wl_ctx *ctx, DevBuf &b, size_t bytes) {
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.cap = 0;
+  ctx->gen++;
   size_t want = bytes + bytes / 4;
   cudaError_t e = cudaMalloc(&b.p, want);
   if (e != cudaSuccess) {
@@ -236,6 +264,7 @@ wl_status ensure_host(wl_ctx *ctx, HostBuf &b, size_t bytes) {
   if (b.p) cudaFreeHost(b.p);
   b.p = nullptr;
   b.cap = 0;
+  ctx->gen++;
   size_t want = bytes + bytes / 4;
   cudaError_t e = cudaMallocHost(&b.p, want);
   if (e != cudaSuccess) {
@@ -254,11 +283,106 @@ wl_status ensure_host(wl_ctx *ctx, HostBuf &b, size_t bytes) {
 
 template <class T> T *P(DevBuf &b) { return static_cast<T *>(b.p); }
 
+// An event record on the context's stream; during graph capture an event
+// node, so that replays record it too.
+inline cudaError_t record(wl_ctx *ctx, cudaEvent_t e) {
+  return ctx->capturing ? cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal)
+                        : cudaEventRecord(e, ctx->stream);
+}
+
 // kernel-group boundary for the optional per-group timings
 inline void mark(wl_ctx *ctx, int i) {
-  if (ctx->profiling) cudaEventRecord(ctx->pev[i], ctx->stream);
+  if (ctx->profiling) record(ctx, ctx->pev[i]);
 }
 template <class T> T *H(HostBuf &b) { return static_cast<T *>(b.p); }
+
+void drop_graph(GraphEntry &g) {
+  for (cudaGraphExec_t &x : g.exec)
+    if (x) {
+      cudaGraphExecDestroy(x);
+      x = nullptr;
+    }
+}
+
+// The cached graph of this batch geometry, a new (empty) entry when the
+// geometry repeats the previous call's, else null: batches that never repeat
+// (serving) run directly and pay no capture.
+GraphEntry *graph_for(wl_ctx *ctx, std::vector<long long> &&key) {
+  // entries of reallocated buffers can never match again
+  for (size_t i = 0; i < ctx->graphs.size();) {
+    if (ctx->graphs[i].gen != ctx->gen) {
+      drop_graph(ctx->graphs[i]);
+      ctx->graphs.erase(ctx->graphs.begin() + i);
+    } else {
+      i++;
+    }
+  }
+  for (GraphEntry &g : ctx->graphs)
+    if (g.key == key) {
+      g.lastUse = ++ctx->useClock;
+      return &g;
+    }
+  const bool repeat = ctx->lastGen == ctx->gen && ctx->lastKey == key;
+  if (!repeat) {
+    ctx->lastKey = std::move(key);
+    ctx->lastGen = ctx->gen;
+    return nullptr;
+  }
+  if (ctx->graphs.size() >= kGraphCache) {
+    size_t lru = 0;
+    for (size_t i = 1; i < ctx->graphs.size(); i++)
+      if (ctx->graphs[i].lastUse < ctx->graphs[lru].lastUse) lru = i;
+    drop_graph(ctx->graphs[lru]);
+    ctx->graphs.erase(ctx->graphs.begin() + lru);
+  }
+  ctx->graphs.emplace_back();
+  GraphEntry &g = ctx->graphs.back();
+  g.key = std::move(key);
+  g.gen = ctx->gen;
+  g.lastUse = ++ctx->useClock;
+  return &g;
+}
+
+// Run one segment of device work: directly, by replaying its graph, or by
+// capturing the graph first.  A capture that fails turns graphs off for the
+// context (the reason is kept) and the segment runs directly.
+template <class F> wl_status run_segment(wl_ctx *ctx, GraphEntry *ge, int seg, F &&enqueue) {
+  cudaStream_t s = ctx->stream;
+  if (!ge || !ctx->graphMode) {
+    ctx->graphStats[0]++;
+    return enqueue();
+  }
+  if (ge->exec[seg]) {
+    ctx->graphStats[2]++;
+    ctx->launches += ge->launches[seg];
+    CU(cudaGraphLaunch(ge->exec[seg], s));
+    return WL_OK;
+  }
+  CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  ctx->capturing = true;
+  const int launches = ctx->launches;
+  const wl_status st = enqueue();
+  ctx->capturing = false;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (st == WL_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge->exec[seg], g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (st == WL_OK && e == cudaSuccess) {
+    ctx->graphStats[1]++;
+    ge->launches[seg] = ctx->launches - launches;
+    CU(cudaGraphLaunch(ge->exec[seg], s));
+    return WL_OK;
+  }
+  // capture failed: nothing was enqueued; run the segment directly
+  ge->exec[seg] = nullptr;
+  cudaGetLastError();
+  ctx->graphStats[3]++;
+  ctx->graphErr = st != WL_OK ? ctx->err : cudaGetErrorString(e);
+  ctx->graphMode = 0;
+  ctx->launches = launches;
+  ctx->graphStats[0]++;
+  return enqueue();
+}
 
 wl_status check_params(wl_ctx *ctx, const wl_params &p) {
   if (p.wavelet != WL_HAAR && p.wavelet != WL_CDF97)
@@ -388,47 +512,78 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
   zs[group_key(false, WL_F32, f.L)].push_back(f);
 }
 
-// Upload a group of passes (descriptor + tile prefix) and launch it.
-wl_status run_group(wl_ctx *ctx, const std::vector<PassDesc> &g, size_t &hoff,
-                    int inType, int outType, bool inverse, bool cols = false,
-                    bool vecLoad = false) {
+// One launch of a transform pass group: its descriptors and tile prefix sit
+// at `off` bytes into the context's upload block.
+struct GroupLaunch {
+  size_t off;
+  int n, tiles, smem, rows, inType, outType;
+  bool inverse, cols, vec;
+};
+
+// Stage a group of passes (descriptors + tile prefix) at hoff of the host
+// upload block and note its launch.  Column-tile groups take the tile height
+// of their size class from the tile table (kind: the pass).
+wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int kind, int inType,
+                      int outType, bool inverse, bool cols, bool vec,
+                      std::vector<GroupLaunch> &out, int forceRows = 0) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
-  const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int) + 64;
+  const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int);
   if (hoff + bytes > ctx->hPasses.cap || hoff + bytes > ctx->passes.cap)
     return fail(ctx, WL_ENOMEM, "pass staging too small");
+  int rows = 0;
+  if (cols) {
+    int Lmax = 0;
+    for (const PassDesc &d : g) Lmax = std::max(Lmax, d.L);
+    const int gtype = kind == kTuneFwdX ? inType : kind == kTuneInvX ? outType : WL_F32;
+    rows = forceRows ? forceRows : tuned_cols_rows(kind, tune_type_index(gtype, vec), Lmax);
+    for (PassDesc &d : g) {
+      d.T = rows;
+      d.tiles = (d.rows + rows - 1) / rows;
+    }
+  }
   char *h = H<char>(ctx->hPasses) + hoff;
-  char *d = P<char>(ctx->passes) + hoff;
   memcpy(h, g.data(), n * sizeof(PassDesc));
   int *tp = reinterpret_cast<int *>(h + n * sizeof(PassDesc));
   int tiles = 0, smem = 0;
   for (size_t i = 0; i < n; i++) {
     tp[i] = tiles;
     tiles += g[i].tiles;
-    smem = std::max(smem, cols ? dwt_cols_smem_bytes(g[i].L)
+    smem = std::max(smem, cols ? dwt_cols_smem_bytes(g[i].L, rows)
                                : dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
   }
   tp[n] = tiles;
-  CU(cudaMemcpyAsync(d, h, bytes - 64, cudaMemcpyHostToDevice, ctx->stream));
-  ctx->launches++;
-  const PassDesc *dp = reinterpret_cast<const PassDesc *>(d);
-  const int *dtp = reinterpret_cast<const int *>(d + n * sizeof(PassDesc));
-  if (cols)
-    launch_dwt_cols(dp, dtp, (int)n, tiles, smem, g[0].T, inType, outType, inverse, vecLoad,
-                    ctx->stream);
-  else
-    launch_dwt_pass(dp, dtp, (int)n, tiles, smem, inType, outType, inverse, ctx->stream);
-  CU(cudaGetLastError());
+  out.push_back({hoff, (int)n, tiles, smem, rows, inType, outType, inverse, cols, vec});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
 
-wl_status run_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int outType,
-                     bool inverse) {
+// Stage every group of one transform phase.
+wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind, int outType,
+                       bool inverse, std::vector<GroupLaunch> &out) {
   for (const auto &kv : gs) {
     const bool cols = (kv.first >> 12) & 1, vec = (kv.first >> 13) & 1;
     const int dt = (kv.first >> 8) & 15;
-    TRY(run_group(ctx, kv.second, hoff, inverse ? WL_F32 : dt, outType, inverse, cols, vec));
+    TRY(stage_group(ctx, kv.second, hoff, kind, inverse ? WL_F32 : dt, outType, inverse, cols, vec,
+                    out));
+  }
+  return WL_OK;
+}
+
+// Launch staged groups [a, b) whose descriptors are already on the device.
+wl_status launch_groups(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b) {
+  const char *base = P<char>(ctx->passes);
+  for (size_t i = a; i < b; i++) {
+    const GroupLaunch &l = ls[i];
+    const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
+    const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
+    if (l.cols)
+      launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.inType, l.outType, l.inverse,
+                      l.vec, ctx->stream);
+    else
+      launch_dwt_pass(dp, dtp, l.n, l.tiles, l.smem, l.inType, l.outType, l.inverse, ctx->stream);
+    CU(cudaGetLastError());
+    ctx->launches++;
   }
   return WL_OK;
 }
@@ -504,8 +659,6 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->bins, (coefTotal + (long long)n * kChunk) * 2));
   TRY(ensure(ctx, ctx->tokCount, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->state, n * sizeof(CubeletState)));
-  TRY(ensure(ctx, ctx->cub, n * sizeof(CubeletDev)));
-  TRY(ensure(ctx, ctx->chunkPrefix, n * sizeof(long long)));
   TRY(ensure(ctx, ctx->chunkCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->groupCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
@@ -523,10 +676,13 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->words, wordsTotal * 4));
   TRY(ensure(ctx, ctx->logHdr, n * sizeof(int4)));
   TRY(ensure(ctx, ctx->meta, (size_t)n * (4 * kMaxSymbols + 2 * kMaxBins) * 4));
-  const size_t passBytes = (size_t)3 * n * (sizeof(PassDesc) + sizeof(int)) + 8 * 4096;
+  // upload block: cubelet records | chunk prefix | transform pass groups
+  const size_t cubBytes = ((size_t)n * sizeof(CubeletDev) + 255) & ~(size_t)255;
+  const size_t prefBytes = ((size_t)n * sizeof(long long) + 255) & ~(size_t)255;
+  const size_t passBytes =
+      cubBytes + prefBytes + (size_t)3 * n * (sizeof(PassDesc) + sizeof(int) + 260) + 4096;
   TRY(ensure(ctx, ctx->passes, passBytes));
   TRY(ensure_host(ctx, ctx->hPasses, passBytes));
-  TRY(ensure_host(ctx, ctx->hCub, n * sizeof(CubeletDev) + n * sizeof(long long)));
   TRY(ensure_host(ctx, ctx->hState, n * sizeof(CubeletState)));
   TRY(ensure_host(ctx, ctx->hLogHdr, n * sizeof(int4)));
   if (anyLog) TRY(ensure_host(ctx, ctx->hTab, (size_t)tableTotal * 4));
@@ -581,9 +737,9 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     }
   }
 
-  // ---- descriptors ----
-  CubeletDev *hc = H<CubeletDev>(ctx->hCub);
-  long long *hp = reinterpret_cast<long long *>(hc + n);
+  // ---- descriptors (host side of the upload block) ----
+  CubeletDev *hc = H<CubeletDev>(ctx->hPasses);
+  long long *hp = reinterpret_cast<long long *>(H<char>(ctx->hPasses) + cubBytes);
   long long groupTotal = 0;
   for (int i = 0; i < n; i++) {
     const Plan &pl = plans[i];
@@ -605,17 +761,11 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     groupTotal += (pl.nChunks + kQuantGroup - 1) / kQuantGroup;
     hp[i] = pl.chunkBase;
   }
-  CU(cudaMemcpyAsync(ctx->cub.p, hc, n * sizeof(CubeletDev), cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(ctx->chunkPrefix.p, hp, n * sizeof(long long), cudaMemcpyHostToDevice, s));
-  CU(cudaMemsetAsync(ctx->state.p, 0, n * sizeof(CubeletState), s));
-  CU(cudaMemsetAsync(ctx->selHist.p, 0, (size_t)n * kSelectBins * 4, s));
-  CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)n * kMaxSymbols * 8, s));
-  if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
 
   DevBatch b;
   memset(&b, 0, sizeof b);
   b.n = n;
-  b.cub = P<CubeletDev>(ctx->cub);
+  b.cub = reinterpret_cast<CubeletDev *>(P<char>(ctx->passes));
   b.state = P<CubeletState>(ctx->state);
   b.coef = P<float>(ctx->coef);
   b.coef2 = P<float>(ctx->coef2);
@@ -634,7 +784,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.codeLen = P<uint8_t>(ctx->codeLen);
   b.decode = P<int>(ctx->decode);
   b.words = P<uint32_t>(ctx->words);
-  b.chunkPrefix = P<long long>(ctx->chunkPrefix);
+  b.chunkPrefix = reinterpret_cast<long long *>(P<char>(ctx->passes) + cubBytes);
   b.chunkCub = P<int>(ctx->chunkCub);
   b.groupCub = P<int>(ctx->groupCub);
   b.totalGroups = groupTotal;
@@ -642,20 +792,105 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
 
-  // ---- transform ----
-  ctx->launches = 0;
   PassGroups xs, ys, zs;
   for (int i = 0; i < n; i++)
     forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs, ys, zs);
-  size_t hoff = 0;
-  mark(ctx, 0);
-  TRY(run_groups(ctx, xs, hoff, WL_F32, false));
-  mark(ctx, 1);
-  TRY(run_groups(ctx, ys, hoff, WL_F32, false));
-  mark(ctx, 2);
-  TRY(run_groups(ctx, zs, hoff, WL_F32, false));
-  mark(ctx, 3);
-  CU(cudaEventRecord(ctx->ev[1], s));
+  std::vector<GroupLaunch> gl;
+  size_t hoff = cubBytes + prefBytes;
+  TRY(stage_groups(ctx, xs, hoff, kTuneFwdX, WL_F32, false, gl));
+  const size_t gx = gl.size();
+  TRY(stage_groups(ctx, ys, hoff, kTuneFwdY, WL_F32, false, gl));
+  const size_t gy = gl.size();
+  TRY(stage_groups(ctx, zs, hoff, kTuneFwdZ, WL_F32, false, gl));
+  const size_t upBytes = hoff;
+
+  // ---- device work, in one or two segments (a host step between them
+  // computes the log quantizer tables); each may run as a CUDA graph ----
+  ctx->launches = 0;
+  auto quantize_to_end = [&]() -> wl_status {
+    if (anyLog) {
+      CU(cudaMemcpyAsync(ctx->qtable.p, ctx->hTab.p, (size_t)tableTotal * 4,
+                         cudaMemcpyHostToDevice, s));
+      CU(cudaMemcpyAsync(ctx->logHdr.p, ctx->hLogHdr.p, n * sizeof(int4), cudaMemcpyHostToDevice, s));
+    }
+    CU(record(ctx, ctx->ev[2]));
+    launch_quant_params(b, s);
+    ctx->launches += 1;
+    if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 3; }
+    mark(ctx, 5);
+    launch_quantize(b, b.coef, maxTable, s);
+    mark(ctx, 6);
+    launch_runs(b, s);
+    ctx->launches += 2;
+    mark(ctx, 7);
+    CU(cudaGetLastError());
+    CU(record(ctx, ctx->ev[3]));
+    launch_huffman_build(b, maxS, s);
+    ctx->launches += 1;
+    mark(ctx, 8);
+    CU(cudaGetLastError());
+    CU(record(ctx, ctx->ev[4]));
+    launch_encode(b, maxS, s);
+    launch_pack_meta(b, s);
+    ctx->launches += 6;
+    mark(ctx, 9);
+    CU(cudaGetLastError());
+    CU(record(ctx, ctx->ev[5]));
+    CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
+                       cudaMemcpyDeviceToHost, s));
+    return WL_OK;
+  };
+  auto transform_select = [&]() -> wl_status {
+    CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, upBytes, cudaMemcpyHostToDevice, s));
+    CU(cudaMemsetAsync(ctx->state.p, 0, n * sizeof(CubeletState), s));
+    CU(cudaMemsetAsync(ctx->selHist.p, 0, (size_t)n * kSelectBins * 4, s));
+    CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)n * kMaxSymbols * 8, s));
+    if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
+    mark(ctx, 0);
+    TRY(launch_groups(ctx, gl, 0, gx));
+    mark(ctx, 1);
+    TRY(launch_groups(ctx, gl, gx, gy));
+    mark(ctx, 2);
+    TRY(launch_groups(ctx, gl, gy, gl.size()));
+    mark(ctx, 3);
+    CU(record(ctx, ctx->ev[1]));
+    if (coefOut) return WL_OK;
+    launch_select(b, b.coef, s);
+    ctx->launches += 9;
+    CU(cudaGetLastError());
+    mark(ctx, 4);
+    if (anyLog)
+      CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
+                         cudaMemcpyDeviceToHost, s));
+    else
+      TRY(quantize_to_end());
+    return WL_OK;
+  };
+
+  GraphEntry *ge = nullptr;
+  if (ctx->graphMode && !coefOut) {
+    // everything the captured launches depend on besides the upload block
+    std::vector<long long> key;
+    key.reserve(4 + (size_t)n * 18);
+    key.push_back(n);
+    key.push_back(onDevice | (ctx->profiling ? 2 : 0));
+    key.push_back((long long)tune_version());
+    for (int i = 0; i < n; i++) {
+      const Plan &pl = plans[i];
+      const wl_params &q = pl.p;
+      uint32_t fb;
+      memcpy(&fb, &q.threshold_fraction, 4);
+      const long long v[] = {pl.dtype | (hostIn[i] << 8), pl.X, pl.Y, pl.Z, pl.pitchY, pl.pitchZ,
+                             q.steps[0], q.steps[1], q.steps[2], q.wavelet, (long long)fb,
+                             q.bin_count, q.quant_alg, q.compress_zeros, q.lloyd_iters,
+                             q.exact_transform};
+      key.insert(key.end(), v, v + sizeof v / sizeof v[0]);
+    }
+    ge = graph_for(ctx, std::move(key));
+  }
+
+  // ---- transform ----
+  TRY(run_segment(ctx, ge, 0, transform_select));
   if (coefOut) {  // transform only: hand back the coefficients of cubelet 0
     const Plan &pl = plans[0];
     if ((size_t)pl.n > coefCap) return fail(ctx, WL_EINVAL, "coefficient buffer too small");
@@ -666,16 +901,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     return WL_OK;
   }
 
-  // ---- threshold ----
-  launch_select(b, b.coef, s);
-  ctx->launches += 9;
-  CU(cudaGetLastError());
-  mark(ctx, 4);
-
   // ---- log quantizer tables (host logf) ----
   if (anyLog) {
-    CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
-                       cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     const CubeletState *hs = H<CubeletState>(ctx->hState);
     float *tab = H<float>(ctx->hTab);
@@ -709,40 +936,10 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     if (bad.load() >= 0)
       return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)",
                   bad.load());
-    CU(cudaMemcpyAsync(ctx->qtable.p, tab, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(ctx->logHdr.p, lh, n * sizeof(int4), cudaMemcpyHostToDevice, s));
+    TRY(run_segment(ctx, ge, 1, quantize_to_end));
   }
-  CU(cudaEventRecord(ctx->ev[2], s));
-
-  // ---- quantize + count ----
-  launch_quant_params(b, s);
-  ctx->launches += 1;
-  if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 3; }
-  mark(ctx, 5);
-  launch_quantize(b, b.coef, maxTable, s);
-  mark(ctx, 6);
-  launch_runs(b, s);
-  ctx->launches += 2;
-  mark(ctx, 7);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(ctx->ev[3], s));
-
-  // ---- Huffman ----
-  launch_huffman_build(b, maxS, s);
-  ctx->launches += 1;
-  mark(ctx, 8);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(ctx->ev[4], s));
-  launch_encode(b, maxS, s);
-  launch_pack_meta(b, s);
-  ctx->launches += 6;
-  mark(ctx, 9);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(ctx->ev[5], s));
 
   // ---- results ----
-  CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
-                     cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   const CubeletState *hs = H<CubeletState>(ctx->hState);
   long long totalWords = 0;
@@ -841,6 +1038,38 @@ void launch_dequant(const int *bins, const float *table, float *out, long long n
 
 namespace {
 
+// Column-tile inverse passes (the forward layouts in reverse): z in place on
+// z-x-y (only with z levels), y z-x-y -> z-y-x into c2, x z-y-x -> x-y-z with
+// the crop to the original size into dst.  Returns the pass count.
+int inverse_passes_cols(int Xp, int Yp, int Zp, const int orig[3], const int steps[3],
+                        int wavelet, float *c1, float *c2, void *dst, PassDesc *out) {
+  const int big = 0x7fffffff;
+  const int X = orig[0], Y = orig[1], Z = orig[2];
+  auto mk = [&]() { PassDesc d; memset(&d, 0, sizeof d); d.cropL = d.cropB = d.cropA = big;
+                    d.clampL = d.clampB = d.clampA = big; d.wavelet = wavelet; d.exact = 0;
+                    d.inSC = 1; return d; };
+  int np = 0;
+  if (steps[2] > 0) {  // rows (a = y, b = x)
+    PassDesc a = mk();
+    a.in = c1; a.inSA = (long long)Zp * Xp; a.inSB = Zp; a.inSC = 1;
+    a.out = c1; a.outSA = (long long)Zp * Xp; a.outSB = Zp; a.outSC = 1;
+    a.L = Zp; a.B = Xp; a.rows = Xp * Yp; a.steps = steps[2];
+    out[np++] = a;
+  }
+  PassDesc e = mk();  // rows (a = x, b = z)
+  e.in = c1; e.inSA = Zp; e.inSB = 1; e.inSC = (long long)Zp * Xp;
+  e.out = c2; e.outSA = (long long)Zp * Yp; e.outSB = 1; e.outSC = Zp;
+  e.L = Yp; e.B = Zp; e.rows = Zp * Xp; e.steps = steps[1];
+  out[np++] = e;
+  PassDesc x = mk();  // rows (a = y, b = z)
+  x.in = c2; x.inSA = Zp; x.inSB = 1; x.inSC = (long long)Zp * Yp;
+  x.out = dst; x.outSA = X; x.outSB = (long long)X * Y; x.outSC = 1;
+  x.cropL = X; x.cropA = Y; x.cropB = Z;
+  x.L = Xp; x.B = Zp; x.rows = Yp * Zp; x.steps = steps[0];
+  out[np++] = x;
+  return np;
+}
+
 // Inverse transform of the coefficients already in ctx->coef (stored order)
 // into out (original size, outType), then synchronize.
 wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int wavelet,
@@ -866,62 +1095,45 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
   wl_params wp;
   memset(&wp, 0, sizeof wp);
   wp.wavelet = wavelet;
+  // descriptors of up to three passes, uploaded in one copy
+  std::vector<GroupLaunch> gl;
   if (use_cols(Xp, Yp, Zp, identity, wp)) {
-    // column-tile layouts, the forward passes in reverse
-    if (steps[2] > 0) {  // z pass in place on z-x-y, rows (a = y, b = x)
+    PassDesc d[3];
+    const int np = inverse_passes_cols(Xp, Yp, Zp, original_size, steps, wavelet, c1, c2, dst, d);
+    for (int i = 0; i < np; i++)
+      TRY(stage_group(ctx, {d[i]}, hoff, kTuneInvX - (np - 1 - i), WL_F32,
+                      i == np - 1 ? outType : WL_F32, true, true, false, gl));
+  } else {
+    if (!identity) {
+      // inverse z pass: z-x-y -> y-z-x
       PassDesc a = mk();
-      a.in = c1; a.inSA = (long long)Zp * Xp; a.inSB = Zp; a.inSC = 1;
-      a.out = c1; a.outSA = (long long)Zp * Xp; a.outSB = Zp; a.outSC = 1;
-      a.L = Zp; a.B = Xp; a.rows = Xp * Yp; a.steps = steps[2];
-      a.T = dwt_cols_tile_rows(a.L); a.tiles = (a.rows + a.T - 1) / a.T;
-      TRY(run_group(ctx, {a}, hoff, WL_F32, WL_F32, true, true));
+      a.in = c1; a.inSA = Zp; a.inSB = (long long)Xp * Zp;
+      a.L = Zp; a.B = Yp; a.rows = Xp * Yp;
+      a.out = c2; a.outSA = (long long)Yp * Zp; a.outSB = 1; a.outSC = Yp;
+      a.steps = steps[2];
+      a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
+      TRY(stage_group(ctx, {a}, hoff, kTuneInvZ, WL_F32, WL_F32, true, false, false, gl));
+      // inverse y pass: y-z-x -> x-y-z
+      PassDesc bq = mk();
+      bq.in = c2; bq.inSA = Yp; bq.inSB = (long long)Zp * Yp;
+      bq.L = Yp; bq.B = Xp; bq.rows = Zp * Xp;
+      bq.out = c1; bq.outSA = (long long)Xp * Yp; bq.outSB = 1; bq.outSC = Xp;
+      bq.steps = steps[1];
+      bq.T = dwt_tile_rows(bq.L, exactCdf); bq.tiles = (bq.rows + bq.T - 1) / bq.T;
+      TRY(stage_group(ctx, {bq}, hoff, kTuneInvY, WL_F32, WL_F32, true, false, false, gl));
     }
-    // y pass z-x-y -> z-y-x, rows (a = x, b = z)
-    PassDesc e = mk();
-    e.in = c1; e.inSA = Zp; e.inSB = 1; e.inSC = (long long)Zp * Xp;
-    e.out = c2; e.outSA = (long long)Zp * Yp; e.outSB = 1; e.outSC = Zp;
-    e.L = Yp; e.B = Zp; e.rows = Zp * Xp; e.steps = steps[1];
-    e.T = dwt_cols_tile_rows(e.L); e.tiles = (e.rows + e.T - 1) / e.T;
-    TRY(run_group(ctx, {e}, hoff, WL_F32, WL_F32, true, true));
-    // x pass z-y-x -> x-y-z + crop + dtype, rows (a = y, b = z)
+    // inverse x pass + crop + dtype
     PassDesc x = mk();
-    x.in = c2; x.inSA = Zp; x.inSB = 1; x.inSC = (long long)Zp * Yp;
-    x.out = dst; x.outSA = X; x.outSB = (long long)X * Y; x.outSC = 1;
-    x.cropL = X; x.cropA = Y; x.cropB = Z;
-    x.L = Xp; x.B = Zp; x.rows = Yp * Zp; x.steps = steps[0];
-    x.T = dwt_cols_tile_rows(x.L); x.tiles = (x.rows + x.T - 1) / x.T;
-    TRY(run_group(ctx, {x}, hoff, WL_F32, outType, true, true));
-    if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
-    CU(cudaStreamSynchronize(s));
-    return WL_OK;
+    x.in = c1; x.inSA = (long long)Yp * Xp; x.inSB = Xp;
+    x.L = Xp; x.B = Yp; x.rows = Yp * Zp;
+    x.out = dst; x.outSA = (long long)X * Y; x.outSB = X; x.outSC = 1;
+    x.cropL = X; x.cropB = Y; x.cropA = Z;
+    x.steps = identity ? 0 : steps[0];
+    x.T = dwt_tile_rows(x.L, exactCdf); x.tiles = (x.rows + x.T - 1) / x.T;
+    TRY(stage_group(ctx, {x}, hoff, kTuneInvX, WL_F32, outType, true, false, false, gl));
   }
-  if (!identity) {
-    // inverse z pass: z-x-y -> y-z-x
-    PassDesc a = mk();
-    a.in = c1; a.inSA = Zp; a.inSB = (long long)Xp * Zp;
-    a.L = Zp; a.B = Yp; a.rows = Xp * Yp;
-    a.out = c2; a.outSA = (long long)Yp * Zp; a.outSB = 1; a.outSC = Yp;
-    a.steps = steps[2];
-    a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
-    TRY(run_group(ctx, {a}, hoff, WL_F32, WL_F32, true));
-    // inverse y pass: y-z-x -> x-y-z
-    PassDesc bq = mk();
-    bq.in = c2; bq.inSA = Yp; bq.inSB = (long long)Zp * Yp;
-    bq.L = Yp; bq.B = Xp; bq.rows = Zp * Xp;
-    bq.out = c1; bq.outSA = (long long)Xp * Yp; bq.outSB = 1; bq.outSC = Xp;
-    bq.steps = steps[1];
-    bq.T = dwt_tile_rows(bq.L, exactCdf); bq.tiles = (bq.rows + bq.T - 1) / bq.T;
-    TRY(run_group(ctx, {bq}, hoff, WL_F32, WL_F32, true));
-  }
-  // inverse x pass + crop + dtype
-  PassDesc x = mk();
-  x.in = c1; x.inSA = (long long)Yp * Xp; x.inSB = Xp;
-  x.L = Xp; x.B = Yp; x.rows = Yp * Zp;
-  x.out = dst; x.outSA = (long long)X * Y; x.outSB = X; x.outSC = 1;
-  x.cropL = X; x.cropB = Y; x.cropA = Z;
-  x.steps = identity ? 0 : steps[0];
-  x.T = dwt_tile_rows(x.L, exactCdf); x.tiles = (x.rows + x.T - 1) / x.T;
-  TRY(run_group(ctx, {x}, hoff, WL_F32, outType, true));
+  CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, hoff, cudaMemcpyHostToDevice, s));
+  TRY(launch_groups(ctx, gl, 0, gl.size()));
   if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   return WL_OK;
@@ -993,6 +1205,134 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
   CU(cudaGetLastError());
   return inverse_impl(ctx, r->size, r->steps, r->wavelet, r->original_size, outType, out,
                       outOnDevice);
+}
+
+// ---- tile autotuner -------------------------------------------------------------
+// For every size class of the column-tile transform -- pass (forward x / y / z,
+// inverse z / y / x), element type of its global side, row-length class 2^k --
+// time each tile height that fits (32, 64, 128 rows) on a synthetic batch of
+// about 2^24 elements on the device: blocks with the tuned axis 2^k long and
+// the other two max(32, min(2^k, 2^((24-k)/2))) (cubes from 32 to 256, two
+// 512 x 128 x 128 blocks at 512), CDF 9/7 with up to 3 levels on the tuned
+// axis.  The fastest height goes
+// into the process-wide tile table.  The forward x pass of 8- and 16-bit data
+// is tuned twice, reading from device memory and from page-locked host memory.
+wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
+  CU(cudaSetDevice(ctx->device));
+  const long long kElems = 1LL << 24;
+  TRY(ensure(ctx, ctx->coef, (kElems + 4096) * 4));
+  TRY(ensure(ctx, ctx->coef2, (kElems + 4096) * 4));
+  TRY(ensure(ctx, ctx->input, (kElems + 4096) * 4));
+  TRY(ensure_host(ctx, ctx->hIn, (kElems + 4096) * 2));
+  cudaStream_t s = ctx->stream;
+  // finite, ordinary values in every element type
+  CU(cudaMemsetAsync(ctx->input.p, 0x3c, (kElems + 4096) * 4, s));
+  CU(cudaMemsetAsync(ctx->coef.p, 0x3c, (kElems + 4096) * 4, s));
+  CU(cudaMemsetAsync(ctx->coef2.p, 0x3c, (kElems + 4096) * 4, s));
+  memset(ctx->hIn.p, 0x3c, (kElems + 4096) * 2);
+  void *hostDev = nullptr;
+  CU(cudaHostGetDevicePointer(&hostDev, ctx->hIn.p, 0));
+  std::vector<cudaEvent_t> ev(reps + 1);
+  for (cudaEvent_t &e : ev) CU(cudaEventCreate(&e));
+  struct EvGuard {
+    std::vector<cudaEvent_t> &v;
+    ~EvGuard() { for (cudaEvent_t e : v) if (e) cudaEventDestroy(e); }
+  } guard{ev};
+  float *c1 = P<float>(ctx->coef), *c2 = P<float>(ctx->coef2);
+
+  for (int lg = 1; lg <= 9 && (1 << lg) <= maxLen; lg++) {
+    const int L = 1 << lg;
+    const int other = std::max(32, std::min(L, 1 << ((24 - lg) / 2)));
+    const long long per = (long long)L * other * other;
+    const int count = (int)std::max(1LL, kElems / per);
+    const int steps = std::min(lg, 3);
+    for (int kind = 0; kind < kTuneKinds; kind++) {
+      // (element type, 16-byte host loads) of this pass's global side
+      std::vector<std::pair<int, bool>> types;
+      if (kind == kTuneFwdX)
+        types = {{WL_U8, false}, {WL_U16, false}, {WL_I32, false}, {WL_F32, false},
+                 {WL_U8, true}, {WL_U16, true}};
+      else if (kind == kTuneInvX)
+        types = {{WL_U8, false}, {WL_U16, false}, {WL_I32, false}, {WL_F32, false}};
+      else
+        types = {{WL_F32, false}};
+      const int axis = kind <= kTuneFwdZ ? kind : kTuneInvX - kind;  // 0 x, 1 y, 2 z
+      for (const auto &ty : types) {
+        std::vector<PassDesc> g;
+        for (int c = 0; c < count; c++) {
+          Plan pl;
+          memset(&pl, 0, sizeof pl);
+          int dims[3] = {other, other, other};
+          dims[axis] = L;
+          pl.X = pl.Xp = dims[0]; pl.Y = pl.Yp = dims[1]; pl.Z = pl.Zp = dims[2];
+          pl.sx = pl.sy = pl.sz = 0;
+          (axis == 0 ? pl.sx : axis == 1 ? pl.sy : pl.sz) = steps;
+          // the other axes get one level so that every pass exists
+          if (axis != 0) pl.sx = 1;
+          if (axis != 1) pl.sy = 1;
+          if (axis != 2) pl.sz = 1;
+          pl.dtype = ty.first;
+          pl.p.wavelet = WL_CDF97;
+          pl.pitchY = pl.X;
+          pl.pitchZ = (long long)pl.X * pl.Y;
+          pl.n = per;
+          pl.coefOff = (long long)c * per;
+          if (kind <= kTuneFwdZ) {
+            const void *in = ty.second ? hostDev : ctx->input.p;
+            PassGroups xs, ys, zs;
+            forward_passes_cols(pl, in, ty.second, c1, c2, xs, ys, zs);
+            PassGroups &ph = kind == kTuneFwdX ? xs : kind == kTuneFwdY ? ys : zs;
+            for (auto &kv : ph) g.insert(g.end(), kv.second.begin(), kv.second.end());
+          } else {
+            const int orig[3] = {pl.X, pl.Y, pl.Z};
+            const int st[3] = {pl.sx, pl.sy, pl.sz};
+            PassDesc d[3];
+            // every cubelet writes the same output block: timing only
+            const int np = inverse_passes_cols(pl.Xp, pl.Yp, pl.Zp, orig, st, WL_CDF97,
+                                               c1 + pl.coefOff, c2 + pl.coefOff,
+                                               kind == kTuneInvX ? ctx->input.p : nullptr, d);
+            g.push_back(d[np - 1 - (kTuneInvX - kind)]);
+          }
+        }
+        if (g.empty()) continue;
+        const size_t need = g.size() * (sizeof(PassDesc) + sizeof(int)) + 4096;
+        TRY(ensure(ctx, ctx->passes, need));
+        TRY(ensure_host(ctx, ctx->hPasses, need));
+        const bool inv = kind >= kTuneInvZ;
+        const int inType = inv ? WL_F32 : ty.first, outType = kind == kTuneInvX ? ty.first : WL_F32;
+        float us[3] = {0, 0, 0};
+        int best = 0;
+        float bestUs = 0;
+        const int cand[3] = {32, 64, 128};
+        for (int ci = 0; ci < 3; ci++) {
+          if (!dwt_cols_rows_fit(L, cand[ci])) continue;
+          std::vector<GroupLaunch> gl;
+          size_t hoff = 0;
+          TRY(stage_group(ctx, g, hoff, kind, inType, outType, inv, true, ty.second, gl,
+                          cand[ci]));
+          CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, hoff, cudaMemcpyHostToDevice, s));
+          TRY(launch_groups(ctx, gl, 0, gl.size()));  // warm-up
+          for (int r = 0; r < reps; r++) {
+            CU(cudaEventRecord(ev[r], s));
+            TRY(launch_groups(ctx, gl, 0, gl.size()));
+          }
+          CU(cudaEventRecord(ev[reps], s));
+          CU(cudaEventSynchronize(ev[reps]));
+          std::vector<float> t(reps);
+          for (int r = 0; r < reps; r++) CU(cudaEventElapsedTime(&t[r], ev[r], ev[r + 1]));
+          std::sort(t.begin(), t.end());
+          us[ci] = t[reps / 2] * 1000.f;
+          if (!best || us[ci] < bestUs) {
+            best = cand[ci];
+            bestUs = us[ci];
+          }
+        }
+        set_tuned_cols_rows(kind, tune_type_index(ty.first, ty.second), lg, best, us);
+      }
+    }
+  }
+  CU(cudaStreamSynchronize(s));
+  return WL_OK;
 }
 
 wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
@@ -1078,14 +1418,15 @@ void wl_destroy(wl_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   DevBuf *dbs[] = {&ctx->input, &ctx->coef, &ctx->coef2, &ctx->bins, &ctx->tokCount,
-                   &ctx->state, &ctx->cub,
+                   &ctx->state,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
-                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkPrefix, &ctx->chunkCub, &ctx->groupCub,
+                   &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkCub, &ctx->groupCub,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
                    &ctx->meta};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
-  HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses, &ctx->hCub,
+  for (GraphEntry &g : ctx->graphs) drop_graph(g);
+  HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses,
                     &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals,
                     &ctx->hFlags};
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
@@ -1252,6 +1593,33 @@ wl_status wl_inverse_transform(wl_ctx *ctx, const float *coeffs, const int store
   CU(cudaMemcpyAsync(ctx->coef.p, coeffs, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
   return inverse_impl(ctx, stored, steps, wavelet, orig, outType, out, 0);
 }
+
+wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps) {
+  if (!ctx) return WL_EINVAL;
+  if (max_len <= 0 || max_len > kColsMaxL) max_len = kColsMaxL;
+  if (reps <= 0) reps = 5;
+  if (reps > 64) reps = 64;
+  return autotune_impl(ctx, max_len, reps);
+}
+
+wl_status wl_set_graph_mode(wl_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return WL_EINVAL;
+  ctx->graphMode = mode;
+  if (!mode) {
+    for (GraphEntry &g : ctx->graphs) drop_graph(g);
+    ctx->graphs.clear();
+    ctx->lastKey.clear();
+  }
+  return WL_OK;
+}
+
+wl_status wl_graph_stats(const wl_ctx *ctx, long long out[4]) {
+  if (!ctx || !out) return WL_EINVAL;
+  for (int i = 0; i < 4; i++) out[i] = ctx->graphStats[i];
+  return WL_OK;
+}
+
+const char *wl_graph_error(const wl_ctx *ctx) { return ctx ? ctx->graphErr.c_str() : ""; }
 
 wl_status wl_last_timings(const wl_ctx *ctx, float out[6]) {
   if (!ctx || !out) return WL_EINVAL;

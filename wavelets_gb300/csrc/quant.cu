@@ -377,19 +377,25 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 // in order: a token for every value that is not the zero bin, preceded by the
 // tokens of the zero-bin run before it when that run starts inside the chunk.
 // Runs touching a chunk edge are left to runs_kernel (counts) and the encoder
-// (tokens).  A CTA codes kQuantGroup consecutive chunks of one cubelet.
+// (tokens).  A CTA codes kQuantGroup consecutive chunks of one cubelet; warp
+// w owns elements [512 w, 512 w + 512) of each chunk, and everything but two
+// CTA barriers per chunk is warp-local.
 //
 // Phase 1 (every element): -thr < x < thr is the zero bin for all three
 // quantizers (uniform and log test |x| <= thr first; the codebook has the
 // boundaries -thr and thr around its zero bin and none in between), so an
-// element costs two compares.  The others are candidates, compacted per warp
-// (warp w owns elements [512 w, 512 w + 512); in word j lane l holds element
+// element costs two compares.  The others are candidates, compacted into the
+// warp's region of shared memory (in word j lane l holds element
 // 512 w + 32 j + l, so loads are coalesced).
-// Phase 2 (per candidate): the exact bin; candidates that are not the zero
-// bin become the chunk's value list (position, bin) in position order.
-// Phase 3 (per value): the gap to the previous value is the zero run in
-// between; each thread takes a contiguous slice of the list, counts its
-// tokens, and after a block scan writes them.
+// Phase 2 (per candidate, 32 at a time): the exact bin; candidates that are
+// not the zero bin become the warp's value list (position, bin), written in
+// place over the candidates, in position order.
+// Phase 3 (per value, 32 at a time): the gap to the previous value -- the
+// lane before, or the last value of the nearest earlier warp -- is the zero
+// run in between; the token counts give each warp its place in the chunk
+// (after a CTA barrier) and each lane its place in the warp (a warp scan),
+// and every lane writes its run tokens and value token straight to the
+// chunk's token slot.
 // greedy split of a zero-bin run into dup tokens and single zero-bin tokens
 // (closed form of run_split; the same counts as run_token_count)
 __device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups) {
@@ -409,16 +415,17 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   constexpr int kWords = kChunk / kThreads;  // 16 words of 32 elements per warp
   constexpr int kSpan = 32 * kWords;         // elements per warp
   constexpr int kWarps = kThreads / 32;
+  constexpr unsigned kAll = 0xffffffffu;
   __shared__ unsigned hist[kMaxSymbols + 1];
   extern __shared__ float tab[];  // quantizer table (Lloyd / log), sized by the launch
   __shared__ __align__(16) uint16_t sLut[kLutStride];
-  // candidate values by warp region, then the packed value list
+  // by warp region: candidate values, overwritten in place by the value list
   __shared__ __align__(16) float sX[kChunk];
-  // candidate positions by warp region, then the chunk's tokens
-  __shared__ uint16_t sPT[kChunk];
-  __shared__ unsigned wVal[kWarps], wTok[kWarps];
-  unsigned *sList = reinterpret_cast<unsigned *>(sX);  // (position << 13) | bin
-  uint16_t *sTok = sPT;
+  __shared__ uint16_t sPos[kChunk];  // candidate positions
+  // per-warp summaries, two sets used by alternate chunks
+  __shared__ int wLast[2][kWarps], wFirst[2][kWarps];
+  __shared__ unsigned wTok[2][kWarps];
+  unsigned *sVal = reinterpret_cast<unsigned *>(sX);  // (position << 13) | bin
   const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
@@ -444,10 +451,12 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
   __syncthreads();
 
   for (int k = 0; k < nc; k++) {
+    const int par = k & 1;
     const long long chunk = cd.chunkBase + c0 + k;
     const long long start = (long long)(c0 + k) * kChunk;
     const int len = (int)min((long long)kChunk, cd.n - start);
     const float *src = coef + cd.coefOff + start;
+    uint16_t *dst = b.tok + cd.coefOff + start;
 
     // ---- phase 1: candidates into the warp's region
     int nCand = 0;  // warp-uniform
@@ -462,116 +471,144 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
       for (int j = 0; j < kWords; j++) {
         const int pos = base + 32 * j + lane;
         const bool cand = pos < len && !(x[j] > zlo && x[j] < zhi);
-        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        const unsigned m = __ballot_sync(kAll, cand);
         if (cand) {
           const int l = base + nCand + __popc(m & ltMask);
           sX[l] = x[j];
-          sPT[l] = (uint16_t)pos;
+          sPos[l] = (uint16_t)pos;
         }
         nCand += __popc(m);
       }
     }
     __syncwarp();
-    // ---- phase 2: exact bins of the warp's candidates
-    unsigned e[kWords];
-    unsigned isv = 0;  // bit r: candidate lane + 32 r is a value
-    int nVal = 0;      // warp-uniform
-#pragma unroll
-    for (int r = 0; r < kWords; r++) {
-      const int l = lane + 32 * r;
+
+    // ---- phase 2: exact bins; values replace the candidates in place (a
+    // write index never passes the read index of its round, and every lane
+    // of the round has read before the ballot)
+    int nVal = 0;  // warp-uniform
+    for (int r = 0; 32 * r < nCand; r++) {
+      const int l = 32 * r + lane;
       const bool has = l < nCand;
-      const int bin = has ? quant_value(sX[base + l], q, tab, sLut) : 0;
-      const unsigned pos = has ? sPT[base + l] : 0u;
+      int bin = 0;
+      unsigned pos = 0;
+      if (has) {
+        bin = quant_value(sX[base + l], q, tab, sLut);
+        pos = sPos[base + l];
+      }
       const bool v = has && bin != dupV;
-      e[r] = (pos << 13) | (unsigned)bin;
-      isv |= (v ? 1u : 0u) << r;
-      nVal += __popc(__ballot_sync(0xffffffffu, v));
+      const unsigned m = __ballot_sync(kAll, v);
+      if (v) sVal[base + nVal + __popc(m & ltMask)] = (pos << 13) | (unsigned)bin;
+      nVal += __popc(m);
     }
-    if (lane == 0) wVal[w] = (unsigned)nVal;
-    __syncthreads();  // every warp has read its candidates
-    unsigned total = 0, vo = 0;
-    for (int v = 0; v < kWarps; v++) {
-      if (v < w) vo += wVal[v];
-      total += wVal[v];
-    }
-#pragma unroll
-    for (int r = 0; r < kWords; r++) {
-      const bool v = (isv >> r) & 1u;
-      const unsigned m = __ballot_sync(0xffffffffu, v);
-      if (v) sList[vo + __popc(m & ltMask)] = e[r];
-      vo += __popc(m);
+    __syncwarp();
+    if (lane == 0) {
+      wFirst[par][w] = nVal ? (int)(sVal[base] >> 13) : -1;
+      wLast[par][w] = nVal ? (int)(sVal[base + nVal - 1] >> 13) : -1;
     }
     __syncthreads();
 
-    // ---- phase 3: tokens of a contiguous slice of the values
-    const unsigned per = (total + kThreads - 1) / kThreads;
-    const unsigned i0 = min(threadIdx.x * per, total), i1 = min(i0 + per, total);
-    const int prev0 = i0 > 0 ? (int)(sList[i0 - 1] >> 13) : -1;
+    // ---- phase 3a: token counts and the histogram
+    // the value before this warp's first: positions grow with the warp index
+    int prevW = -1;
+    for (int v = 0; v < w; v++) prevW = max(prevW, wLast[par][v]);
     int myTok = 0, singles = 0, dups = 0;
     {
-      int prev = prev0;
-      for (unsigned i = i0; i < i1; i++) {
-        const int p = (int)(sList[i] >> 13);
-        const int gap = prev >= 0 ? p - prev - 1 : 0;
-        if (gap > 0) {
-          int sg, dp;
-          run_split_closed(gap, sg, dp);
-          myTok += sg + dp;
-          singles += sg;
-          dups += dp;
+      int carry = prevW;
+      for (int r = 0; 32 * r < nVal; r++) {
+        const int i = 32 * r + lane;
+        const bool hasV = i < nVal;
+        const unsigned ev = hasV ? sVal[base + i] : 0u;
+        const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
+        const int pl = __shfl_up_sync(kAll, p, 1);
+        const int prev = lane ? pl : carry;
+        const unsigned act = __ballot_sync(kAll, hasV);
+        if (hasV) {
+          const int gap = prev >= 0 ? p - prev - 1 : 0;
+          if (gap > 0) {
+            int sg, dp;
+            run_split_closed(gap, sg, dp);
+            myTok += sg + dp;
+            singles += sg;
+            dups += dp;
+          }
+          myTok += 1;
+          const unsigned peers = __match_any_sync(act, bin);
+          if (lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
         }
-        myTok += 1;
-        prev = p;
+        carry = __shfl_sync(kAll, p, 31);
       }
-    }
-    // block exclusive scan of the token counts
-    int inc = myTok;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, inc, d);
-      if (lane >= d) inc += t;
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-      singles += __shfl_xor_sync(0xffffffffu, singles, d);
-      dups += __shfl_xor_sync(0xffffffffu, dups, d);
+      myTok += __shfl_xor_sync(kAll, myTok, d);
+      singles += __shfl_xor_sync(kAll, singles, d);
+      dups += __shfl_xor_sync(kAll, dups, d);
     }
-    if (lane == 31) wTok[w] = (unsigned)inc;
     if (lane == 0) {
+      wTok[par][w] = (unsigned)myTok;
       if (singles) atomicAdd(&hist[dupV], (unsigned)singles);
       if (dups) atomicAdd(&hist[B], (unsigned)dups);
     }
     __syncthreads();
-    unsigned o = (unsigned)(inc - myTok), nTok = 0;
+
+    // ---- phase 3b: tokens, straight to the chunk's slot
+    unsigned o = 0, nTok = 0;
     for (int v = 0; v < kWarps; v++) {
-      if (v < w) o += wTok[v];
-      nTok += wTok[v];
+      if (v < w) o += wTok[par][v];
+      nTok += wTok[par][v];
     }
     {
-      int prev = prev0;
-      for (unsigned i = i0; i < i1; i++) {
-        const unsigned ev = sList[i];
+      int carry = prevW;
+      for (int r = 0; 32 * r < nVal; r++) {
+        const int i = 32 * r + lane;
+        const bool hasV = i < nVal;
+        const unsigned ev = hasV ? sVal[base + i] : 0u;
         const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
-        if (prev >= 0 && p - prev > 1)
-          run_tokens(prev + 1, p, prev + 1, p, B, dupV, [&](uint16_t t) { sTok[o++] = t; });
-        sTok[o++] = make_token(bin, 0);
-        atomicAdd(&hist[bin], 1u);
-        prev = p;
+        const int pl = __shfl_up_sync(kAll, p, 1);
+        const int prev = lane ? pl : carry;
+        int cnt = 0;
+        if (hasV) {
+          const int gap = prev >= 0 ? p - prev - 1 : 0;
+          if (gap > 0) {
+            int sg, dp;
+            run_split_closed(gap, sg, dp);
+            cnt = sg + dp;
+          }
+          cnt += 1;
+        }
+        int inc = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int t = __shfl_up_sync(kAll, inc, d);
+          if (lane >= d) inc += t;
+        }
+        if (hasV) {
+          unsigned t = o + (unsigned)(inc - cnt);
+          if (prev >= 0 && p - prev > 1)
+            run_tokens(prev + 1, p, prev + 1, p, B, dupV, [&](uint16_t tk) { dst[t++] = tk; });
+          dst[t] = make_token(bin, 0);
+        }
+        o += (unsigned)__shfl_sync(kAll, inc, 31);
+        carry = __shfl_sync(kAll, p, 31);
       }
     }
-    __syncthreads();
-    uint16_t *dst = b.tok + cd.coefOff + start;
-    for (unsigned i = threadIdx.x; i < nTok; i += kThreads) dst[i] = sTok[i];
     if (threadIdx.x == 0) {
       b.chunkTok[chunk] = (int)nTok;
       if (dupV >= 0) {
-        const int lead = total ? (int)(sList[0] >> 13) : len;
-        const int trail = total ? len - 1 - (int)(sList[total - 1] >> 13) : len;
-        b.chunkRun[chunk] = make_int4(lead, trail, total ? 0 : 1, len);
+        int first = -1, last = -1;
+        for (int v = 0; v < kWarps; v++) {
+          if (first < 0) first = wFirst[par][v];
+          last = max(last, wLast[par][v]);
+        }
+        const bool any = last >= 0;
+        b.chunkRun[chunk] = make_int4(any ? first : len, any ? len - 1 - last : len, any ? 0 : 1, len);
       }
     }
-    __syncthreads();  // the buffers are reused by the next chunk
+    // no barrier: the next chunk writes the other summary set, and a warp
+    // reaches this chunk's set again only after every warp has passed the
+    // next chunk's two barriers
   }
+  __syncthreads();
   unsigned long long *gh = b.hist + (size_t)ci * kMaxSymbols;
   for (int i = threadIdx.x; i <= B; i += kThreads)
     if (hist[i]) atomicAdd(&gh[i], (unsigned long long)hist[i]);

@@ -210,8 +210,17 @@ constexpr int kColsMaxL = 512;
 void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int tiles,
                      int smem, int rows, int inType, int outType, bool inverse, bool vecLoad,
                      cudaStream_t s);
-int dwt_cols_tile_rows(int L);
-int dwt_cols_smem_bytes(int L);
+int dwt_cols_tile_rows(int L);               // default tile height for rows of L
+int dwt_cols_smem_bytes(int L, int rows);
+bool dwt_cols_rows_fit(int L, int rows);      // rows in {32, 64, 128} and smem fits
+
+// ---- column-tile heights per size class (tune.cpp) ----
+enum TuneKind { kTuneFwdX, kTuneFwdY, kTuneFwdZ, kTuneInvZ, kTuneInvY, kTuneInvX, kTuneKinds };
+int tune_type_index(int dtype, bool vec);
+// tile height for rows of up to L elements: the tuned entry, else the default
+int tuned_cols_rows(int kind, int typeIdx, int L);
+void set_tuned_cols_rows(int kind, int typeIdx, int cls, int rows, const float us[3]);
+unsigned tune_version();  // changes whenever the table does
 
 // launchers (select.cu)
 void launch_select(DevBatch &b, const float *coef, cudaStream_t s);

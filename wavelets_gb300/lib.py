@@ -132,6 +132,14 @@ EXPORTS = {
                                      ctypes.POINTER(WlResult), ctypes.POINTER(WlRequestInfo)]),
     "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_serve_destroy": (None, [ctypes.c_void_p]),
+    "wl_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "wl_tune_export": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_size_t)]),
+    "wl_tune_import": (ctypes.c_int, [ctypes.c_char_p]),
+    "wl_tune_reset": (None, []),
+    "wl_set_graph_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "wl_graph_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "wl_graph_error": (ctypes.c_char_p, [ctypes.c_void_p]),
 }
 
 _lib = None
@@ -520,6 +528,67 @@ class Context:
 
     def sync(self):
         self._check(self.lib.wl_sync(self.h))
+
+    def autotune(self, max_len: int = 0, reps: int = 0) -> str:
+        """Time every tile height of every column-transform size class on
+        this context's device and keep the fastest (process-wide); returns
+        the table as text (see tune_table)."""
+        self._check(self.lib.wl_autotune(self.h, int(max_len), int(reps)))
+        return tune_table()
+
+    def set_graph_mode(self, mode: int):
+        """1: capture a batch geometry seen twice in a row as a CUDA graph
+        and replay it; 0: always launch directly."""
+        self._check(self.lib.wl_set_graph_mode(self.h, int(mode)))
+
+    def graph_stats(self):
+        t = (ctypes.c_longlong * 4)()
+        self._check(self.lib.wl_graph_stats(self.h, t))
+        out = dict(zip(("direct", "captures", "replays", "failed"), [int(x) for x in t]))
+        err = self.lib.wl_graph_error(self.h)
+        if err:
+            out["error"] = err.decode()
+        return out
+
+
+TUNE_PASSES = ("fwd_x", "fwd_y", "fwd_z", "inv_z", "inv_y", "inv_x")
+
+
+def tune_table() -> str:
+    """The process-wide tile table: one line per tuned size class,
+    "pass type class rows us32 us64 us128"."""
+    lib = load()
+    n = ctypes.c_size_t()
+    st = lib.wl_tune_export(None, 0, ctypes.byref(n))
+    if st:
+        raise WlError(st, "tune export")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    st = lib.wl_tune_export(buf, n.value + 1, ctypes.byref(n))
+    if st:
+        raise WlError(st, "tune export")
+    return buf.value.decode()
+
+
+def tune_load(text: str):
+    """Install tile-table lines (as tune_table returns them)."""
+    st = load().wl_tune_import(text.encode())
+    if st:
+        raise WlError(st, "malformed tile table")
+
+
+def tune_reset():
+    load().wl_tune_reset()
+
+
+def tune_rows(text: str):
+    """Parse a tile table: {(pass, type, class): (rows, (us32, us64, us128))}."""
+    out = {}
+    for ln in text.splitlines():
+        f = ln.split()
+        if len(f) >= 4:
+            out[(int(f[0]), int(f[1]), int(f[2]))] = (
+                int(f[3]), tuple(float(x) for x in f[4:7]) if len(f) >= 7 else ())
+    return out
 
 
 def encode_cube(c: Compressed, footer: bool = False) -> bytes:
