@@ -95,6 +95,8 @@ typedef struct {
 } wl_result;
 
 void wl_result_free(wl_result *r);
+/* wl_result_free on each of r[0..n). */
+void wl_results_free(wl_result *r, int n);
 
 typedef struct wl_ctx wl_ctx;
 
@@ -170,6 +172,13 @@ void wl_free(void *p);
  * Huffman build, encode, total device time. */
 wl_status wl_last_timings(const wl_ctx *ctx, float out[6]);
 
+/* Page-locked host inputs: mode 0 (default) reads them in place from the
+ * first transform pass over the host link (fastest for one call at a time);
+ * mode 1 copies them into device memory with the copy engine first, leaving
+ * the SMs free for work of other contexts meanwhile (lanes whose batches
+ * overlap).  Results are identical. */
+wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode);
+
 /* Synchronize the context's stream. */
 wl_status wl_sync(wl_ctx *ctx);
 
@@ -189,6 +198,10 @@ typedef struct {
   int lanes;                /* concurrent batches on the device (default 2) */
   size_t memory_budget;     /* device working bytes admitted at once (default 16 GiB) */
   int max_batch;            /* requests per batch (default 1024) */
+  int stage_host_inputs;    /* 1 (default): lanes copy page-locked host inputs
+                               with the copy engine (wl_set_host_input_mode 1),
+                               so one lane's transfer overlaps another's
+                               compute; 0: lanes read them in place */
 } wl_serve_config;
 
 typedef struct {
@@ -215,6 +228,17 @@ void wl_serve_config_default(wl_serve_config *cfg);
 wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out);
 /* Queue a request; *ticket identifies it for wl_serve_wait. */
 wl_status wl_serve_submit(wl_server *srv, const wl_request *req, unsigned long long *ticket);
+/* Queue n requests back to back (nothing else between them in the queue),
+ * so that a free lane can take them as one batch; tickets[i] for reqs[i].
+ * Either all are queued or none (a request that fails validation queues
+ * nothing). */
+wl_status wl_serve_submit_batch(wl_server *srv, const wl_request *reqs, int n,
+                                unsigned long long *tickets);
+/* wl_serve_wait on each of tickets[0..n) with no time limit; outs[i]
+ * (compress requests) and statuses[i] (may be NULL) receive each result.
+ * Returns WL_OK when every request succeeded, else the first failure. */
+wl_status wl_serve_wait_batch(wl_server *srv, const unsigned long long *tickets, int n,
+                              wl_result *outs, wl_status *statuses);
 /* Wait up to timeout_ms (0 polls, negative waits without limit).  Returns
  * WL_ETIMEOUT while the request is pending; otherwise the request's own
  * status, fills *info (may be NULL) and, for compress, *out (owns its arrays;
@@ -248,21 +272,23 @@ wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
  * 4 inverse y, 5 inverse x), element type of the pass's global side (0 u8,
  * 1 u16, 2 i32, 3 f32; +4 for 8/16-bit input read from page-locked host
  * memory) and row-length class k (rows of 2^(k-1)+1 .. 2^k elements) -- in
- * tiles of 32, 64 or 128 rows: 32-row tiles split every level into four
- * segments over four warps, 64-row tiles into two, 128-row tiles sweep each
- * row whole.  wl_autotune times every height that fits on a synthetic batch
- * of about 2^24 elements per class on ctx's device (rows up to max_len
- * elements, 0 = 512; reps timed launches per candidate, 0 = 5) and keeps the
- * fastest in a process-wide table that every context uses from its next
- * call.  Untuned classes use 128-row tiles for rows of up to 64 elements and
- * 32-row tiles above.  The tile height changes speed only: every height does
- * the same arithmetic on every element, so results are bit-identical.
+ * tiles of 32, 64 or 128 rows worked by four or eight warps: the warps that
+ * share 32 rows split every lifting level into warps x 32 / rows segments
+ * (a 128-row tile of four warps sweeps each row whole).  wl_autotune times
+ * every shape that fits on a synthetic batch of about 2^24 elements per
+ * class on ctx's device (rows up to max_len elements, 0 = 512; reps timed
+ * launches per candidate, 0 = 5) and keeps the fastest in a process-wide
+ * table that every context uses from its next call.  Untuned classes use
+ * 128-row tiles for rows of up to 64 elements and 32-row tiles above, four
+ * warps.  The shape changes speed only: every shape does the same
+ * arithmetic on every element, so results are bit-identical.
  *
  * The table as text (wl_tune_export; *len = bytes without the NUL, buf may be
  * NULL to ask for the length): one line per tuned class,
- * "pass type class rows us32 us64 us128" with the measured microseconds per
- * launch (0 = not measured).  wl_tune_import reads the same lines (the times
- * are optional); wl_tune_reset returns every class to the default. */
+ * "pass type class rows warps t0 t1 t2 t3 t4 t5" with the measured
+ * microseconds per launch of the shapes 32x4, 64x4, 128x4, 32x8, 64x8, 128x8
+ * (0 = not measured).  wl_tune_import reads the same lines (the times are
+ * optional); wl_tune_reset returns every class to the default. */
 wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps);
 wl_status wl_tune_export(char *buf, size_t cap, size_t *len);
 wl_status wl_tune_import(const char *text);

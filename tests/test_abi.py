@@ -97,11 +97,12 @@ def test_tile_table_round_trip(lib):
     from wavelets_gb300 import lib as L
     L.tune_reset()
     assert L.tune_table() == ""
-    L.tune_load("0 0 6 64 10.5 9.25 11\n3 3 9 32\n\n")
+    L.tune_load("0 0 6 64 8 10.5 9.25 11 0 8 7.5\n3 3 9 32 4\n\n")
     rows = L.tune_rows(L.tune_table())
-    assert rows[(0, 0, 6)] == (64, (10.5, 9.25, 11.0))
-    assert rows[(3, 3, 9)][0] == 32
-    for bad in ("0 0 6 48\n", "6 0 6 32\n", "0 8 6 32\n", "0 0 10 32\n", "0 0\n"):
+    assert rows[(0, 0, 6)] == ((64, 8), (10.5, 9.25, 11.0, 0.0, 8.0, 7.5))
+    assert rows[(3, 3, 9)][0] == (32, 4)
+    for bad in ("0 0 6 48 4\n", "0 0 6 32 6\n", "6 0 6 32 4\n", "0 8 6 32 4\n",
+                "0 0 10 32 4\n", "0 0 6 32\n"):
         with pytest.raises(L.WlError):
             L.tune_load(bad)
     L.tune_reset()

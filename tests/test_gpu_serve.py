@@ -126,3 +126,50 @@ def test_poll_and_device_inputs(ctx):
     srv.close()
     for t, r in zip(tickets, ref):
         assert _same(done[t], r)
+
+
+@pytest.mark.parametrize("stage", [True, False])
+def test_batch_submission_matches_standalone(ctx, stage):
+    """A prepared batch submitted whole (twice, overlapping on two lanes) gives
+    each cubelet's standalone result, with page-locked inputs copied by the
+    copy engine or read in place."""
+    items = _mix(14, 24)
+    ref = [ctx.compress(a, p) for a, p in items]
+    off, offs = 0, []
+    for a, _ in items:
+        offs.append(off)
+        off += (a.nbytes + 255) & ~255
+    pin = lib.PinnedBuffer(off)
+    flat = pin.array(np.uint8, (off,))
+    for (a, _), o in zip(items, offs):
+        flat[o:o + a.nbytes] = a.view(np.uint8).ravel()
+    pb = ctx.prepare_batch([(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                            for (a, p), o in zip(items, offs)], raw=True)
+    srv = lib.Server(lanes=2, max_batch=len(items), stage_host_inputs=stage)
+    t1 = srv.submit_batch(pb)
+    t2 = srv.submit_batch(pb)
+    r1 = srv.wait_batch(t1).results()
+    r2 = srv.wait_batch(t2).results()
+    srv.close()
+    for a, b, r in zip(r1, r2, ref):
+        assert _same(a, r) and _same(b, r)
+
+
+def test_staged_host_inputs_match(ctx):
+    items = _mix(15, 12)
+    ref = [ctx.compress(a, p) for a, p in items]
+    off, offs = 0, []
+    for a, _ in items:
+        offs.append(off)
+        off += (a.nbytes + 255) & ~255
+    pin = lib.PinnedBuffer(off)
+    flat = pin.array(np.uint8, (off,))
+    for (a, _), o in zip(items, offs):
+        flat[o:o + a.nbytes] = a.view(np.uint8).ravel()
+    raw = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+           for (a, p), o in zip(items, offs)]
+    ctx.set_host_input_mode(1)
+    got = ctx.compress_batch(raw, raw=True)
+    ctx.set_host_input_mode(0)
+    for g, r in zip(got, ref):
+        assert _same(g, r)

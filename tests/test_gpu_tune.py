@@ -1,7 +1,7 @@
 """Tile autotuner and CUDA graph replay.
 
-Every tile height of the column-tile transform does the same arithmetic on
-every element, so forcing any height for every size class gives bit-identical
+Every tile shape of the column-tile transform does the same arithmetic on
+every element, so forcing any shape for every size class gives bit-identical
 streams; the autotuner fills the table with measured choices; a batch whose
 geometry repeats is captured once and replayed, with results identical to
 direct launches (for log batches too, whose host table step splits the work
@@ -46,35 +46,35 @@ def _same(a, b):
             and np.array_equal(a.boundaries, b.boundaries))
 
 
-def _forced(rows):
-    """Table lines forcing one tile height for every class where it fits
+def _forced(rows, warps):
+    """Table lines forcing one tile shape for every class where it fits
     (512-element rows cannot take 128-row tiles)."""
     lines = []
     for k in range(6):
         for t in range(8):
             for c in range(10):
                 r = rows if not (rows == 128 and c == 9) else 64
-                lines.append(f"{k} {t} {c} {r}")
+                lines.append(f"{k} {t} {c} {r} {warps}")
     return "\n".join(lines) + "\n"
 
 
-def test_tile_heights_give_identical_results(ctx):
+def test_tile_shapes_give_identical_results(ctx):
     items = _mix(21, 24)
     ctx.set_graph_mode(0)
     got = {}
-    for rows in (32, 64, 128):
-        lib.tune_load(_forced(rows))
+    for shape in lib.TILE_SHAPES:
+        lib.tune_load(_forced(*shape))
         comp = ctx.compress_batch(items)
         dec = [ctx.decompress(c, dtype=a.dtype) for c, (a, _) in zip(comp[:8], items[:8])]
-        got[rows] = (comp, dec)
+        got[shape] = (comp, dec)
     lib.tune_reset()
-    ref_c, ref_d = got[32]
-    for rows in (64, 128):
-        c, d = got[rows]
+    ref_c, ref_d = got[(32, 4)]
+    for shape in lib.TILE_SHAPES[1:]:
+        c, d = got[shape]
         for i, (x, y) in enumerate(zip(c, ref_c)):
-            assert _same(x, y), (rows, i)
+            assert _same(x, y), (shape, i)
         for i, (x, y) in enumerate(zip(d, ref_d)):
-            assert np.array_equal(x, y), (rows, i)
+            assert np.array_equal(x, y), (shape, i)
     ctx.set_graph_mode(1)
 
 
@@ -83,10 +83,11 @@ def test_autotune_fills_table(ctx):
     rows = lib.tune_rows(text)
     # classes 1..7 of six forward-x types, four inverse-x types, four float passes
     assert len(rows) == 7 * (6 + 4 + 4)
-    for (k, t, c), (r, us) in rows.items():
-        assert r in (32, 64, 128)
+    for (k, t, c), (shape, us) in rows.items():
+        assert shape in lib.TILE_SHAPES
         measured = [u for u in us if u > 0]
-        assert measured and min(measured) == us[(32, 64, 128).index(r)]
+        assert len(measured) == 6  # every shape fits rows of up to 128 elements
+        assert min(measured) == us[lib.TILE_SHAPES.index(shape)]
     # results do not depend on the table
     items = _mix(22, 12)
     tuned = ctx.compress_batch(items)

@@ -1,5 +1,5 @@
-// Column-tile wavelet passes: a CTA of four warps per tile of 32, 64 or 128
-// rows; every lane owns one row of the tile.
+// Column-tile wavelet passes: a CTA of four or eight warps per tile of 32, 64
+// or 128 rows; every lane owns one row of the tile.
 //
 // The row-cooperative kernel (dwt.cu) spreads a row over the lanes of a warp
 // and pays index arithmetic and a warp barrier for every lifting step of
@@ -7,14 +7,15 @@
 // streaming sweep that keeps a two-pair window in registers and applies all
 // four lifting steps (or the Haar butterfly) on the way, so an element costs
 // one shared load, one shared store and four float operations per level.
-// The warps that share 32 rows split every level into segments of pairs:
-// four segments for a 32-row tile, two for a 64-row tile, and none for a
-// 128-row tile, where each warp sweeps its 32 rows whole with no halos and no
-// barriers between levels.  More segments give the SM more warps per byte of
-// shared memory; fewer spend less on halos and barriers.  The tile height of
-// each row-length class is chosen by measurement (the tile autotuner in the
+// The warps that share 32 rows split every level into segments of pairs
+// (warps x 32 / rows segments: with four warps, four for a 32-row tile, two
+// for a 64-row tile, none for a 128-row tile, where each warp sweeps its 32
+// rows whole with no halos and no barriers between levels; eight warps
+// double each).  More segments give the SM more warps per byte of shared
+// memory; fewer spend less on halos and barriers.  The tile shape of each
+// row-length class is chosen by measurement (the tile autotuner in the
 // engine); the default is 128 rows for rows of at most 64 elements and 32
-// rows above.
+// rows above, four warps.
 //
 // Tile layout in shared memory: element p of tile row r at tile[p * (R+1) + r]
 // for an R-row tile.  Lanes reading one position of 32 neighbouring rows hit
@@ -46,9 +47,7 @@ namespace wl {
 namespace {
 using namespace dwtc;
 
-constexpr int kRows = 32;         // rows per tile (one per lane)
-constexpr int kSeg = 4;           // warps per CTA = segments per level
-constexpr int kThreadsC = 32 * kSeg;
+constexpr int kRows = 32;         // rows per warp (one per lane)
 
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -294,15 +293,18 @@ __device__ __forceinline__ int group_width(int len) {
   return G;
 }
 
-// ROWS = 32, 64 or 128: warp w owns rows 32 (w / kSegs) .. +31 of the tile
-// and segment w % kSegs of every level of them, kSegs = 128 / ROWS.
-template <typename InT, typename OutT, bool INV, bool VEC, int ROWS>
-__global__ void __launch_bounds__(kThreadsC)
+// ROWS = 32, 64 or 128 rows, NW = 4 or 8 warps: warp w owns rows
+// 32 (w / kSegs) .. +31 of the tile and segment w % kSegs of every level of
+// them, kSegs = 32 NW / ROWS.
+template <typename InT, typename OutT, bool INV, bool VEC, int ROWS, int NW>
+__global__ void __launch_bounds__(32 * NW)
 dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                 int nPasses) {
   static_assert(ROWS == kRows || ROWS == 2 * kRows || ROWS == 4 * kRows, "tile height");
+  static_assert(NW == 4 || NW == 8, "warps per tile");
+  constexpr int kThreadsC = 32 * NW;
   constexpr int kP = ROWS + 1;                 // words between positions of a row
-  constexpr int kSegs = kSeg * kRows / ROWS;   // warps per 32 rows = segments per level
+  constexpr int kSegs = NW * kRows / ROWS;     // warps per 32 rows = segments per level
   extern __shared__ float4 smem4[];
   float *tile = reinterpret_cast<float *>(smem4);
   __shared__ long long rowIn[ROWS], rowOut[ROWS];
@@ -375,7 +377,7 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   } else {
     // contiguous rows: lanes over the elements of one row (G lanes per row)
     const int G = group_width(L), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
-    for (int rb = warp * rpi; rb < nr; rb += kSeg * rpi) {
+    for (int rb = warp * rpi; rb < nr; rb += NW * rpi) {
       const int rr = rb + rsub;
       if (rr >= nr) continue;
       const InT *src = in + rowIn[rr];
@@ -460,7 +462,7 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   } else {
     const int Lc = INV ? min(L, d.cropL) : L;
     const int G = group_width(Lc), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
-    for (int rb = warp * rpi; rb < nr; rb += kSeg * rpi) {
+    for (int rb = warp * rpi; rb < nr; rb += NW * rpi) {
       const int rr = rb + rsub;
       if (rr >= nr) continue;
       const long long base = rowOut[rr];
@@ -479,14 +481,21 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   }
 }
 
-template <typename InT, typename OutT, bool INV, bool VEC = false>
-void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
+template <typename InT, typename OutT, bool INV, bool VEC, int NW>
+void launch_w(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
               cudaStream_t s) {
-  auto k = rows == kRows       ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows>
-           : rows == 2 * kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, 2 * kRows>
-                               : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows>;
+  auto k = rows == kRows       ? dwt_cols_kernel<InT, OutT, INV, VEC, kRows, NW>
+           : rows == 2 * kRows ? dwt_cols_kernel<InT, OutT, INV, VEC, 2 * kRows, NW>
+                               : dwt_cols_kernel<InT, OutT, INV, VEC, 4 * kRows, NW>;
   if (smem > 32 * 1024) raise_smem_limit(k, smem);  // static + dynamic may pass 48 KB
-  k<<<tiles, kThreadsC, smem, s>>>(p, tp, n);
+  k<<<tiles, 32 * NW, smem, s>>>(p, tp, n);
+}
+
+template <typename InT, typename OutT, bool INV, bool VEC = false>
+void launch_t(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows, int warps,
+              cudaStream_t s) {
+  if (warps == 8) launch_w<InT, OutT, INV, VEC, 8>(p, tp, n, tiles, smem, rows, s);
+  else launch_w<InT, OutT, INV, VEC, 4>(p, tp, n, tiles, smem, rows, s);
 }
 
 }  // namespace
@@ -499,32 +508,33 @@ int dwt_cols_smem_bytes(int L, int rows) { return L * (rows + 1) * (int)sizeof(f
 
 // dynamic shared memory available beside the kernel's static arrays
 bool dwt_cols_rows_fit(int L, int rows) {
-  if (rows != kRows && rows != 2 * kRows && rows != 4 * kRows) return false;
+  if (rows != kRows && rows != 2 * kRows && rows != 4 * kRows) return false;  // any warps
   const int kStatic = 2 * 4 * kRows * 8 + 32 * 4 + 1024;  // row bases, scales, reserve
   return dwt_cols_smem_bytes(L, rows) <= 227 * 1024 - kStatic;
 }
 
 void launch_dwt_cols(const PassDesc *p, const int *tp, int n, int tiles, int smem, int rows,
-                     int inType, int outType, bool inverse, bool vecLoad, cudaStream_t s) {
+                     int warps, int inType, int outType, bool inverse, bool vecLoad,
+                     cudaStream_t s) {
   if (!inverse) {
     switch (inType) {
       case WL_U8:
-        if (vecLoad) launch_t<uint8_t, float, false, true>(p, tp, n, tiles, smem, rows, s);
-        else launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, rows, s);
+        if (vecLoad) launch_t<uint8_t, float, false, true>(p, tp, n, tiles, smem, rows, warps, s);
+        else launch_t<uint8_t, float, false>(p, tp, n, tiles, smem, rows, warps, s);
         break;
       case WL_U16:
-        if (vecLoad) launch_t<uint16_t, float, false, true>(p, tp, n, tiles, smem, rows, s);
-        else launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, rows, s);
+        if (vecLoad) launch_t<uint16_t, float, false, true>(p, tp, n, tiles, smem, rows, warps, s);
+        else launch_t<uint16_t, float, false>(p, tp, n, tiles, smem, rows, warps, s);
         break;
-      case WL_I32: launch_t<int32_t, float, false>(p, tp, n, tiles, smem, rows, s); break;
-      default: launch_t<float, float, false>(p, tp, n, tiles, smem, rows, s); break;
+      case WL_I32: launch_t<int32_t, float, false>(p, tp, n, tiles, smem, rows, warps, s); break;
+      default: launch_t<float, float, false>(p, tp, n, tiles, smem, rows, warps, s); break;
     }
   } else {
     switch (outType) {
-      case WL_U8: launch_t<float, uint8_t, true>(p, tp, n, tiles, smem, rows, s); break;
-      case WL_U16: launch_t<float, uint16_t, true>(p, tp, n, tiles, smem, rows, s); break;
-      case WL_I32: launch_t<float, int32_t, true>(p, tp, n, tiles, smem, rows, s); break;
-      default: launch_t<float, float, true>(p, tp, n, tiles, smem, rows, s); break;
+      case WL_U8: launch_t<float, uint8_t, true>(p, tp, n, tiles, smem, rows, warps, s); break;
+      case WL_U16: launch_t<float, uint16_t, true>(p, tp, n, tiles, smem, rows, warps, s); break;
+      case WL_I32: launch_t<float, int32_t, true>(p, tp, n, tiles, smem, rows, warps, s); break;
+      default: launch_t<float, float, true>(p, tp, n, tiles, smem, rows, warps, s); break;
     }
   }
 }

@@ -206,6 +206,7 @@ struct wl_ctx {
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
   // and replay it from then on
   int graphMode = 1;
+  int stageHost = 0;  // copy page-locked inputs with the copy engine
   bool capturing = false;
   unsigned long long gen = 0;  // bumped whenever a buffer is reallocated
   unsigned long long useClock = 0;
@@ -215,6 +216,10 @@ struct wl_ctx {
   long long graphStats[4] = {0, 0, 0, 0};  // direct runs, captures, replays, capture failures
   std::string graphErr;
   cudaEvent_t ev[7] = {};
+  // side streams for the independent launch groups of one transform phase
+  static constexpr int kSide = 3;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork = nullptr, join[kSide] = {};
   float timings[6] = {0, 0, 0, 0, 0, 0};
   bool profiling = false;
   cudaEvent_t pev[10] = {};
@@ -516,27 +521,30 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
 // at `off` bytes into the context's upload block.
 struct GroupLaunch {
   size_t off;
-  int n, tiles, smem, rows, inType, outType;
+  int n, tiles, smem, rows, warps, inType, outType;
   bool inverse, cols, vec;
 };
 
 // Stage a group of passes (descriptors + tile prefix) at hoff of the host
-// upload block and note its launch.  Column-tile groups take the tile height
-// of their size class from the tile table (kind: the pass).
+// upload block and note its launch.  Column-tile groups take the tile shape
+// of their size class from the tile table (kind: the pass) unless one is
+// forced.
 wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int kind, int inType,
                       int outType, bool inverse, bool cols, bool vec,
-                      std::vector<GroupLaunch> &out, int forceRows = 0) {
+                      std::vector<GroupLaunch> &out, const TileShape *force = nullptr) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int);
   if (hoff + bytes > ctx->hPasses.cap || hoff + bytes > ctx->passes.cap)
     return fail(ctx, WL_ENOMEM, "pass staging too small");
-  int rows = 0;
+  int rows = 0, warps = 4;
   if (cols) {
     int Lmax = 0;
     for (const PassDesc &d : g) Lmax = std::max(Lmax, d.L);
     const int gtype = kind == kTuneFwdX ? inType : kind == kTuneInvX ? outType : WL_F32;
-    rows = forceRows ? forceRows : tuned_cols_rows(kind, tune_type_index(gtype, vec), Lmax);
+    const TileShape t = force ? *force : tuned_cols_shape(kind, tune_type_index(gtype, vec), Lmax);
+    rows = t.rows;
+    warps = t.warps;
     for (PassDesc &d : g) {
       d.T = rows;
       d.tiles = (d.rows + rows - 1) / rows;
@@ -553,7 +561,7 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
                                : dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
   }
   tp[n] = tiles;
-  out.push_back({hoff, (int)n, tiles, smem, rows, inType, outType, inverse, cols, vec});
+  out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
@@ -570,20 +578,50 @@ wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind
   return WL_OK;
 }
 
-// Launch staged groups [a, b) whose descriptors are already on the device.
-wl_status launch_groups(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b) {
+wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
   const char *base = P<char>(ctx->passes);
-  for (size_t i = a; i < b; i++) {
-    const GroupLaunch &l = ls[i];
-    const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
-    const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
-    if (l.cols)
-      launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.inType, l.outType, l.inverse,
-                      l.vec, ctx->stream);
-    else
-      launch_dwt_pass(dp, dtp, l.n, l.tiles, l.smem, l.inType, l.outType, l.inverse, ctx->stream);
-    CU(cudaGetLastError());
-    ctx->launches++;
+  const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
+  const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
+  if (l.cols)
+    launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.warps, l.inType, l.outType, l.inverse,
+                    l.vec, s);
+  else
+    launch_dwt_pass(dp, dtp, l.n, l.tiles, l.smem, l.inType, l.outType, l.inverse, s);
+  CU(cudaGetLastError());
+  ctx->launches++;
+  return WL_OK;
+}
+
+// Launch staged groups [a, b) whose descriptors are already on the device,
+// in order on the context's stream.
+wl_status launch_groups(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b) {
+  for (size_t i = a; i < b; i++) TRY(launch_one(ctx, ls[i], ctx->stream));
+  return WL_OK;
+}
+
+// Launch the groups [a, b) of one transform phase concurrently.  They touch
+// disjoint cubelets, so they fork from the context's stream onto it and the
+// side streams (largest first, dealt round-robin), and the phase joins back
+// before anything later in the stream runs.  Small groups -- a few hundred
+// tiles of short rows -- fill the SMs that a lone launch of them would leave
+// idle.
+wl_status launch_phase(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b) {
+  if (b - a <= 1 || !ctx->fork) return launch_groups(ctx, ls, a, b);
+  std::vector<size_t> order;
+  for (size_t i = a; i < b; i++) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return (double)ls[x].tiles * ls[x].smem > (double)ls[y].tiles * ls[y].smem;
+  });
+  const int nStreams = (int)std::min<size_t>(order.size(), wl_ctx::kSide + 1);
+  CU(cudaEventRecord(ctx->fork, ctx->stream));
+  for (int k = 1; k < nStreams; k++) CU(cudaStreamWaitEvent(ctx->side[k - 1], ctx->fork, 0));
+  for (size_t j = 0; j < order.size(); j++) {
+    const int k = (int)(j % nStreams);
+    TRY(launch_one(ctx, ls[order[j]], k ? ctx->side[k - 1] : ctx->stream));
+  }
+  for (int k = 1; k < nStreams; k++) {
+    CU(cudaEventRecord(ctx->join[k - 1], ctx->side[k - 1]));
+    CU(cudaStreamWaitEvent(ctx->stream, ctx->join[k - 1], 0));
   }
   return WL_OK;
 }
@@ -697,13 +735,15 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     for (int i = 0; i < n; i++) dIn[i] = plans[i].data;
   } else {
     // Page-locked host inputs are read in place by the first transform pass
-    // (the GPU reaches pinned memory directly); pageable ones are copied;
-    // device (or managed) pointers are used as they are.
+    // (the GPU reaches pinned memory directly) unless the context stages
+    // them (then, like pageable ones, they are copied -- by the copy engine,
+    // without staging, since they are page-locked); device (or managed)
+    // pointers are used as they are.
     bool staged = false;
     for (int i = 0; i < n; i++) {
       cudaPointerAttributes attr;
       const bool known = cudaPointerGetAttributes(&attr, plans[i].data) == cudaSuccess;
-      if (known && attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+      if (known && attr.type == cudaMemoryTypeHost && attr.devicePointer && !ctx->stageHost) {
         dIn[i] = attr.devicePointer;
         hostIn[i] = 1;
       } else if (known && (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)) {
@@ -847,11 +887,11 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)n * kMaxSymbols * 8, s));
     if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
     mark(ctx, 0);
-    TRY(launch_groups(ctx, gl, 0, gx));
+    TRY(launch_phase(ctx, gl, 0, gx));
     mark(ctx, 1);
-    TRY(launch_groups(ctx, gl, gx, gy));
+    TRY(launch_phase(ctx, gl, gx, gy));
     mark(ctx, 2);
-    TRY(launch_groups(ctx, gl, gy, gl.size()));
+    TRY(launch_phase(ctx, gl, gy, gl.size()));
     mark(ctx, 3);
     CU(record(ctx, ctx->ev[1]));
     if (coefOut) return WL_OK;
@@ -1210,13 +1250,13 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
 // ---- tile autotuner -------------------------------------------------------------
 // For every size class of the column-tile transform -- pass (forward x / y / z,
 // inverse z / y / x), element type of its global side, row-length class 2^k --
-// time each tile height that fits (32, 64, 128 rows) on a synthetic batch of
-// about 2^24 elements on the device: blocks with the tuned axis 2^k long and
-// the other two max(32, min(2^k, 2^((24-k)/2))) (cubes from 32 to 256, two
-// 512 x 128 x 128 blocks at 512), CDF 9/7 with up to 3 levels on the tuned
-// axis.  The fastest height goes
-// into the process-wide tile table.  The forward x pass of 8- and 16-bit data
-// is tuned twice, reading from device memory and from page-locked host memory.
+// time each tile shape that fits (32, 64 or 128 rows, four or eight warps) on
+// a synthetic batch of about 2^24 elements on the device: blocks with the
+// tuned axis 2^k long and the other two max(32, min(2^k, 2^((24-k)/2))) (cubes
+// from 32 to 256, two 512 x 128 x 128 blocks at 512), CDF 9/7 with up to 3
+// levels on the tuned axis.  The fastest shape goes into the process-wide tile
+// table.  The forward x pass of 8- and 16-bit data is tuned twice, reading
+// from device memory and from page-locked host memory.
 wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
   CU(cudaSetDevice(ctx->device));
   const long long kElems = 1LL << 24;
@@ -1300,16 +1340,14 @@ wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
         TRY(ensure_host(ctx, ctx->hPasses, need));
         const bool inv = kind >= kTuneInvZ;
         const int inType = inv ? WL_F32 : ty.first, outType = kind == kTuneInvX ? ty.first : WL_F32;
-        float us[3] = {0, 0, 0};
-        int best = 0;
-        float bestUs = 0;
-        const int cand[3] = {32, 64, 128};
-        for (int ci = 0; ci < 3; ci++) {
-          if (!dwt_cols_rows_fit(L, cand[ci])) continue;
+        float us[kTileShapes] = {0, 0, 0, 0, 0, 0};
+        int best = -1;
+        for (int ci = 0; ci < kTileShapes; ci++) {
+          const TileShape cand = kTileShape[ci];
+          if (!dwt_cols_rows_fit(L, cand.rows)) continue;
           std::vector<GroupLaunch> gl;
           size_t hoff = 0;
-          TRY(stage_group(ctx, g, hoff, kind, inType, outType, inv, true, ty.second, gl,
-                          cand[ci]));
+          TRY(stage_group(ctx, g, hoff, kind, inType, outType, inv, true, ty.second, gl, &cand));
           CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, hoff, cudaMemcpyHostToDevice, s));
           TRY(launch_groups(ctx, gl, 0, gl.size()));  // warm-up
           for (int r = 0; r < reps; r++) {
@@ -1322,12 +1360,10 @@ wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
           for (int r = 0; r < reps; r++) CU(cudaEventElapsedTime(&t[r], ev[r], ev[r + 1]));
           std::sort(t.begin(), t.end());
           us[ci] = t[reps / 2] * 1000.f;
-          if (!best || us[ci] < bestUs) {
-            best = cand[ci];
-            bestUs = us[ci];
-          }
+          if (best < 0 || us[ci] < us[best]) best = ci;
         }
-        set_tuned_cols_rows(kind, tune_type_index(ty.first, ty.second), lg, best, us);
+        if (best >= 0)
+          set_tuned_cols_shape(kind, tune_type_index(ty.first, ty.second), lg, kTileShape[best], us);
       }
     }
   }
@@ -1390,6 +1426,11 @@ void wl_result_free(wl_result *r) {
   memset(r, 0, sizeof *r);
 }
 
+void wl_results_free(wl_result *r, int n) {
+  if (!r) return;
+  for (int i = 0; i < n; i++) wl_result_free(r + i);
+}
+
 wl_status wl_init(int device, wl_ctx **out) {
   if (!out) return WL_EINVAL;
   *out = nullptr;
@@ -1408,6 +1449,15 @@ wl_status wl_init(int device, wl_ctx **out) {
     return WL_ECUDA;
   }
   for (auto &e : ctx->ev) cudaEventCreate(&e);
+  bool sideOk = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < wl_ctx::kSide && sideOk; k++)
+    sideOk = cudaStreamCreateWithFlags(&ctx->side[k], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->join[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!sideOk) {  // phases then run in order on the context's stream
+    cudaGetLastError();
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    ctx->fork = nullptr;
+  }
   for (auto &e : ctx->pev) cudaEventCreate(&e);
   *out = ctx;
   return WL_OK;
@@ -1432,6 +1482,11 @@ void wl_destroy(wl_ctx *ctx) {
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
   for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
   for (auto &e : ctx->pev) if (e) cudaEventDestroy(e);
+  for (int k = 0; k < wl_ctx::kSide; k++) {
+    if (ctx->side[k]) cudaStreamDestroy(ctx->side[k]);
+    if (ctx->join[k]) cudaEventDestroy(ctx->join[k]);
+  }
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1600,6 +1655,12 @@ wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps) {
   if (reps <= 0) reps = 5;
   if (reps > 64) reps = 64;
   return autotune_impl(ctx, max_len, reps);
+}
+
+wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return WL_EINVAL;
+  ctx->stageHost = mode;
+  return WL_OK;
 }
 
 wl_status wl_set_graph_mode(wl_ctx *ctx, int mode) {

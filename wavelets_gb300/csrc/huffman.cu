@@ -56,7 +56,11 @@ __host__ __device__ inline size_t build_smem_bytes(int S) {
   return (b + 15) & ~(size_t)15;
 }
 
-__global__ void __launch_bounds__(1024) huffman_build_kernel(DevBatch b) {
+// 256 threads: the merge, depths and decode table are one thread's work, so a
+// small CTA lets every cubelet of a large batch build at once (eight CTAs per
+// SM) instead of waiting for a second wave.
+constexpr int kBuildThreads = 256;
+__global__ void __launch_bounds__(kBuildThreads) huffman_build_kernel(DevBatch b) {
   extern __shared__ unsigned long long hsm[];
   __shared__ int nLeaves;
   const int ci = blockIdx.x;
@@ -540,7 +544,7 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const size_t smem = build_smem_bytes(maxSymbols);
   raise_smem_limit(huffman_build_kernel, (int)smem);
-  huffman_build_kernel<<<b.n, 1024, smem, s>>>(b);
+  huffman_build_kernel<<<b.n, kBuildThreads, smem, s>>>(b);
 }
 
 void launch_pack_meta(DevBatch &b, cudaStream_t s) { pack_meta_kernel<<<b.n, 256, 0, s>>>(b); }

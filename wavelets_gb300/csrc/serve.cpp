@@ -205,6 +205,7 @@ void wl_serve_config_default(wl_serve_config *cfg) {
   cfg->lanes = 2;
   cfg->memory_budget = (size_t)16 << 30;
   cfg->max_batch = 1024;
+  cfg->stage_host_inputs = 1;
 }
 
 wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out) {
@@ -225,42 +226,62 @@ wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **ou
       return st;
     }
     s->ctxs.push_back(c);
+    wl_set_host_input_mode(c, s->cfg.stage_host_inputs ? 1 : 0);
   }
   for (int i = 0; i < s->cfg.lanes; i++) s->workers.emplace_back(worker, s, i);
   *out = s;
   return WL_OK;
 }
 
-wl_status wl_serve_submit(wl_server *s, const wl_request *req, unsigned long long *ticket) {
-  if (!s || !req || !ticket) return WL_EINVAL;
-  if (req->kind == WL_REQ_COMPRESS) {
-    if (!req->cubelet.data) return serve_fail(s, WL_EINVAL, "compress request without data");
-    for (int a = 0; a < 3; a++)
-      if (req->cubelet.size[a] < 1) return serve_fail(s, WL_EINVAL, "empty cubelet size");
-  } else if (req->kind == WL_REQ_DECOMPRESS) {
-    if (!req->compressed || !req->out)
-      return serve_fail(s, WL_EINVAL, "decompress request without input or output");
-  } else {
-    return serve_fail(s, WL_EINVAL, "unknown request kind %d", req->kind);
+wl_status wl_serve_submit_batch(wl_server *s, const wl_request *reqs, int n,
+                                unsigned long long *tickets) {
+  if (!s || !reqs || !tickets || n < 0) return WL_EINVAL;
+  for (int i = 0; i < n; i++) {
+    const wl_request *req = reqs + i;
+    if (req->kind == WL_REQ_COMPRESS) {
+      if (!req->cubelet.data)
+        return serve_fail(s, WL_EINVAL, "request %d: compress request without data", i);
+      for (int a = 0; a < 3; a++)
+        if (req->cubelet.size[a] < 1)
+          return serve_fail(s, WL_EINVAL, "request %d: empty cubelet size", i);
+    } else if (req->kind == WL_REQ_DECOMPRESS) {
+      if (!req->compressed || !req->out)
+        return serve_fail(s, WL_EINVAL, "request %d: decompress request without input or output",
+                          i);
+    } else {
+      return serve_fail(s, WL_EINVAL, "request %d: unknown request kind %d", i, req->kind);
+    }
   }
-  Job *j = new Job;
-  j->req = *req;
-  memset(&j->res, 0, sizeof j->res);
-  j->est = estimate(*req);
-  j->submitted = Clock::now();
+  std::vector<Job *> js(n);
+  const Clock::time_point now = Clock::now();
+  for (int i = 0; i < n; i++) {
+    Job *j = new Job;
+    j->req = reqs[i];
+    memset(&j->res, 0, sizeof j->res);
+    j->est = estimate(reqs[i]);
+    j->submitted = now;
+    js[i] = j;
+  }
   {
     std::lock_guard<std::mutex> g(s->mu);
     if (s->stop) {
-      delete j;
+      for (Job *j : js) delete j;
       return WL_EINVAL;
     }
-    j->id = s->nextId++;
-    s->jobs[j->id] = j;
-    s->pending.push_back(j);
-    *ticket = j->id;
+    for (int i = 0; i < n; i++) {
+      Job *j = js[i];
+      j->id = s->nextId++;
+      s->jobs[j->id] = j;
+      s->pending.push_back(j);
+      tickets[i] = j->id;
+    }
   }
   s->cvWork.notify_one();
   return WL_OK;
+}
+
+wl_status wl_serve_submit(wl_server *s, const wl_request *req, unsigned long long *ticket) {
+  return wl_serve_submit_batch(s, req, 1, ticket);
 }
 
 wl_status wl_serve_wait(wl_server *s, unsigned long long ticket, int timeout_ms, wl_result *out,
@@ -296,6 +317,18 @@ wl_status wl_serve_wait(wl_server *s, unsigned long long ticket, int timeout_ms,
   }
   delete j;
   return st;
+}
+
+wl_status wl_serve_wait_batch(wl_server *s, const unsigned long long *tickets, int n,
+                              wl_result *outs, wl_status *statuses) {
+  if (!s || !tickets || n < 0) return WL_EINVAL;
+  wl_status first = WL_OK;
+  for (int i = 0; i < n; i++) {
+    const wl_status st = wl_serve_wait(s, tickets[i], -1, outs ? outs + i : nullptr, nullptr);
+    if (statuses) statuses[i] = st;
+    if (st != WL_OK && first == WL_OK) first = st;
+  }
+  return first;
 }
 
 const char *wl_serve_last_error(const wl_server *s) {

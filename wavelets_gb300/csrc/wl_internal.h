@@ -208,7 +208,8 @@ int dwt_smem_bytes(int L, int T, bool exact);
 // column-tile passes (dwt_cols.cu): lifting / Haar, rows up to kColsMaxL
 constexpr int kColsMaxL = 512;
 void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int tiles,
-                     int smem, int rows, int inType, int outType, bool inverse, bool vecLoad,
+                     int smem, int rows, int warps, int inType, int outType, bool inverse,
+                     bool vecLoad,
                      cudaStream_t s);
 int dwt_cols_tile_rows(int L);               // default tile height for rows of L
 int dwt_cols_smem_bytes(int L, int rows);
@@ -217,9 +218,17 @@ bool dwt_cols_rows_fit(int L, int rows);      // rows in {32, 64, 128} and smem 
 // ---- column-tile heights per size class (tune.cpp) ----
 enum TuneKind { kTuneFwdX, kTuneFwdY, kTuneFwdZ, kTuneInvZ, kTuneInvY, kTuneInvX, kTuneKinds };
 int tune_type_index(int dtype, bool vec);
-// tile height for rows of up to L elements: the tuned entry, else the default
-int tuned_cols_rows(int kind, int typeIdx, int L);
-void set_tuned_cols_rows(int kind, int typeIdx, int cls, int rows, const float us[3]);
+// tile shape (rows, warps) for rows of up to L elements: the tuned entry,
+// else the default
+struct TileShape {
+  int rows, warps;
+};
+constexpr int kTileShapes = 6;  // candidates: rows 32/64/128 x warps 4/8
+constexpr TileShape kTileShape[kTileShapes] = {{32, 4}, {64, 4}, {128, 4},
+                                               {32, 8}, {64, 8}, {128, 8}};
+TileShape tuned_cols_shape(int kind, int typeIdx, int L);
+void set_tuned_cols_shape(int kind, int typeIdx, int cls, TileShape t,
+                          const float us[kTileShapes]);
 unsigned tune_version();  // changes whenever the table does
 
 // launchers (select.cu)

@@ -66,7 +66,7 @@ REQ_COMPRESS, REQ_DECOMPRESS = 1, 2
 
 class WlServeConfig(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("memory_budget", ctypes.c_size_t),
-                ("max_batch", ctypes.c_int)]
+                ("max_batch", ctypes.c_int), ("stage_host_inputs", ctypes.c_int)]
 
 
 class WlRequest(ctypes.Structure):
@@ -130,8 +130,15 @@ EXPORTS = {
                                        ctypes.POINTER(ctypes.c_ulonglong)]),
     "wl_serve_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_int,
                                      ctypes.POINTER(WlResult), ctypes.POINTER(WlRequestInfo)]),
+    "wl_serve_submit_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlRequest),
+                                             ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "wl_serve_wait_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
+                                           ctypes.c_int, ctypes.POINTER(WlResult),
+                                           ctypes.POINTER(ctypes.c_int)]),
+    "wl_set_host_input_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_serve_destroy": (None, [ctypes.c_void_p]),
+    "wl_results_free": (None, [ctypes.POINTER(WlResult), ctypes.c_int]),
     "wl_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "wl_tune_export": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t,
                                       ctypes.POINTER(ctypes.c_size_t)]),
@@ -269,8 +276,50 @@ class _ResultsOwner:
 
     def __del__(self):
         try:
-            for i in range(self.n):
-                self.lib.wl_result_free(ctypes.byref(self.outs[i]))
+            self.lib.wl_results_free(self.outs, self.n)
+        except Exception:
+            pass
+
+
+class PreparedBatch:
+    """A batch description (the wl_cubelet array) built once and compressed
+    any number of times: inputs that stay at the same addresses -- pinned
+    staging buffers, device arrays -- are described once, so a call costs
+    only the library's own work."""
+
+    def __init__(self, cubs, n, on_device, keep):
+        self.cubs, self.n, self.on_device, self._keep = cubs, n, on_device, keep
+
+
+class ResultBatch:
+    """The results of one compression call, left in the library's structs
+    until asked for: results() makes the Compressed objects (zero-copy),
+    release() frees them without looking."""
+
+    def __init__(self, lib, outs, n):
+        self.lib, self.outs, self.n = lib, outs, n
+        self._live = True
+
+    def __len__(self):
+        return self.n
+
+    def compressed_bytes(self) -> int:
+        rec = np.frombuffer(self.outs, _result_dtype_cached(), count=self.n)
+        return int(rec["n_words"].astype(np.int64).sum()) * 4
+
+    def results(self) -> List["Compressed"]:
+        assert self._live, "results already taken or released"
+        self._live = False
+        return adopt_results(self.lib, self.outs, self.n)
+
+    def release(self):
+        if self._live:
+            self._live = False
+            self.lib.wl_results_free(self.outs, self.n)
+
+    def __del__(self):
+        try:
+            self.release()
         except Exception:
             pass
 
@@ -298,6 +347,13 @@ def _result_dtype():
 _RESULT_DT = None
 
 
+def _result_dtype_cached():
+    global _RESULT_DT
+    if _RESULT_DT is None:
+        _RESULT_DT = _result_dtype()
+    return _RESULT_DT
+
+
 def adopt_results(lib, outs, n) -> List["Compressed"]:
     """Compressed objects over the results' arrays without copying them.  The
     library keeps a batch's arrays in one block; the numpy views hold a
@@ -312,8 +368,7 @@ def adopt_results(lib, outs, n) -> List["Compressed"]:
     used = (cnts > 0) & (ptrs != 0)
     if n == 0 or not used.any() or not (rec["owner"] != 0).all():
         res = [Compressed.from_struct(outs[i]) for i in range(n)]
-        for i in range(n):
-            lib.wl_result_free(ctypes.byref(outs[i]))
+        lib.wl_results_free(outs, n)
         return res
     # one numpy view per storage block (a pipelined batch has several); all
     # views share the owner that releases the batch's results
@@ -404,10 +459,9 @@ class Context:
         self._check(st)
         return adopt_results(self.lib, (WlResult * 1)(res), 1)[0]
 
-    def compress_batch(self, items: Sequence, params=None, on_device: bool = False,
-                       raw: bool = False) -> List[Compressed]:
-        """items: list of numpy arrays, or (array, Params) pairs, or, with
-        on_device/raw, (ptr, dtype, size, Params) tuples."""
+    def prepare_batch(self, items: Sequence, params=None, on_device: bool = False,
+                      raw: bool = False) -> PreparedBatch:
+        """Describe a batch once (see compress_batch for items)."""
         n = len(items)
         cubs = (WlCubelet * n)()
         keep = []
@@ -428,10 +482,21 @@ class Context:
             cubs[i].dtype = dt
             cubs[i].size[:] = size
             cubs[i].params = make_params(prm if prm is not None else params)
-        outs = (WlResult * n)()
-        st = self.lib.wl_compress_batch(self.h, cubs, n, 1 if on_device else 0, outs)
+        return PreparedBatch(cubs, n, on_device, keep)
+
+    def compress_prepared(self, pb: PreparedBatch, lazy: bool = False):
+        """Compress a prepared batch; lazy returns a ResultBatch."""
+        outs = (WlResult * pb.n)()
+        st = self.lib.wl_compress_batch(self.h, pb.cubs, pb.n, 1 if pb.on_device else 0, outs)
         self._check(st)
-        return adopt_results(self.lib, outs, n)
+        rb = ResultBatch(self.lib, outs, pb.n)
+        return rb if lazy else rb.results()
+
+    def compress_batch(self, items: Sequence, params=None, on_device: bool = False,
+                       raw: bool = False) -> List[Compressed]:
+        """items: list of numpy arrays, or (array, Params) pairs, or, with
+        on_device/raw, (ptr, dtype, size, Params) tuples."""
+        return self.compress_prepared(self.prepare_batch(items, params, on_device, raw))
 
     def compress_split(self, volume, cube=(128, 128, 128), overlap=8, params=None,
                        ptr=None, on_device=False):
@@ -536,6 +601,11 @@ class Context:
         self._check(self.lib.wl_autotune(self.h, int(max_len), int(reps)))
         return tune_table()
 
+    def set_host_input_mode(self, mode: int):
+        """0: read page-locked host inputs in place; 1: copy them with the
+        copy engine first."""
+        self._check(self.lib.wl_set_host_input_mode(self.h, int(mode)))
+
     def set_graph_mode(self, mode: int):
         """1: capture a batch geometry seen twice in a row as a CUDA graph
         and replay it; 0: always launch directly."""
@@ -556,7 +626,8 @@ TUNE_PASSES = ("fwd_x", "fwd_y", "fwd_z", "inv_z", "inv_y", "inv_x")
 
 def tune_table() -> str:
     """The process-wide tile table: one line per tuned size class,
-    "pass type class rows us32 us64 us128"."""
+    "pass type class rows warps" and the microseconds of the six candidate
+    shapes (TILE_SHAPES)."""
     lib = load()
     n = ctypes.c_size_t()
     st = lib.wl_tune_export(None, 0, ctypes.byref(n))
@@ -580,14 +651,18 @@ def tune_reset():
     load().wl_tune_reset()
 
 
+TILE_SHAPES = ((32, 4), (64, 4), (128, 4), (32, 8), (64, 8), (128, 8))
+
+
 def tune_rows(text: str):
-    """Parse a tile table: {(pass, type, class): (rows, (us32, us64, us128))}."""
+    """Parse a tile table: {(pass, type, class): ((rows, warps), times)} with
+    the microseconds of the TILE_SHAPES candidates (0 = not measured)."""
     out = {}
     for ln in text.splitlines():
         f = ln.split()
-        if len(f) >= 4:
+        if len(f) >= 5:
             out[(int(f[0]), int(f[1]), int(f[2]))] = (
-                int(f[3]), tuple(float(x) for x in f[4:7]) if len(f) >= 7 else ())
+                (int(f[3]), int(f[4])), tuple(float(x) for x in f[5:11]))
     return out
 
 
@@ -670,11 +745,12 @@ class Server:
     until their request has been waited for."""
 
     def __init__(self, lanes: int = 2, memory_budget: int = 16 << 30, max_batch: int = 1024,
-                 device: int = 0):
+                 device: int = 0, stage_host_inputs: bool = True):
         self.lib = load()
         cfg = WlServeConfig()
         self.lib.wl_serve_config_default(ctypes.byref(cfg))
         cfg.lanes, cfg.memory_budget, cfg.max_batch = lanes, memory_budget, max_batch
+        cfg.stage_host_inputs = 1 if stage_host_inputs else 0
         h = ctypes.c_void_p()
         st = self.lib.wl_serve_create(device, ctypes.byref(cfg), ctypes.byref(h))
         if st != WL_OK:
@@ -703,6 +779,34 @@ class Server:
         req.cubelet.size[:] = size
         req.cubelet.params = make_params(params)
         return self._submit(req, keep)
+
+    def submit_batch(self, pb: "PreparedBatch") -> np.ndarray:
+        """Queue every cubelet of a prepared batch back to back (a free lane
+        takes them together); returns their tickets."""
+        reqs = getattr(pb, "_reqs", None)
+        if reqs is None:
+            reqs = (WlRequest * pb.n)()
+            for i in range(pb.n):
+                reqs[i].kind = REQ_COMPRESS
+                reqs[i].cubelet = pb.cubs[i]
+            pb._reqs = reqs
+        t = (ctypes.c_ulonglong * pb.n)()
+        st = self.lib.wl_serve_submit_batch(self.h, reqs, pb.n, t)
+        if st != WL_OK:
+            raise WlError(st, self.lib.wl_serve_last_error(self.h).decode())
+        return t
+
+    def wait_batch(self, tickets) -> "ResultBatch":
+        """Wait for the tickets of submit_batch; the results as a ResultBatch."""
+        n = len(tickets)
+        outs = (WlResult * n)()
+        sts = (ctypes.c_int * n)()
+        st = self.lib.wl_serve_wait_batch(self.h, tickets, n, outs, sts)
+        rb = ResultBatch(self.lib, outs, n)
+        if st != WL_OK:
+            rb.release()
+            raise WlError(st, self.lib.wl_serve_last_error(self.h).decode())
+        return rb
 
     def submit_decompress(self, c: "Compressed", out: np.ndarray) -> int:
         """Restore `c` into the host array `out` (original size, any dtype)."""
