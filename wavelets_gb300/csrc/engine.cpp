@@ -200,7 +200,7 @@ struct wl_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
   HostBuf hState, hWords, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
@@ -706,6 +706,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
   TRY(ensure(ctx, ctx->hist, (size_t)n * kMaxSymbols * 8));
   TRY(ensure(ctx, ctx->chunkRun, chunkTotal * sizeof(int4)));
+  TRY(ensure(ctx, ctx->chunkSpan, chunkTotal * sizeof(int2)));
   TRY(ensure(ctx, ctx->chunkRunCtx, chunkTotal * 2 * sizeof(long long)));
   TRY(ensure(ctx, ctx->chunkBits, chunkTotal * 8));
   TRY(ensure(ctx, ctx->codes, (size_t)n * kMaxSymbols * 8));
@@ -818,6 +819,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.dqtable = P<float>(ctx->dqtable);
   b.hist = P<unsigned long long>(ctx->hist);
   b.chunkRun = P<int4>(ctx->chunkRun);
+  b.chunkSpan = P<int2>(ctx->chunkSpan);
   b.chunkRunCtx = P<long long>(ctx->chunkRunCtx);
   b.chunkBits = P<unsigned long long>(ctx->chunkBits);
   b.codes = P<unsigned long long>(ctx->codes);
@@ -1471,6 +1473,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->state,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkCub, &ctx->groupCub,
+                   &ctx->chunkSpan,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
                    &ctx->meta};

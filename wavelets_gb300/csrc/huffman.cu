@@ -225,48 +225,10 @@ __global__ void __launch_bounds__(kBuildThreads) huffman_build_kernel(DevBatch b
 }
 
 // ---- tokens -----------------------------------------------------------------
-constexpr int kMaxEdgeTokens = 32;   // tokens of one run inside one chunk: <= 19
-constexpr int kMaxChunkTokens = kChunk + 2 * kMaxEdgeTokens;
-
-// Build the ordered token list of a chunk in shared memory: the tokens of
-// the run entering the chunk, the chunk's stored tokens, the tokens of the
-// run leaving it.  The stored tokens go to list[kMaxEdgeTokens...] while
-// thread 0 works out the edge runs, whose entering tokens end right before
-// them.  Returns the count; *first = index of the first token.  Collective
-// (one barrier).
-__device__ int chunk_tokens(const DevBatch &b, long long chunk, const CubeletDev &cd,
-                            int dupV, uint16_t *list, int *sCount, int *first) {
-  const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int nInt = b.chunkTok[chunk];
-  const uint16_t *src = b.tok + cd.coefOff + cstart;
-  for (int i = threadIdx.x; i < nInt; i += kThreads) list[kMaxEdgeTokens + i] = src[i];
-  if (threadIdx.x == 0) {
-    int nPre = 0, nPost = 0;
-    uint16_t pre[kMaxEdgeTokens];
-    uint16_t *post = list + kMaxEdgeTokens + nInt;
-    if (dupV >= 0) {
-      const int4 cr = b.chunkRun[chunk];  // lead, trail, allZero, len
-      const long long runIn = b.chunkRunCtx[2 * chunk], runOut = b.chunkRunCtx[2 * chunk + 1];
-      const int dupKey = cd.binCount;
-      if (cr.x > 0) {
-        const long long e = cr.z ? runOut : cstart + cr.x;
-        run_tokens(runIn, e, cstart, cstart + (cr.z ? cr.w : cr.x), dupKey, dupV,
-                   [&](uint16_t t) { if (nPre < kMaxEdgeTokens) pre[nPre++] = t; });
-      }
-      if (!cr.z && cr.y > 0) {
-        const long long s0 = cstart + cr.w - cr.y;
-        run_tokens(s0, runOut, s0, cstart + cr.w, dupKey, dupV,
-                   [&](uint16_t t) { if (nPost < kMaxEdgeTokens) post[nPost++] = t; });
-      }
-    }
-    for (int i = 0; i < nPre; i++) list[kMaxEdgeTokens - nPre + i] = pre[i];
-    sCount[0] = kMaxEdgeTokens - nPre;
-    sCount[1] = nPre + nInt + nPost;
-  }
-  __syncthreads();
-  *first = sCount[0];
-  return sCount[1];
-}
+// A chunk's tokens, in stream order, are slots [span.x, span.x + span.y) of
+// its token slot: the zero-run tokens entering it, its stored tokens and the
+// zero-run tokens leaving it (quantize_kernel and runs_kernel put them there).
+constexpr int kMaxChunkTokens = kChunk;
 
 __device__ __forceinline__ int token_len(uint16_t t, const uint8_t *len, int dupKey) {
   const int sym = t & 0x1fff;
@@ -305,36 +267,22 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, un
   return before + inc - v;
 }
 
-// Bits of a chunk: its stored tokens straight from global memory, plus the
-// tokens of the zero runs crossing its edges (thread 0).
+// Bits of a chunk: the code lengths of its tokens, read straight from its slot.
 __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
   __shared__ uint8_t sLen[kMaxSymbols + 3];
   __shared__ unsigned long long sh[kThreads / 32];
   const long long chunk = blockIdx.x;
   const int ci = b.chunkCub[chunk];
   const CubeletDev cd = b.cub[ci];
-  const int dupV = b.state[ci].dupValue, dupKey = cd.binCount;
+  const int dupKey = cd.binCount;
   const int S = cd.binCount + 1;
   for (int i = threadIdx.x; i < S; i += kThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
   const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int nInt = b.chunkTok[chunk];
-  const uint16_t *src = b.tok + cd.coefOff + cstart;
+  const int2 span = b.chunkSpan[chunk];
+  const uint16_t *src = b.tok + cd.coefOff + cstart + span.x;
   __syncthreads();
   unsigned long long s = 0;
-  for (int i = threadIdx.x; i < nInt; i += kThreads) s += token_len(src[i], sLen, dupKey);
-  if (threadIdx.x == 0 && dupV >= 0) {
-    const int4 cr = b.chunkRun[chunk];  // lead, trail, allZero, len
-    const long long runIn = b.chunkRunCtx[2 * chunk], runOut = b.chunkRunCtx[2 * chunk + 1];
-    auto add = [&](uint16_t t) { s += token_len(t, sLen, dupKey); };
-    if (cr.x > 0) {
-      const long long e = cr.z ? runOut : cstart + cr.x;
-      run_tokens(runIn, e, cstart, cstart + (cr.z ? cr.w : cr.x), dupKey, dupV, add);
-    }
-    if (!cr.z && cr.y > 0) {
-      const long long s0 = cstart + cr.w - cr.y;
-      run_tokens(s0, runOut, s0, cstart + cr.w, dupKey, dupV, add);
-    }
-  }
+  for (int i = threadIdx.x; i < span.y; i += kThreads) s += token_len(src[i], sLen, dupKey);
   s = block_sum(s, sh);
   if (threadIdx.x == 0) b.chunkBits[chunk] = s;
 }
@@ -457,7 +405,6 @@ __host__ __device__ inline size_t write_smem_bytes(int S) {
 
 __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   __shared__ uint16_t list[kMaxChunkTokens];
-  __shared__ int sCount[2];
   __shared__ unsigned shs[kThreads / 32];
   extern __shared__ unsigned long long wsm[];
   const int ci = b.groupCub[blockIdx.x];
@@ -466,7 +413,7 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
   if (st->error) return;
   const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
   const int nc = min(kQuantGroup, cd.nChunks - c0);
-  const int dupV = st->dupValue, dupKey = cd.binCount;
+  const int dupKey = cd.binCount;
   const int S = cd.binCount + 1;
   // tables sized for this cubelet's alphabet (the launch sizes for the largest)
   unsigned long long *sCode = wsm;
@@ -492,9 +439,12 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
       // by encode_zero_kernel and are shared with the neighbours
       for (int i = 1 + threadIdx.x; i < nW - 1; i += kThreads) gw[i] = 0;
     }
-    int first;
-    const int n = chunk_tokens(b, chunk, cd, dupV, list, sCount, &first);  // has a barrier
-    const uint16_t *tl = list + first;
+    const int2 span = b.chunkSpan[chunk];
+    const uint16_t *src = b.tok + cd.coefOff + (chunk - cd.chunkBase) * (long long)kChunk + span.x;
+    const int n = span.y;
+    for (int i = threadIdx.x; i < n; i += kThreads) list[i] = src[i];
+    __syncthreads();
+    const uint16_t *tl = list;
     uint32_t *dstw = staged ? sw : gw;
     // each thread takes a contiguous slice of the tokens
     const int per = (n + kThreads - 1) / kThreads;

@@ -456,7 +456,6 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
     const long long start = (long long)(c0 + k) * kChunk;
     const int len = (int)min((long long)kChunk, cd.n - start);
     const float *src = coef + cd.coefOff + start;
-    uint16_t *dst = b.tok + cd.coefOff + start;
 
     // ---- phase 1: candidates into the warp's region
     int nCand = 0;  // warp-uniform
@@ -511,6 +510,13 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
     // the value before this warp's first: positions grow with the warp index
     int prevW = -1;
     for (int v = 0; v < w; v++) prevW = max(prevW, wLast[par][v]);
+    // the chunk's tokens go to its slot from the first value's position on;
+    // the lead zero run's tokens (written later by runs_kernel) fit before
+    // it, since each token starts at its own element
+    int lead = len;
+    for (int v = kWarps - 1; v >= 0; v--)
+      if (wFirst[par][v] >= 0) lead = wFirst[par][v];
+    uint16_t *dst = b.tok + cd.coefOff + start + lead;
     int myTok = 0, singles = 0, dups = 0;
     {
       int carry = prevW;
@@ -594,6 +600,7 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef) {
     }
     if (threadIdx.x == 0) {
       b.chunkTok[chunk] = (int)nTok;
+      b.chunkSpan[chunk] = make_int2(lead, (int)nTok);  // runs_kernel adds the edge runs
       if (dupV >= 0) {
         int first = -1, last = -1;
         for (int v = 0; v < kWarps; v++) {
@@ -724,6 +731,29 @@ __global__ void __launch_bounds__(1024) runs_kernel(DevBatch b) {
           dups += dp;
         }
       }
+      // Tokens of the zero runs at the chunk's edges that start inside it,
+      // in stream order around the stored tokens [lead, lead + nInt): the
+      // entering run's right before them, the leaving run's right after.
+      const long long cstart = (long long)c * kChunk;
+      uint16_t *slot = b.tok + cd.coefOff + cstart;
+      const int nInt = b.chunkTok[base + c];
+      const int dupKey = cd.binCount;
+      int nPre = 0, nPost = 0;
+      if (me.x > 0) {
+        const long long runIn = ctx[2 * c];
+        const long long re = me.z ? e : cstart + me.x;
+        const long long w1 = cstart + (me.z ? me.w : me.x);
+        run_tokens(runIn, re, cstart, w1, dupKey, dupV, [&](uint16_t) { nPre++; });
+        int i = me.x - nPre;
+        run_tokens(runIn, re, cstart, w1, dupKey, dupV, [&](uint16_t t) { slot[i++] = t; });
+      }
+      if (!me.z && me.y > 0) {
+        const long long s0 = cstart + me.w - me.y;
+        int i = me.x + nInt;
+        run_tokens(s0, e, s0, cstart + me.w, dupKey, dupV, [&](uint16_t t) { slot[i++] = t; });
+        nPost = i - (me.x + nInt);
+      }
+      b.chunkSpan[base + c] = make_int2(me.x - nPre, nPre + nInt + nPost);
     }
     // the run starting at element 0 belongs to no chunk's tail
     if (seg == 0 && threadIdx.x == 0) {

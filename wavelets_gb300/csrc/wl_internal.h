@@ -168,7 +168,9 @@ struct DevBatch {
   float *coef;                    // coefficients (ping)
   float *coef2;                   // second buffer (pong)
   uint16_t *tok;                  // Huffman tokens, one slot of kChunk per chunk
-  int *chunkTok;                  // tokens stored per chunk
+  int *chunkTok;                  // tokens stored per chunk by quantize
+  int2 *chunkSpan;                // per chunk: first token slot, token count
+                                  // (with the zero-run tokens at its edges)
   unsigned *selHist;              // [n][kSelectBins]
   float *lloydHist;               // [n][kLloydBins][2] (count, sum)
   float *qtable;                  // quantizer tables
