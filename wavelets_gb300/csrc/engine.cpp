@@ -860,7 +860,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     ctx->launches += 1;
     if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 3; }
     mark(ctx, 5);
-    launch_quantize(b, b.coef, maxTable, s);
+    launch_quantize(b, b.coef, maxTable, maxS, s);
     mark(ctx, 6);
     launch_runs(b, s);
     ctx->launches += 2;

@@ -411,13 +411,15 @@ __device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups)
 }
 
 __global__ void __launch_bounds__(kThreads, 4)
-quantize_kernel(DevBatch b, const float *__restrict__ coef) {
+quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   constexpr int kWords = kChunk / kThreads;  // 16 words of 32 elements per warp
   constexpr int kSpan = 32 * kWords;         // elements per warp
   constexpr int kWarps = kThreads / 32;
   constexpr unsigned kAll = 0xffffffffu;
-  __shared__ unsigned hist[kMaxSymbols + 1];
-  extern __shared__ float tab[];  // quantizer table (Lloyd / log), sized by the launch
+  // sized by the launch: the quantizer table (Lloyd / log), then the counts
+  // of the batch's largest alphabet
+  extern __shared__ float tab[];
+  unsigned *hist = reinterpret_cast<unsigned *>(tab + histOff);
   __shared__ __align__(16) uint16_t sLut[kLutStride];
   // by warp region: candidate values, overwritten in place by the value list
   __shared__ __align__(16) float sX[kChunk];
@@ -792,10 +794,12 @@ void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
   lloyd_solve_kernel<<<b.n, 1024, kLloydSmem, s>>>(b);
 }
 
-void launch_quantize(DevBatch &b, const float *coef, int maxTable, cudaStream_t s) {
-  const int smem = maxTable * (int)sizeof(float);
-  raise_smem_limit(quantize_kernel, smem > 0 ? smem : 1);
-  quantize_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b, coef);
+void launch_quantize(DevBatch &b, const float *coef, int maxTable, int maxSymbols,
+                     cudaStream_t s) {
+  const int histOff = (maxTable + 3) & ~3;
+  const int smem = (histOff + maxSymbols + 1) * (int)sizeof(float);
+  raise_smem_limit(quantize_kernel, smem);
+  quantize_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b, coef, histOff);
 }
 
 void launch_runs(DevBatch &b, cudaStream_t s) { runs_kernel<<<b.n, 1024, 0, s>>>(b); }

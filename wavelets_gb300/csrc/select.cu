@@ -71,8 +71,9 @@ __device__ __forceinline__ void load_chunk(const float *src, int len, float (&v)
 
 // First digit (bits 31..20 of |c|) plus min, max and the two largest |c|.
 // A CTA takes kQuantGroup consecutive chunks of one cubelet (one histogram
-// flush per group) and loads the next chunk while it counts the current one.
-__global__ void __launch_bounds__(kThreads)
+// flush per group); a thread's 16 loads of a chunk are issued together, and
+// six CTAs per SM keep enough of them in flight.
+__global__ void __launch_bounds__(kThreads, 6)
 select_pass0(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kSelectBins];
   __shared__ unsigned sMin[kThreads / 32], sMax[kThreads / 32], sA1[kThreads / 32], sA2[kThreads / 32];
@@ -87,15 +88,13 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
   auto chunk_src = [&](int k) { return coef + cd.coefOff + (long long)(c0 + k) * kChunk; };
 
   for (int i = threadIdx.x; i < kSelectBins; i += kThreads) hist[i] = 0;
-  float v[kPerThread];
-  load_chunk(chunk_src(0), chunk_len(0), v);
   __syncthreads();
 
   unsigned mn = 0xffffffffu, mx = 0u, a1 = 0u, a2 = 0u;
   for (int k = 0; k < nc; k++) {
     const int len = chunk_len(k);
-    float vn[kPerThread];
-    if (k + 1 < nc) load_chunk(chunk_src(k + 1), chunk_len(k + 1), vn);
+    float v[kPerThread];
+    load_chunk(chunk_src(k), len, v);
 #pragma unroll
     for (int j = 0; j < kPerThread; j++) {
       if (chunk_index(j) >= len) continue;
@@ -105,8 +104,6 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
       mx = max(mx, ord_enc(v[j]));
       top2_merge(a1, a2, a, 0u);
     }
-#pragma unroll
-    for (int j = 0; j < kPerThread; j++) v[j] = vn[j];
   }
   for (int off = 16; off > 0; off >>= 1) {
     mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
@@ -148,7 +145,7 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
 // (|c| >> 20 == prefix) into the cubelet's candidate region, and add every
 // |c| above the bucket to the Lloyd histogram (those are above the threshold
 // whatever its low 20 bits turn out to be).  Chunk groups as in pass 0.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
 select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict__ cand) {
   __shared__ unsigned lh[kLloydBins];
   __shared__ unsigned wCnt[kThreads / 32];
@@ -168,16 +165,14 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
   auto chunk_src = [&](int k) { return coef + cd.coefOff + (long long)(c0 + k) * kChunk; };
   if (lloyd)
     for (int i = threadIdx.x; i < kLloydBins; i += kThreads) lh[i] = 0;
-  float v[kPerThread];
-  load_chunk(chunk_src(0), chunk_len(0), v);
   __syncthreads();
 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned *dst = cand + cd.coefOff;
   for (int k = 0; k < nc; k++) {
     const int len = chunk_len(k);
-    float vn[kPerThread];
-    if (k + 1 < nc) load_chunk(chunk_src(k + 1), chunk_len(k + 1), vn);
+    float v[kPerThread];
+    load_chunk(chunk_src(k), len, v);
     unsigned m = 0;  // candidates among this thread's values
 #pragma unroll
     for (int j = 0; j < kPerThread; j++) {
@@ -206,8 +201,6 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
 #pragma unroll
     for (int j = 0; j < kPerThread; j++)
       if ((m >> j) & 1u) dst[o++] = __float_as_uint(v[j]) & 0x7fffffffu;
-#pragma unroll
-    for (int j = 0; j < kPerThread; j++) v[j] = vn[j];
     __syncthreads();  // wCnt and sBase are reused by the next chunk
   }
   if (lloyd) {
