@@ -21,6 +21,8 @@
 // reference's lower_bound with its last-boundary special case.
 #include <cfloat>
 
+#include <type_traits>
+
 #include "wl_internal.h"
 
 namespace wl {
@@ -410,6 +412,21 @@ __device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups)
   }
 }
 
+// Tokens of a zero-bin run of L < 2^31 elements lying inside one chunk, in
+// the order of run_tokens (whole run, no window): runs of 1024, then one dup
+// token per set bit of the remainder above 8, then single zero-bin tokens.
+template <class F>
+__device__ __forceinline__ void run_tokens_short(int L, int dupKey, int dupV, F f) {
+  for (int j = L >> 10; j > 0; j--) f(make_token(dupKey, 7));
+  int r = L & 1023;
+  while (r > 8) {
+    const int lg = 31 - __clz(r);
+    f(make_token(dupKey, lg - 3));
+    r -= 1 << lg;
+  }
+  for (; r > 0; r--) f(make_token(dupV, 0));
+}
+
 __global__ void __launch_bounds__(kThreads, 4)
 quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   constexpr int kWords = kChunk / kThreads;  // 16 words of 32 elements per warp
@@ -440,8 +457,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int base = w * kSpan;
   const unsigned ltMask = (1u << lane) - 1u;
-  // zero-bin elements can be skipped only when they are coded as runs
-  const float zlo = dupV >= 0 ? -q.thr : 0.f, zhi = dupV >= 0 ? q.thr : 0.f;
+  // zero-bin elements (-thr < x < thr) can be skipped only when they are
+  // coded as runs; without runs every element is a candidate (|x| < 0 never)
+  const float zthr = dupV >= 0 ? q.thr : 0.f;
 
   for (int i = threadIdx.x; i < B + 1; i += kThreads) hist[i] = 0;
   for (int i = threadIdx.x; i < nTab; i += kThreads) tab[i] = b.qtable[cd.tableOff + i];
@@ -461,17 +479,19 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
 
     // ---- phase 1: candidates into the warp's region
     int nCand = 0;  // warp-uniform
-    {
+    auto phase1 = [&](auto full) {
+      constexpr bool kFull = decltype(full)::value;
       float x[kWords];
 #pragma unroll
       for (int j = 0; j < kWords; j++) {
         const int pos = base + 32 * j + lane;
-        x[j] = pos < len ? src[pos] : 0.f;
+        x[j] = (kFull || pos < len) ? src[pos] : 0.f;
       }
 #pragma unroll
       for (int j = 0; j < kWords; j++) {
         const int pos = base + 32 * j + lane;
-        const bool cand = pos < len && !(x[j] > zlo && x[j] < zhi);
+        // zero bin iff |x| < zthr (NaN is a candidate)
+        const bool cand = (kFull || pos < len) && !(fabsf(x[j]) < zthr);
         const unsigned m = __ballot_sync(kAll, cand);
         if (cand) {
           const int l = base + nCand + __popc(m & ltMask);
@@ -480,7 +500,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
         }
         nCand += __popc(m);
       }
-    }
+    };
+    if (len == kChunk) phase1(std::true_type());
+    else phase1(std::false_type());
     __syncwarp();
 
     // ---- phase 2: exact bins; values replace the candidates in place (a
@@ -593,7 +615,7 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
         if (hasV) {
           unsigned t = o + (unsigned)(inc - cnt);
           if (prev >= 0 && p - prev > 1)
-            run_tokens(prev + 1, p, prev + 1, p, B, dupV, [&](uint16_t tk) { dst[t++] = tk; });
+            run_tokens_short(p - prev - 1, B, dupV, [&](uint16_t tk) { dst[t++] = tk; });
           dst[t] = make_token(bin, 0);
         }
         o += (unsigned)__shfl_sync(kAll, inc, 31);
