@@ -639,7 +639,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   CU(cudaSetDevice(ctx->device));
   std::vector<Plan> plans(n);
   long long coefTotal = 0, chunkTotal = 0, inBytes = 0, wordsTotal = 0;
-  int tableTotal = 0, maxS = 2, maxTable = 0;
+  int tableTotal = 0, maxS = 2, maxTable = 0, maxLloyd = 3;
   bool anyLog = false, anyLloyd = false;
   for (int i = 0; i < n; i++) {
     const wl_cubelet &it = items[i];
@@ -686,6 +686,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     tableTotal += ((2 * pl.p.bin_count + 2) + 63) & ~63;
     maxS = std::max(maxS, pl.p.bin_count + 1);
     if (pl.p.quant_alg == WL_LLOYD) maxTable = std::max(maxTable, pl.p.bin_count);
+    if (pl.p.quant_alg == WL_LLOYD) maxLloyd = std::max(maxLloyd, pl.p.bin_count);
     if (pl.p.quant_alg == WL_LOG) maxTable = std::max(maxTable, 2 * pl.p.bin_count);
     if (pl.p.quant_alg == WL_LOG) anyLog = true;
     if (pl.p.quant_alg == WL_LLOYD) anyLloyd = true;
@@ -858,7 +859,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     CU(record(ctx, ctx->ev[2]));
     launch_quant_params(b, s);
     ctx->launches += 1;
-    if (anyLloyd) { launch_lloyd(b, b.coef, s); ctx->launches += 3; }
+    if (anyLloyd) { launch_lloyd(b, b.coef, maxLloyd, s); ctx->launches += 3; }
     mark(ctx, 5);
     launch_quantize(b, b.coef, maxTable, maxS, s);
     mark(ctx, 6);

@@ -163,15 +163,24 @@ lloyd_deferred_kernel(DevBatch b, const float *__restrict__ coef) {
     if (hist[i]) atomicAdd(&g[i], hist[i]);
 }
 
-// block-wide inclusive scan of doubles (1024 threads, 4 bins per thread)
-constexpr int kLloydSmem = 2 * (kLloydBins + 1) * 8 + 3 * (kMaxBins / 2 + 1) * 4;
+// 512 threads and shared memory sized for the batch's largest codebook:
+// four CTAs per SM, so a batch of up to 4 x 152 cubelets solves in one wave.
+constexpr int kSolveThreads = 512;
+// prefix sums: counts (exact in 32 bits) and count * centre (double), block
+// scan scratch, then the codebook, midpoints and next codebook (cbCap each)
+__host__ __device__ inline size_t lloyd_smem_bytes(int cbCap) {
+  return (size_t)(kLloydBins + 1) * 8 + (size_t)(kLloydBins + 2) * 4 + 64 * 8 +
+         (size_t)3 * cbCap * 4;
+}
 
-__global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kSolveThreads, 4) lloyd_solve_kernel(DevBatch b, int cbCap) {
   extern __shared__ double lsm[];
-  double *pw = lsm, *pwx = lsm + (kLloydBins + 1);
-  float *cb = reinterpret_cast<float *>(pwx + (kLloydBins + 1));
-  float *mid = cb + (kMaxBins / 2 + 1);
-  float *nxt = mid + (kMaxBins / 2 + 1);
+  double *pwx = lsm;
+  unsigned *pw = reinterpret_cast<unsigned *>(pwx + (kLloydBins + 1));
+  double *scratch = reinterpret_cast<double *>(pw + (kLloydBins + 2));
+  float *cb = reinterpret_cast<float *>(scratch + 64);
+  float *mid = cb + cbCap;
+  float *nxt = mid + cbCap;
   const int ci = blockIdx.x;
   const CubeletDev cd = b.cub[ci];
   if (cd.quantAlg != WL_LLOYD) return;
@@ -193,18 +202,20 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
   };
 
   // prefix sums of counts and count*centre; fixed order, so the codebook is
-  // deterministic: each thread sums 4 consecutive bins, then a block scan
+  // deterministic: each thread sums 8 consecutive bins, then a block scan
   {
-    const int per = kLloydBins / 1024;
-    double c4[per], x4[per], sc = 0, sx = 0;
-    for (int j = 0; j < per; j++) {
+    const int per = kLloydBins / kSolveThreads;
+    auto bin_at = [&](int j, double &c, double &x) {
       const int i = threadIdx.x * per + j;
-      const double c = degenerate ? 0.0 : (double)g[i];
-      const double x = (double)__uint_as_float(base + ((unsigned)i << shift) + half);
+      c = degenerate ? 0.0 : (double)g[i];
+      x = (double)__uint_as_float(base + ((unsigned)i << shift) + half);
+    };
+    double sc = 0, sx = 0;
+    for (int j = 0; j < per; j++) {
+      double c, x;
+      bin_at(j, c, x);
       sc += c;
       sx += c * x;
-      c4[j] = sc;
-      x4[j] = sx;
     }
     // inclusive warp scan of the per-thread totals
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -214,7 +225,7 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
       const double tx = __shfl_up_sync(0xffffffffu, ix, off);
       if (lane >= off) { ic += tc; ix += tx; }
     }
-    double *wc = reinterpret_cast<double *>(nxt);  // scratch before the iterations
+    double *wc = scratch;
     double *wx = wc + 32;
     if (lane == 31) { wc[wp] = ic; wx[wp] = ix; }
     __syncthreads();
@@ -223,33 +234,39 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
     bc += ic - sc;
     bx += ix - sx;
     if (threadIdx.x == 0) { pw[0] = 0; pwx[0] = 0; }
+    // the thread's running sums again, in the same order (same values)
+    double rc = 0, rx = 0;
     for (int j = 0; j < per; j++) {
+      double c, x;
+      bin_at(j, c, x);
+      rc += c;
+      rx += c * x;
       const int i = threadIdx.x * per + j;
-      pw[i + 1] = bc + c4[j];
-      pwx[i + 1] = bx + x4[j];
+      pw[i + 1] = (unsigned)(bc + rc);
+      pwx[i + 1] = bx + rx;
     }
     __syncthreads();
   }
   // initialLloydCodebook (test_compress_common.cc:749-779)
   if (cbs >= 1) {
     const float logScale = degenerate ? 0.f : __fdiv_rn(logf(__fdiv_rn(hi, lo)), (float)cbs);
-    for (int i = threadIdx.x; i < cbs; i += 1024) cb[i] = lo * expf(i * logScale);
+    for (int i = threadIdx.x; i < cbs; i += kSolveThreads) cb[i] = lo * expf(i * logScale);
   }
   __syncthreads();
   for (int it = 0; it < cd.lloydIters && !degenerate; it++) {
-    for (int i = threadIdx.x; i + 1 < cbs; i += 1024) mid[i] = 0.5f * (cb[i] + cb[i + 1]);
+    for (int i = threadIdx.x; i + 1 < cbs; i += kSolveThreads) mid[i] = 0.5f * (cb[i] + cb[i + 1]);
     __syncthreads();
     // cell i covers histogram bins [first(i), first(i+1)): first bin whose
     // centre is >= mid[i-1]
-    for (int i = threadIdx.x; i < cbs; i += 1024) {
+    for (int i = threadIdx.x; i < cbs; i += kSolveThreads) {
       const int a = i > 0 ? first_bin(mid[i - 1]) : 0;
       int z = i + 1 < cbs ? first_bin(mid[i]) : kLloydBins;
       if (z < a) z = a;
-      const double cw = pw[z] - pw[a];
+      const double cw = (double)(pw[z] - pw[a]);
       nxt[i] = cw > 0 ? (float)((pwx[z] - pwx[a]) / cw) : cb[i];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < cbs; i += 1024) cb[i] = nxt[i];
+    for (int i = threadIdx.x; i < cbs; i += kSolveThreads) cb[i] = nxt[i];
     __syncthreads();
   }
   // setBinsFromCodebook (test_compress_common.cc:784-846), one thread, the
@@ -303,7 +320,7 @@ __global__ void __launch_bounds__(1024) lloyd_solve_kernel(DevBatch b) {
     const float *bnd = b.qtable + cd.tableOff;
     const int nb = st->nBounds;
     uint16_t *lut = b.qlut + (size_t)ci * kLutStride;
-    for (int c = threadIdx.x; c < kLutCells; c += 1024) {
+    for (int c = threadIdx.x; c < kLutCells; c += kSolveThreads) {
       const float m = cell_min(c);  // NaN cells: never looked up; keep the table monotone
       lut[c] = (uint16_t)(m != m ? (c >= kLutCells / 2 ? nb : 0) : count_lt(bnd, nb, m));
     }
@@ -808,12 +825,14 @@ void launch_quant_params(DevBatch &b, cudaStream_t s) {
   quant_params_kernel<<<(b.n + 127) / 128, 128, 0, s>>>(b);
 }
 
-void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s) {
+void launch_lloyd(DevBatch &b, const float *coef, int maxBins, cudaStream_t s) {
   lloyd_cand_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(
       b, reinterpret_cast<const unsigned *>(b.coef2));
   lloyd_deferred_kernel<<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, coef);
-  raise_smem_limit(lloyd_solve_kernel, kLloydSmem);
-  lloyd_solve_kernel<<<b.n, 1024, kLloydSmem, s>>>(b);
+  const int cbCap = ((maxBins / 2 + 1) + 3) & ~3;
+  const int smem = (int)lloyd_smem_bytes(cbCap);
+  raise_smem_limit(lloyd_solve_kernel, smem);
+  lloyd_solve_kernel<<<b.n, kSolveThreads, smem, s>>>(b, cbCap);
 }
 
 void launch_quantize(DevBatch &b, const float *coef, int maxTable, int maxSymbols,

@@ -238,7 +238,7 @@ void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
 
 // launchers (quant.cu)
 void launch_quant_params(DevBatch &b, cudaStream_t s);
-void launch_lloyd(DevBatch &b, const float *coef, cudaStream_t s);
+void launch_lloyd(DevBatch &b, const float *coef, int maxBins, cudaStream_t s);
 void launch_quantize(DevBatch &b, const float *coef, int maxTable, int maxSymbols,
                      cudaStream_t s);
 void launch_runs(DevBatch &b, cudaStream_t s);
