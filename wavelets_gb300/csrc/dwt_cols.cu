@@ -309,6 +309,10 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   float *tile = reinterpret_cast<float *>(smem4);
   __shared__ long long rowIn[ROWS], rowOut[ROWS];
   __shared__ float scaleTab[32];
+  // band order of rows stored / loaded contiguously: band index q holds the
+  // in-place position p = bandPos[q] >> 4 of level bandPos[q] & 15, so lanes
+  // walk q (coalesced global accesses) instead of p
+  __shared__ uint16_t bandPos[kColsMaxL];
 
   const int bid = blockIdx.x;
   int lo = 0, hi = nPasses - 1;
@@ -343,6 +347,22 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   }
   if (threadIdx.x >= kThreadsC - 32 && lane <= S)
     scaleTab[lane] = lifting ? lifting_scale(lane, S) : 1.0f;
+  const bool bandRows = INV ? d.inSC == 1 : d.outSC == 1;
+  if (bandRows)
+    for (int q = threadIdx.x; q < L; q += kThreadsC) {
+      // inverse of pos_to_band: low band q < L >> S at q << S; detail band of
+      // level t (q in [L >> (t+1), L >> t)) at (1 << t) + (q - (L >> (t+1))) << (t+1)
+      int t = S, pos;
+      const int nLow = L >> S;
+      if (q < nLow) {
+        pos = q << S;
+      } else {
+        t = 0;
+        while (q < (L >> (t + 1))) t++;
+        pos = (1 << t) + ((q - (L >> (t + 1))) << (t + 1));
+      }
+      bandPos[q] = (uint16_t)((pos << 4) | t);
+    }
   __syncthreads();
 
   // ---- load ----------------------------------------------------------------
@@ -388,10 +408,9 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
         if (VEC && G == 32) c0 = load_row_vec(trow, src, cl + 1, lane, kP);
         for (int c = c0 + sub; c < L; c += G) stage(trow + c * kP, src + min(c, cl));
       } else {
-        for (int p = sub; p < L; p += G) {
-          int lev;
-          const int q = pos_to_band(p, L, S, lev);
-          trow[p * kP] = load_as_float(src + q) / scaleTab[lev];
+        for (int q = sub; q < L; q += G) {
+          const int e = bandPos[q];
+          trow[(e >> 4) * kP] = load_as_float(src + q) / scaleTab[e & 15];
         }
       }
     }
@@ -469,10 +488,9 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       if (base < 0) continue;
       const float *trow = tile + rr;
       if (!INV) {
-        for (int p = sub; p < L; p += G) {
-          int lev;
-          const int q = pos_to_band(p, L, S, lev);
-          store_from_float(out + base + q, trow[p * kP] * scaleTab[lev]);
+        for (int q = sub; q < L; q += G) {
+          const int e = bandPos[q];
+          store_from_float(out + base + q, trow[(e >> 4) * kP] * scaleTab[e & 15]);
         }
       } else {
         for (int c = sub; c < Lc; c += G) store_from_float(out + base + c, trow[c * kP]);
@@ -509,7 +527,8 @@ int dwt_cols_smem_bytes(int L, int rows) { return L * (rows + 1) * (int)sizeof(f
 // dynamic shared memory available beside the kernel's static arrays
 bool dwt_cols_rows_fit(int L, int rows) {
   if (rows != kRows && rows != 2 * kRows && rows != 4 * kRows) return false;  // any warps
-  const int kStatic = 2 * 4 * kRows * 8 + 32 * 4 + 1024;  // row bases, scales, reserve
+  // row bases, scales, band table, reserve
+  const int kStatic = 2 * 4 * kRows * 8 + 32 * 4 + kColsMaxL * 2 + 1024;
   return dwt_cols_smem_bytes(L, rows) <= 227 * 1024 - kStatic;
 }
 
