@@ -293,6 +293,59 @@ __device__ __forceinline__ int group_width(int len) {
   return G;
 }
 
+// 8- and 16-bit rows of device memory whose starts are all 4-byte aligned:
+// the lanes of a row load 32-bit words (W = 4 or 2 elements) of its first n
+// real elements, U rows per lane at once so that U loads are in flight
+// before the first store, and store the elements into the transposed tile
+// (lane l of a row starts at element (l W / 32) mod W of its word, so a
+// step's stores fall in different banks); the rest of each row (the last
+// partial word and the REPEAT padding up to L) is moved element by element.
+template <typename InT, int NW>
+__device__ __forceinline__ void load_rows_narrow(float *tile, const InT *in,
+                                                 const long long *rowIn, int nr, int L, int n,
+                                                 int pitch, int warp, int lane) {
+  constexpr int W = 4 / (int)sizeof(InT);
+  constexpr int U = 4;
+  const int nw = n / W;
+  const int G = group_width(nw > 0 ? nw : 1), rpi = 32 / G;
+  const int sub = lane & (G - 1), rsub = lane / G;
+  const int rot = (sub * W / 32) & (W - 1);
+  const int Ge = group_width(L), rpie = 32 / Ge, sube = lane & (Ge - 1), rsube = lane / Ge;
+  for (int rb = warp * rpi; rb < nr; rb += U * NW * rpi) {
+    for (int v0 = 0; v0 < nw; v0 += G) {
+      unsigned wv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int rr = rb + u * NW * rpi + rsub, v = v0 + sub;
+        wv[u] = (rr < nr && v < nw) ? reinterpret_cast<const unsigned *>(in + rowIn[rr])[v] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int rr = rb + u * NW * rpi + rsub, v = v0 + sub;
+        if (rr < nr && v < nw) {
+          float *dst = tile + rr + v * W * pitch;
+#pragma unroll
+          for (int k = 0; k < W; k++) {
+            const int idx = (k + rot) & (W - 1);
+            const unsigned e = (wv[u] >> (idx * 8 * (int)sizeof(InT))) &
+                               (sizeof(InT) == 1 ? 0xffu : 0xffffu);
+            dst[idx * pitch] = (float)e;
+          }
+        }
+      }
+    }
+  }
+  // elements nw W .. L-1 of every row (clamped to the last real element)
+  if (nw * W < L)
+    for (int rb = warp * rpie; rb < nr; rb += NW * rpie) {
+      const int rr = rb + rsube;
+      if (rr >= nr) continue;
+      const InT *src = in + rowIn[rr];
+      for (int c = nw * W + sube; c < L; c += Ge)
+        tile[rr + c * pitch] = load_as_float(src + min(c, n - 1));
+    }
+}
+
 // ROWS = 32, 64 or 128 rows, NW = 4 or 8 warps: warp w owns rows
 // 32 (w / kSegs) .. +31 of the tile and segment w % kSegs of every level of
 // them, kSegs = 32 NW / ROWS.
@@ -397,6 +450,13 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   } else {
     // contiguous rows: lanes over the elements of one row (G lanes per row)
     const int G = group_width(L), rpi = 32 / G, sub = lane & (G - 1), rsub = lane / G;
+    const bool narrowWords = !INV && !VEC && sizeof(InT) < 4 &&
+                             (reinterpret_cast<size_t>(in) & 3) == 0 &&
+                             ((d.inSA * (long long)sizeof(InT)) & 3) == 0 &&
+                             ((d.inSB * (long long)sizeof(InT)) & 3) == 0;
+    if (narrowWords)
+      load_rows_narrow<InT, NW>(tile, in, rowIn, nr, L, min(L, d.clampL), kP, warp, lane);
+    else
     for (int rb = warp * rpi; rb < nr; rb += NW * rpi) {
       const int rr = rb + rsub;
       if (rr >= nr) continue;
