@@ -359,6 +359,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile heights (profiling runs)")
+    ap.add_argument("--no-stream", action="store_true",
+                    help="skip the streamed two-lane end-to-end section (profiling runs)")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the serving measurement (0: skip)")
     args = ap.parse_args()
@@ -577,11 +579,14 @@ def main():
             srv.wait_batch(pending.pop(0)).release()
         return time.perf_counter() - t0
 
-    stream(4)
-    barrier()
-    st_s = gmax(stream(max(2, args.steps)))
-    barrier()
-    streamed_ms = st_s * 1e3 / max(2, args.steps)
+    if args.no_stream:
+        streamed_ms = e2e_ms
+    else:
+        stream(4)
+        barrier()
+        st_s = gmax(stream(max(2, args.steps)))
+        barrier()
+        streamed_ms = st_s * 1e3 / max(2, args.steps)
     srv.close()
     # the same through the Python API (list of Compressed objects per call)
     py_t = []
@@ -668,8 +673,10 @@ def main():
             "e2e": {"value": world * in_bytes / (streamed_ms / 1e3) / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
                     "ms_per_step": streamed_ms,
-                    "how": "wl_serve_submit_batch / wl_serve_wait_batch, two lanes, "
-                           "two batches in flight, inputs copied by the copy engine",
+                    "how": ("one synchronous wl_compress_batch per step (--no-stream)"
+                            if args.no_stream else
+                            "wl_serve_submit_batch / wl_serve_wait_batch, two lanes, "
+                            "two batches in flight, inputs copied by the copy engine"),
                     "single_call": {"value": world * in_bytes / (e2e_ms / 1e3) / 1e9,
                                     "ms_per_step": e2e_ms,
                                     "how": "one synchronous wl_compress_batch per step, "

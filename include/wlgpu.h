@@ -63,6 +63,10 @@ typedef struct {
   int lloyd_iters;          /* Lloyd iterations on the |coefficient| histogram */
   int exact_transform;      /* 1 = reference float operation order (filter bank);
                                0 = lifting (default) */
+  int transform_2d;         /* 1 = -2d: a 2-D transform of every z layer
+                               (test_compress_common.cc:519-541); x and y step
+                               counts below 1 mean the maximum, z steps only
+                               pad; the stored order stays x fastest */
 } wl_params;
 
 /* Fill p with the reference's defaults. */
@@ -92,6 +96,7 @@ typedef struct {
   float *boundaries, *values;
   void *owner;              /* library-internal: shared storage of the arrays
                                (NULL: each array is its own malloc block) */
+  int transform_2d;         /* 2-D mode: size is the padded (x, y, z), not rotated */
 } wl_result;
 
 void wl_result_free(wl_result *r);

@@ -66,10 +66,16 @@ def _axis(x: np.ndarray, steps: int, wavelet: int) -> np.ndarray:
     return x
 
 
-def forward(vol_zyx: np.ndarray, steps, wavelet: int = 2):
+def forward(vol_zyx: np.ndarray, steps, wavelet: int = 2, transform_2d: bool = False):
     """vol_zyx: (Z, Y, X) array of any dtype.  steps: (sx, sy, sz), negative
-    for the maximum.  Returns (flat float64 coefficients in the stored Z-X-Y
-    order, clamped steps)."""
+    for the maximum.  Returns (flat float64 coefficients in the stored order --
+    Z-X-Y, or x fastest in 2-D mode -- and the clamped steps).
+
+    2-D mode (-2d, test_compress_common.cc:519-541; cdf97_2d / haar_2d
+    dwt_cpu.cc:811-864, :495-547): every z layer gets its x levels, then its
+    y levels, with no axis rotation; a step count below 1 means the maximum
+    for the padded length, and layers whose padded size does not suit the
+    step counts are left as they are."""
     Z, Y, X = vol_zyx.shape
     st = []
     for s, n in zip(steps, (X, Y, Z)):
@@ -77,6 +83,16 @@ def forward(vol_zyx: np.ndarray, steps, wavelet: int = 2):
         st.append(m if s < 0 or s > m else s)
     Xp, Yp, Zp = (padded_length(n, s) for n, s in zip((X, Y, Z), st))
     v = np.pad(vol_zyx.astype(np.float64), ((0, Zp - Z), (0, Yp - Y), (0, Xp - X)), mode="edge")
+    if transform_2d:
+        if st == [0, 0, 0]:
+            return v.ravel(), tuple(st)
+        sx = st[0] if 1 <= st[0] <= ceil_log2(Xp) else ceil_log2(Xp)
+        sy = st[1] if 1 <= st[1] <= ceil_log2(Yp) else ceil_log2(Yp)
+        if Xp % (1 << sx) or Yp % (1 << sy):
+            return v.ravel(), tuple(st)
+        v = _axis(v, sx, wavelet)                                        # x
+        v = np.moveaxis(_axis(np.moveaxis(v, 1, 2).copy(), sy, wavelet), 2, 1)   # y
+        return v.ravel(), tuple(st)
     v = _axis(v, st[0], wavelet)                                    # x: last axis
     v = np.moveaxis(_axis(np.moveaxis(v, 1, 2).copy(), st[1], wavelet), 2, 1)   # y
     v = np.moveaxis(_axis(np.moveaxis(v, 0, 2).copy(), st[2], wavelet), 2, 0)   # z

@@ -635,7 +635,7 @@ void huffman_part(Encoded &e, int n, int binCount, int zeroBin) {
 // as Cube::copyToCubeletBuffer fills them (wavelet.cc:283-343).
 CubeletBuffer compressed_meta(const Encoded &e, int Xr, int Yr, int Zr,
                               int ox, int oy, int oz, int odt, int sx, int sy,
-                              int sz, int wavelet, float frac) {
+                              int sz, int wavelet, float frac, bool two_d) {
   CubeletBuffer m;
   m.set_width(Xr); m.set_height(Yr); m.set_depth(Zr);
   m.set_x_offset(0); m.set_y_offset(0); m.set_z_offset(0);
@@ -649,7 +649,7 @@ CubeletBuffer compressed_meta(const Encoded &e, int Xr, int Yr, int Zr,
   p->set_wavelet_transform_steps_y(sy);
   p->set_wavelet_transform_steps_z(sz);
   p->set_wavelet_algorithm((CompressionParametersBuffer_WaveletAlgorithm)wavelet);
-  p->set_transform_2d(false);
+  p->set_transform_2d(two_d);
   p->set_threshold_fraction(frac);
   p->set_threshold_value(e.r.threshold);
   p->set_quant_bin_count(e.r.bin_count);
@@ -717,10 +717,45 @@ void inverse3d(std::vector<float> &v, int X, int Y, int Z, int sx, int sy,
   each_row(v.data(), X, Y, Z, sx, row);
 }
 
+// 2-D transform of every z layer of a W x H x D cube (-2d; waveletTransform
+// test_compress_common.cc:519-541 -> cdf97_2d / haar_2d, dwt_cpu.cc:811-864 and
+// :495-547): step counts below 1 or above the maximum become the maximum
+// (ceilLog2 of the padded length); a layer whose padded size does not suit
+// those counts is left untransformed (the reference reports it and returns).
+// Rows along x, a transpose, rows along y, a transpose back: the layout
+// stays x fastest.
+void transform2d(std::vector<float> &v, int W, int H, int D, int sx, int sy, int wavelet,
+                 bool inverse) {
+  if (sx < 1 || sx > ceil_log2(W)) sx = ceil_log2(W);
+  if (sy < 1 || sy > ceil_log2(H)) sy = ceil_log2(H);
+  if ((W & ((1 << sx) - 1)) || (H & ((1 << sy) - 1))) return;
+  auto fwd = [wavelet](float *d, int len, int s, float *t) {
+    if (wavelet == ORC_HAAR) haar_row(d, len, s, t); else cdf97_row(d, len, s, t);
+  };
+  auto inv = [wavelet](float *d, int len, int s, float *t) {
+    if (wavelet == ORC_HAAR) haar_inv_row(d, len, s, t); else cdf97_inv_row(d, len, s, t);
+  };
+  std::vector<float> t((size_t)W * H);
+  for (int z = 0; z < D; z++) {
+    float *layer = v.data() + (size_t)z * W * H;
+    if (!inverse) {
+      each_row(layer, W, H, 1, sx, fwd);
+      transpose2d(layer, t.data(), W, H);  // [y][x] -> [x][y]
+      each_row(t.data(), H, W, 1, sy, fwd);
+      transpose2d(t.data(), layer, H, W);  // back to [y][x]
+    } else {
+      transpose2d(layer, t.data(), W, H);
+      each_row(t.data(), H, W, 1, sy, inv);
+      transpose2d(t.data(), layer, H, W);
+      each_row(layer, W, H, 1, sx, inv);
+    }
+  }
+}
+
 int compress_common(const void *data, int dtype, int X, int Y, int Z, int sx,
                     int sy, int sz, int wavelet, float frac, int binCount,
                     int qalg, int compressZeros, const char *out_path,
-                    orc_result *res) {
+                    orc_result *res, bool two_d = false) {
   // setWaveletSteps (test_compress_common.cc:362-374)
   int mx = ceil_log2(X), my = ceil_log2(Y), mz = ceil_log2(Z);
   if (sx < 0 || sx > mx) sx = mx;
@@ -731,15 +766,17 @@ int compress_common(const void *data, int dtype, int X, int Y, int Z, int sx,
   if (dtype == ORC_UINT8) load_padded((const uint8_t *)data, X, Y, Z, Xp, Yp, Zp, v);
   else if (dtype == ORC_INT32) load_padded((const int32_t *)data, X, Y, Z, Xp, Yp, Zp, v);
   else load_padded((const float *)data, X, Y, Z, Xp, Yp, Zp, v);
-  forward3d(v, Xp, Yp, Zp, sx, sy, sz, wavelet);
+  const bool any = !(sx == 0 && sy == 0 && sz == 0);
+  if (!two_d) forward3d(v, Xp, Yp, Zp, sx, sy, sz, wavelet);
+  else if (any) transform2d(v, Xp, Yp, Zp, sx, sy, wavelet, false);
   Encoded e;
   encode_coeffs(v.data(), (int)v.size(), frac, binCount, qalg, compressZeros, e);
   if (res) *res = e.r;
   if (!out_path) return 0;
-  bool rotated = !(sx == 0 && sy == 0 && sz == 0);
+  bool rotated = any && !two_d;
   CubeletBuffer m = compressed_meta(e, rotated ? Zp : Xp, rotated ? Xp : Yp,
                                     rotated ? Yp : Zp, X, Y, Z, dtype, sx, sy,
-                                    sz, wavelet, frac);
+                                    sz, wavelet, frac, two_d);
   std::string words((const char *)e.words.data(), e.words.size() * 4);
   return write_cube_file(out_path, {m}, {words}, false) ? 0 : 1;
 }
@@ -779,9 +816,11 @@ int decompress_file(const char *in_path, const char *out_path) {
                  p.quant_max_value(), vals.data(), v.data());
   int sx = p.wavelet_transform_steps_x(), sy = p.wavelet_transform_steps_y(),
       sz = p.wavelet_transform_steps_z();
-  bool rotated = !(sx == 0 && sy == 0 && sz == 0);
+  const bool any = !(sx == 0 && sy == 0 && sz == 0), two_d = p.transform_2d();
+  bool rotated = any && !two_d;
   int Xp = rotated ? H : W, Yp = rotated ? D : H, Zp = rotated ? W : D;
-  inverse3d(v, Xp, Yp, Zp, sx, sy, sz, p.wavelet_algorithm());
+  if (!two_d) inverse3d(v, Xp, Yp, Zp, sx, sy, sz, p.wavelet_algorithm());
+  else if (any) transform2d(v, Xp, Yp, Zp, sx, sy, p.wavelet_algorithm(), true);
   int ox = p.original_width(), oy = p.original_height(), oz = p.original_depth();
   int odt = p.has_original_data_type() ? p.original_data_type() : ORC_FLOAT32;
   // translateCubeDataToOriginal (test_compress_common.cc:699-746), cropped to
@@ -969,9 +1008,9 @@ int orc_compress_volume(const void *data, int dtype, int X, int Y, int Z,
 
 // Command line with the reference's flags (parseOptions,
 // test_compress_common.cc:73-192): -d -steps -thresh -qcount -wave -qalg
-// -noz -q (other reference flags are accepted and ignored).
+// -noz -2d -q (other reference flags are accepted and ignored).
 int orc_main(int argc, const char **argv) {
-  bool decompress = false, zeros = true;
+  bool decompress = false, zeros = true, two_d = false;
   int sx = -1, sy = -1, sz = -1, bins = 256, wave = ORC_CDF97, qalg = ORC_LOG;
   float frac = 0.5f;
   int i = 1;
@@ -979,6 +1018,7 @@ int orc_main(int argc, const char **argv) {
     std::string a = argv[i];
     if (a == "-d") decompress = true;
     else if (a == "-noz") zeros = false;
+    else if (a == "-2d") two_d = true;
     else if (a == "-q" || a == "-v" || a == "-err" || a == "-pb" || a == "-enc") {}
     else if (i + 1 < argc && a == "-steps") {
       int x = 1, y = 1, z = 1;
@@ -1016,7 +1056,7 @@ int orc_main(int argc, const char **argv) {
     int dt = c.meta.data_type();
     return compress_common(c.data.data(), dt, c.meta.width(), c.meta.height(),
                            c.meta.depth(), sx, sy, sz, wave, frac, bins, qalg,
-                           zeros, out, nullptr);
+                           zeros, out, nullptr, two_d);
   }
   return 1;
 }

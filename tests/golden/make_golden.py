@@ -38,7 +38,17 @@ PARAMS = {
     "p5": ["-wave", "haar", "-thresh", "0.8", "-qalg", "uniform", "-qcount", "7"],
     "p6": ["-steps", "0,0,0", "-thresh", "0.6", "-qalg", "log", "-qcount", "64"],
     "p7": ["-steps", "4,4,4", "-thresh", "0.9", "-qalg", "lloyd", "-qcount", "255"],
+    # -2d: a 2-D transform of every z layer (test_compress_common.cc:519-541)
+    "p8": ["-2d", "-steps", "-1", "-thresh", "0.8", "-qalg", "log", "-qcount", "256"],
+    "p9": ["-2d", "-wave", "haar", "-steps", "3,2", "-thresh", "0.9", "-qalg", "uniform",
+           "-qcount", "512"],
+    # x steps 0 mean the maximum in 2-D mode; z steps still pad the layers
+    "p10": ["-2d", "-steps", "0,2,3", "-thresh", "0.7", "-qalg", "log", "-qcount", "255"],
 }
+
+# extra -2d parameter sets per case
+PLANS_2D = {"uint8_1x64x64": ["p8", "p10"], "float32_12x20x24": ["p9"],
+            "uint8_5x7x9": ["p8", "p10"], "uint16_16x16x16": ["p8", "p9"]}
 
 # (case name, array, parameter sets)
 def cases():
@@ -48,7 +58,7 @@ def cases():
              ["p1", "p5"], ["p2", "p3", "p7"], ["p1", "p4"], ["p3", "p6"],
              ["p1", "p2", "p4"]]
     for (name, arr), plan in zip(small, plans):
-        out.append((name, arr, plan))
+        out.append((name, arr, plan + PLANS_2D.get(name, [])))
     rng = np.random.default_rng(11)
     img = synth.scaled_blob_cubelet(rng, (1, 256, 256), np.uint8)
     out.append(("uint8_1x256x256", img, ["p1", "p4"]))

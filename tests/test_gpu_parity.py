@@ -339,7 +339,7 @@ def test_transform_error_against_float64_lifting(ctx, case):
     from oracle import lifting64
     p = _params(case)
     coeffs, _ = ctx.forward_transform(_input(case), p)
-    ref, _ = lifting64.forward(_input(case), p.steps, p.wavelet)
+    ref, _ = lifting64.forward(_input(case), p.steps, p.wavelet, p.transform_2d)
     scale = float(np.abs(ref).max())
     if scale == 0:
         assert np.abs(coeffs).max() == 0
@@ -366,3 +366,39 @@ def test_full_size_transform_error_against_float64_lifting(ctx, shape, steps, wa
     print(f"transform error vs float64 lifting, {shape} {steps}: {err:.3e}")
     assert err <= FP64_RTOL
 
+
+
+@pytest.mark.parametrize("two_d_steps", [(-1, -1, -1), (3, 2, 0), (0, 2, 3), (4, 4, 1)])
+def test_2d_mode_batched_equals_single_and_round_trips(ctx, two_d_steps, tmp_path):
+    """-2d on the column-tile kernel (lifting): a batch of mixed sizes equals
+    each cubelet alone, the stored size is the padded (x, y, z), and the
+    restored volume is as close to the input as the reference path's own
+    round trip (oracle port, same flags)."""
+    rng = np.random.default_rng(31)
+    items = []
+    for i, shape in enumerate([(3, 64, 64), (5, 40, 24), (2, 17, 33), (4, 128, 96)]):
+        a = synth.scaled_blob_cubelet(rng, shape, [np.uint8, np.uint16, np.float32, np.uint8][i])
+        items.append((a, P.Params(steps=two_d_steps, transform_2d=True, threshold_fraction=0.5,
+                                  quant_alg=P.UNIFORM, bin_count=1024)))
+    batch = ctx.compress_batch(items)
+    flags = ["-2d", "-steps", ",".join(str(s) for s in two_d_steps), "-thresh", "0.5",
+             "-qalg", "uniform", "-qcount", "1024"]
+    for k, ((a, p), c) in enumerate(zip(items, batch)):
+        single = ctx.compress(a, p)
+        assert np.array_equal(single.words, c.words)
+        assert c.transform_2d
+        st = P.clamp_steps(p.steps, lib._size_of(a))
+        assert tuple(c.size) == tuple(P.padded_length(n, s) for n, s in zip(lib._size_of(a), st))
+        back = ctx.decompress(c).astype(np.float64)
+        x = a.astype(np.float64)
+        # the reference path's round trip (16-bit data travels as INT32)
+        inp, outp, decp = (str(tmp_path / f"{k}.{e}.cube") for e in ("in", "o", "d"))
+        src = a.astype(np.int32) if a.dtype == np.uint16 else a
+        cubefile.write_file(inp, [cubefile.from_array(src)])
+        assert oracle.main(flags + [inp, outp]) == 0
+        assert oracle.main(["-d", outp, decp]) == 0
+        ref = cubefile.read_file(decp)[0].array().astype(np.float64)
+        rms_gpu = float(np.sqrt(np.mean((back - x) ** 2)))
+        rms_ref = float(np.sqrt(np.mean((ref - x) ** 2)))
+        span = float(x.max() - x.min()) or 1.0
+        assert rms_gpu <= 1.02 * rms_ref + 1e-3 * span, (k, rms_gpu, rms_ref)

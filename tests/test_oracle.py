@@ -99,7 +99,7 @@ def test_float64_lifting_agrees_with_reference_coefficients(case):
     from wavelets_gb300 import params as P
     p, _, _ = P.parse_flags(MANIFEST["params"][case["params"]])
     a = cubefile.read_file(os.path.join(GOLDEN, case["input"]))[0].array()
-    got, st = lifting64.forward(a, p.steps, p.wavelet)
+    got, st = lifting64.forward(a, p.steps, p.wavelet, p.transform_2d)
     assert [int(s) for s in case["stats"]["steps"]] == list(st)
     ref = np.fromfile(os.path.join(GOLDEN, case["coeffs"]), np.float32).astype(np.float64)
     assert got.shape == ref.shape

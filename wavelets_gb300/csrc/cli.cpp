@@ -4,9 +4,9 @@
 //
 // Flags and defaults follow parseOptions / printHelp
 // (test_compress_common.cc:35-192): -d, -steps, -thresh, -qcount, -wave,
-// -qalg, -noz, -q, -v; -exact selects the reference float order for the
+// -qalg, -noz, -2d, -q, -v; -exact selects the reference float order for the
 // CDF 9/7 transform (bit-identical output files).  Flags of the reference
-// that only print diagnostics (-err, -pb, -enc, -bq, -aq, -opt, -2d) are
+// that only print diagnostics (-err, -pb, -enc, -bq, -aq, -opt) are
 // rejected with a message rather than silently ignored.
 #include <chrono>
 #include <cstdio>
@@ -28,6 +28,7 @@ static void help() {
           "    -wave <wavelet> : haar or cdf97 (default = cdf97)\n"
           "    -qalg <algorithm> : uniform, log, or lloyd (default = log)\n"
           "    -noz : disable compression of long strings of zeros\n"
+          "    -2d : rather than 3d transform, do 2d transform at each layer\n"
           "    -exact : CDF9/7 in the reference's float order\n"
           "    -q : be quiet\n\n");
   exit(1);
@@ -49,6 +50,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(a, "-v")) {}
     else if (!strcmp(a, "-noz")) p.compress_zeros = 0;
     else if (!strcmp(a, "-exact")) p.exact_transform = 1;
+    else if (!strcmp(a, "-2d")) p.transform_2d = 1;
     else if (!strcmp(a, "-steps")) {
       const char *v = need();
       int x = 1, y = 1, z = 1;

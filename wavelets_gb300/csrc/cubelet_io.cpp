@@ -100,7 +100,7 @@ std::string encode_params(const CubeMeta &m) {
   put_int(o, 15, m.original_size[1]);
   put_int(o, 16, m.original_size[2]);
   if (m.original_data_type > 0) put_int(o, 17, m.original_data_type);
-  put_int(o, 18, 0);  // transform_2d = false
+  put_int(o, 18, m.transform_2d ? 1 : 0);  // transform_2d
   if (m.dup_key >= 0) put_int(o, 19, m.dup_key);
   if (m.dup_value >= 0) put_int(o, 20, m.dup_value);
   return o;
@@ -136,7 +136,7 @@ bool decode_params(In r, CubeMeta &m) {
       case 15: m.original_size[1] = (int)r.varint(); break;
       case 16: m.original_size[2] = (int)r.varint(); break;
       case 17: m.original_data_type = (int)r.varint(); break;
-      case 18: r.varint(); break;
+      case 18: m.transform_2d = r.varint() != 0; break;
       case 19: m.dup_key = (int32_t)r.varint(); break;
       case 20: m.dup_value = (int32_t)r.varint(); break;
       default: r.skip(w);

@@ -23,6 +23,7 @@ struct CubeMeta {
   // compression parameters (compressed cubelets only)
   int steps[3] = {0, 0, 0};
   int wavelet = 2;
+  bool transform_2d = false;
   float threshold_fraction = 0, threshold_value = 0;
   int bin_count = 0;
   int pb_quant_alg = kPbLog;

@@ -63,6 +63,8 @@ struct Plan {
   int tableOff;
   bool identity;       // all steps zero: no transform, no axis rotation
   bool cols;           // transform runs on the column-tile kernel
+  bool two_d;          // -2d: x and y levels of every z layer, no rotation
+  int sx2, sy2;        // 2-D mode: x / y levels actually applied
   long long pitchY, pitchZ;  // source elements between rows / slices
 };
 
@@ -454,8 +456,64 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   zs[group_key(true, WL_F32, f.L)].push_back(f);
 }
 
+// 2-D mode (cdf97_2d / haar_2d, dwt_cpu.cc:811-864 and :495-547): x and y
+// step counts below 1 or above the maximum become the maximum for the padded
+// length; false when the padded size does not suit them (the reference then
+// leaves the layers untransformed).
+bool twod_steps(int Xp, int Yp, int sx, int sy, int &sx2, int &sy2) {
+  const int mx = ceil_log2((unsigned)Xp), my = ceil_log2((unsigned)Yp);
+  sx2 = (sx < 1 || sx > mx) ? mx : sx;
+  sy2 = (sy < 1 || sy > my) ? my : sy;
+  return Xp % (1 << sx2) == 0 && Yp % (1 << sy2) == 0;
+}
+
+// 2-D mode passes (both kernels): x pass raw x-y-z (REPEAT clamp) -> coef2 in
+// [z][x][y] (y fastest), y pass [z][x][y] -> coef in [z][y][x], the stored
+// order (x fastest).  Both read rows contiguous in memory.
+void forward_passes_2d(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
+                       PassGroups &xs, PassGroups &ys) {
+  const int big = 0x7fffffff;
+  const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
+  const bool exact = pl.p.exact_transform && pl.p.wavelet == WL_CDF97;
+  PassDesc d;
+  memset(&d, 0, sizeof d);
+  d.cropL = d.cropB = d.cropA = big;
+  d.wavelet = pl.p.wavelet;
+  d.exact = pl.p.exact_transform;
+  // x pass: rows (a = z, b = y) of the source
+  d.in = in;
+  d.vecLoad = pl.cols && hostIn ? 1 : 0;
+  d.inSA = pl.pitchZ; d.inSB = pl.pitchY; d.inSC = 1;
+  d.clampL = pl.X; d.clampA = pl.Z; d.clampB = pl.Y;
+  d.L = pl.Xp; d.B = pl.Yp; d.rows = (int)(Yp * Zp);
+  d.out = coef2 + pl.coefOff;
+  d.outSA = Xp * Yp; d.outSB = 1; d.outSC = Yp;
+  d.steps = pl.sx2;
+  d.T = pl.cols ? dwt_cols_tile_rows(d.L) : dwt_tile_rows(d.L, exact);
+  d.tiles = (d.rows + d.T - 1) / d.T;
+  xs[group_key(pl.cols, pl.dtype, d.L, pl.cols && hostIn && dtype_size(pl.dtype) < 4)]
+      .push_back(d);
+  // y pass: rows (a = z, b = x) of [z][x][y]
+  PassDesc e = d;
+  e.clampL = e.clampA = e.clampB = big;
+  e.vecLoad = 0;
+  e.in = coef2 + pl.coefOff;
+  e.inSA = Xp * Yp; e.inSB = Yp; e.inSC = 1;
+  e.L = pl.Yp; e.B = pl.Xp; e.rows = (int)(Xp * Zp);
+  e.out = coef + pl.coefOff;
+  e.outSA = Xp * Yp; e.outSB = 1; e.outSC = Xp;
+  e.steps = pl.sy2;
+  e.T = pl.cols ? dwt_cols_tile_rows(e.L) : dwt_tile_rows(e.L, exact);
+  e.tiles = (e.rows + e.T - 1) / e.T;
+  ys[group_key(pl.cols, WL_F32, e.L)].push_back(e);
+}
+
 void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
                     PassGroups &xs, PassGroups &ys, PassGroups &zs) {
+  if (pl.two_d && !pl.identity) {
+    forward_passes_2d(pl, in, hostIn, coef, coef2, xs, ys);
+    return;
+  }
   if (pl.cols) {
     forward_passes_cols(pl, in, hostIn, coef, coef2, xs, ys, zs);
     return;
@@ -667,7 +725,16 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     pl.Yp = padded_length(pl.Y, pl.sy);
     pl.Zp = padded_length(pl.Z, pl.sz);
     pl.identity = pl.sx == 0 && pl.sy == 0 && pl.sz == 0;
-    pl.cols = use_cols(pl.Xp, pl.Yp, pl.Zp, pl.identity, pl.p);
+    pl.two_d = pl.p.transform_2d != 0;
+    pl.sx2 = pl.sy2 = 0;
+    if (pl.two_d) {
+      if (!pl.identity && !twod_steps(pl.Xp, pl.Yp, pl.sx, pl.sy, pl.sx2, pl.sy2))
+        pl.identity = true;  // the reference leaves such layers as they are
+      pl.cols = !pl.identity && !(pl.p.exact_transform && pl.p.wavelet == WL_CDF97) &&
+                pl.Xp <= kColsMaxL && pl.Yp <= kColsMaxL;
+    } else {
+      pl.cols = use_cols(pl.Xp, pl.Yp, pl.Zp, pl.identity, pl.p);
+    }
     if (pl.Xp > kMaxAxis || pl.Yp > kMaxAxis || pl.Zp > kMaxAxis)
       return fail(ctx, WL_EINVAL, "cubelet %d: padded axis length above %d", i, kMaxAxis);
     pl.n = (long long)pl.Xp * pl.Yp * pl.Zp;
@@ -926,7 +993,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       const long long v[] = {pl.dtype | (hostIn[i] << 8), pl.X, pl.Y, pl.Z, pl.pitchY, pl.pitchZ,
                              q.steps[0], q.steps[1], q.steps[2], q.wavelet, (long long)fb,
                              q.bin_count, q.quant_alg, q.compress_zeros, q.lloyd_iters,
-                             q.exact_transform};
+                             q.exact_transform, q.transform_2d};
       key.insert(key.end(), v, v + sizeof v / sizeof v[0]);
     }
     ge = graph_for(ctx, std::move(key));
@@ -939,7 +1006,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     if ((size_t)pl.n > coefCap) return fail(ctx, WL_EINVAL, "coefficient buffer too small");
     CU(cudaMemcpyAsync(coefOut, b.coef + pl.coefOff, (size_t)pl.n * 4, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
-    if (pl.identity) { storedSize[0] = pl.Xp; storedSize[1] = pl.Yp; storedSize[2] = pl.Zp; }
+    if (pl.identity || pl.two_d) { storedSize[0] = pl.Xp; storedSize[1] = pl.Yp; storedSize[2] = pl.Zp; }
     else { storedSize[0] = pl.Zp; storedSize[1] = pl.Xp; storedSize[2] = pl.Yp; }
     return WL_OK;
   }
@@ -1038,7 +1105,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     const CubeletState &st = hs[i];
     wl_result &r = outs[i];
     memset(&r, 0, sizeof r);
-    if (pl.identity) { r.size[0] = pl.Xp; r.size[1] = pl.Yp; r.size[2] = pl.Zp; }
+    r.transform_2d = pl.two_d ? 1 : 0;
+    if (pl.identity || pl.two_d) { r.size[0] = pl.Xp; r.size[1] = pl.Yp; r.size[2] = pl.Zp; }
     else { r.size[0] = pl.Zp; r.size[1] = pl.Xp; r.size[2] = pl.Yp; }
     r.original_size[0] = pl.X; r.original_size[1] = pl.Y; r.original_size[2] = pl.Z;
     r.original_dtype = pl.dtype;
@@ -1116,12 +1184,16 @@ int inverse_passes_cols(int Xp, int Yp, int Zp, const int orig[3], const int ste
 // Inverse transform of the coefficients already in ctx->coef (stored order)
 // into out (original size, outType), then synchronize.
 wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int wavelet,
-                       const int original_size[3], int outType, void *out, int outOnDevice) {
+                       const int original_size[3], int outType, void *out, int outOnDevice,
+                       bool two_d = false) {
   cudaStream_t s = ctx->stream;
-  const bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
-  const int Xp = identity ? size[0] : size[1];
-  const int Yp = identity ? size[1] : size[2];
-  const int Zp = identity ? size[2] : size[0];
+  bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
+  const bool unrotated = identity || two_d;
+  const int Xp = unrotated ? size[0] : size[1];
+  const int Yp = unrotated ? size[1] : size[2];
+  const int Zp = unrotated ? size[2] : size[0];
+  int sx2 = 0, sy2 = 0;
+  if (two_d && !identity && !twod_steps(Xp, Yp, steps[0], steps[1], sx2, sy2)) identity = true;
   const int X = original_size[0], Y = original_size[1], Z = original_size[2];
   const size_t outBytes = (size_t)X * Y * Z * dtype_size(outType);
   if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, outBytes));
@@ -1140,7 +1212,26 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
   wp.wavelet = wavelet;
   // descriptors of up to three passes, uploaded in one copy
   std::vector<GroupLaunch> gl;
-  if (use_cols(Xp, Yp, Zp, identity, wp)) {
+  if (two_d && !identity) {
+    // x levels first ([z][y][x] -> [z][x][y]), then y levels into the output
+    // (the reference undoes y first; the 1-D transforms along different axes
+    // commute, so this differs from its order only by float rounding), both
+    // reading rows contiguous in memory
+    const bool cols = Xp <= kColsMaxL && Yp <= kColsMaxL;
+    PassDesc a = mk();
+    a.in = c1; a.inSA = (long long)Xp * Yp; a.inSB = Xp; a.inSC = 1;
+    a.out = c2; a.outSA = (long long)Xp * Yp; a.outSB = 1; a.outSC = Yp;
+    a.L = Xp; a.B = Yp; a.rows = Yp * Zp; a.steps = sx2;
+    a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
+    TRY(stage_group(ctx, {a}, hoff, kTuneInvY, WL_F32, WL_F32, true, cols, false, gl));
+    PassDesc b = mk();
+    b.in = c2; b.inSA = (long long)Xp * Yp; b.inSB = Yp; b.inSC = 1;
+    b.out = dst; b.outSA = (long long)X * Y; b.outSB = 1; b.outSC = X;
+    b.cropL = Y; b.cropA = Z; b.cropB = X;
+    b.L = Yp; b.B = Xp; b.rows = Xp * Zp; b.steps = sy2;
+    b.T = dwt_tile_rows(b.L, exactCdf); b.tiles = (b.rows + b.T - 1) / b.T;
+    TRY(stage_group(ctx, {b}, hoff, kTuneInvX, WL_F32, outType, true, cols, false, gl));
+  } else if (use_cols(Xp, Yp, Zp, identity, wp)) {
     PassDesc d[3];
     const int np = inverse_passes_cols(Xp, Yp, Zp, original_size, steps, wavelet, c1, c2, dst, d);
     for (int i = 0; i < np; i++)
@@ -1183,11 +1274,11 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
 }
 
 wl_status check_sizes(wl_ctx *ctx, const int size[3], const int steps[3], const int orig[3],
-                      long long &n) {
-  const bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
-  const int Xp = identity ? size[0] : size[1];
-  const int Yp = identity ? size[1] : size[2];
-  const int Zp = identity ? size[2] : size[0];
+                      long long &n, bool two_d = false) {
+  const bool unrotated = two_d || (steps[0] == 0 && steps[1] == 0 && steps[2] == 0);
+  const int Xp = unrotated ? size[0] : size[1];
+  const int Yp = unrotated ? size[1] : size[2];
+  const int Zp = unrotated ? size[2] : size[0];
   for (int a = 0; a < 3; a++)
     if (steps[a] < 0 || steps[a] > 30) return fail(ctx, WL_EFORMAT, "bad step count");
   if (orig[0] < 1 || orig[1] < 1 || orig[2] < 1 || orig[0] > Xp || orig[1] > Yp || orig[2] > Zp)
@@ -1203,7 +1294,7 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
   if (!r || !out) return fail(ctx, WL_EINVAL, "null argument");
   if (dtype_size(outType) == 0) return fail(ctx, WL_EINVAL, "bad output dtype %d", outType);
   long long n;
-  TRY(check_sizes(ctx, r->size, r->steps, r->original_size, n));
+  TRY(check_sizes(ctx, r->size, r->steps, r->original_size, n, r->transform_2d != 0));
   if (r->size[0] > kMaxAxis || r->size[1] > kMaxAxis || r->size[2] > kMaxAxis)
     return fail(ctx, WL_EINVAL, "axis length above %d", kMaxAxis);
   if (r->bin_count < 2 || r->bin_count > kMaxBins) return fail(ctx, WL_EFORMAT, "bad bin count");
@@ -1247,7 +1338,7 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
                  r->bin_count, s);
   CU(cudaGetLastError());
   return inverse_impl(ctx, r->size, r->steps, r->wavelet, r->original_size, outType, out,
-                      outOnDevice);
+                      outOnDevice, r->transform_2d != 0);
 }
 
 // ---- tile autotuner -------------------------------------------------------------
@@ -1376,6 +1467,7 @@ wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
 
 wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
   m.width = r->size[0]; m.height = r->size[1]; m.depth = r->size[2];
+  m.transform_2d = r->transform_2d != 0;
   m.data_type = kPbInt32;
   m.compressed = true;
   m.steps[0] = r->steps[0]; m.steps[1] = r->steps[1]; m.steps[2] = r->steps[2];
@@ -1413,6 +1505,7 @@ void wl_params_default(wl_params *p) {
   p->compress_zeros = 1;
   p->lloyd_iters = 20;
   p->exact_transform = 0;
+  p->transform_2d = 0;
 }
 
 void wl_result_free(wl_result *r) {
@@ -1591,6 +1684,7 @@ wl_status wl_decompress_file(wl_ctx *ctx, const char *inPath, const char *outPat
     r.original_dtype = odt;
     r.steps[0] = m.steps[0]; r.steps[1] = m.steps[1]; r.steps[2] = m.steps[2];
     r.wavelet = m.wavelet;
+    r.transform_2d = m.transform_2d ? 1 : 0;
     r.quant_alg = m.pb_quant_alg == kPbUniform ? WL_UNIFORM : m.pb_quant_alg == kPbLog ? WL_LOG : WL_LLOYD;
     r.bin_count = m.bin_count;
     r.threshold_fraction = m.threshold_fraction;

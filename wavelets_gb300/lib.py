@@ -35,7 +35,8 @@ class WlParams(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int * 3), ("wavelet", ctypes.c_int),
                 ("threshold_fraction", ctypes.c_float), ("bin_count", ctypes.c_int),
                 ("quant_alg", ctypes.c_int), ("compress_zeros", ctypes.c_int),
-                ("lloyd_iters", ctypes.c_int), ("exact_transform", ctypes.c_int)]
+                ("lloyd_iters", ctypes.c_int), ("exact_transform", ctypes.c_int),
+                ("transform_2d", ctypes.c_int)]
 
 
 class WlResult(ctypes.Structure):
@@ -52,7 +53,7 @@ class WlResult(ctypes.Structure):
                 ("n_boundaries", ctypes.c_int), ("n_values", ctypes.c_int),
                 ("boundaries", ctypes.POINTER(ctypes.c_float)),
                 ("values", ctypes.POINTER(ctypes.c_float)),
-                ("owner", ctypes.c_void_p)]
+                ("owner", ctypes.c_void_p), ("transform_2d", ctypes.c_int)]
 
 
 class WlCubelet(ctypes.Structure):
@@ -185,6 +186,7 @@ def make_params(p: Optional[P.Params] = None) -> WlParams:
     w.compress_zeros = 1 if p.compress_zeros else 0
     w.lloyd_iters = int(p.lloyd_iters)
     w.exact_transform = 1 if p.exact_transform else 0
+    w.transform_2d = 1 if getattr(p, "transform_2d", False) else 0
     return w
 
 
@@ -211,6 +213,7 @@ class Compressed:
     decode: np.ndarray
     boundaries: np.ndarray
     values: np.ndarray
+    transform_2d: bool = False  # 2-D mode: size is the padded (x, y, z), not rotated
 
     @classmethod
     def from_struct(cls, r: WlResult) -> "Compressed":
@@ -226,7 +229,7 @@ class Compressed:
                    r.dup_key, r.dup_value, r.longest_code,
                    arr(r.words, r.n_words, np.uint32), arr(r.decode, r.n_decode, np.int32),
                    arr(r.boundaries, r.n_boundaries, np.float32),
-                   arr(r.values, r.n_values, np.float32))
+                   arr(r.values, r.n_values, np.float32), bool(r.transform_2d))
 
     def to_struct(self):
         """A WlResult pointing into this object's arrays (keep self alive)."""
@@ -242,6 +245,7 @@ class Compressed:
         r.min_coef, r.max_coef = self.min_coef, self.max_coef
         r.zero_bin, r.dup_key, r.dup_value = self.zero_bin, self.dup_key, self.dup_value
         r.longest_code = self.longest_code
+        r.transform_2d = 1 if self.transform_2d else 0
         self._keep = [np.ascontiguousarray(self.words, np.uint32),
                       np.ascontiguousarray(self.decode, np.int32),
                       np.ascontiguousarray(self.boundaries, np.float32),
@@ -405,7 +409,8 @@ def adopt_results(lib, outs, n) -> List["Compressed"]:
             f["dup_value"][i], f["longest_code"][i],
             base[o[0]:z[0]].view(np.uint32), base[o[1]:z[1]].view(np.int32),
             base[o[2]:z[2]].view(np.float32) if z[2] > o[2] else e32,
-            base[o[3]:z[3]].view(np.float32) if z[3] > o[3] else ef))
+            base[o[3]:z[3]].view(np.float32) if z[3] > o[3] else ef,
+            bool(f["transform_2d"][i])))
     return res
 
 

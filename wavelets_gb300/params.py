@@ -48,6 +48,7 @@ class Params:
     compress_zeros: bool = True
     lloyd_iters: int = 20            # Lloyd-on-histogram iterations
     exact_transform: bool = False    # reference float order instead of lifting
+    transform_2d: bool = False       # -2d: a 2-D transform of every z layer
 
 
 def parse_flags(args):
@@ -62,7 +63,9 @@ def parse_flags(args):
             decompress = True
         elif a == "-noz":
             p.compress_zeros = False
-        elif a in ("-q", "-v", "-err", "-pb", "-enc", "-opt", "-2d"):
+        elif a == "-2d":
+            p.transform_2d = True
+        elif a in ("-q", "-v", "-err", "-pb", "-enc", "-opt"):
             pass
         elif a == "-exact":
             p.exact_transform = True
