@@ -270,6 +270,36 @@ int wl_last_launch_count(const wl_ctx *ctx);
 wl_status wl_set_profiling(wl_ctx *ctx, int on);
 wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
 
+/* ---- Parameter sweep (-opt) -----------------------------------------------
+ * The reference's -opt (optimizeParameters -> plotAll, optimize.cc:96-133;
+ * testParameters optimize_cpu.cc:47-130), on the GPU: for every threshold
+ * fraction f = 0.50, 0.51, ... < 0.999 (float steps of 0.01) and bin count
+ * b = 100, (int)(b * 1.1), ... <= 2000, log quantization of the cubelet's
+ * coefficients with the threshold at sorted |c| index (int)(count * f):
+ * size_bytes = the Huffman-coded size as the reference counts it
+ * (totalEncodedLengthBytes, huffman.cc:241-251: the code bits of every token,
+ * zero-run tokens with their 3 length bits, in 32-bit words) and
+ * psnr = 10 log10(255^2 / mse) of the restored 8-bit cubelet against the
+ * input (computeErrorRatesAfterDequant, test_compress_common.cc:616-694).
+ * 8-bit input only, like the reference (test_compress_cpu.cc:106-114); the
+ * transform follows params (steps, wavelet, exact_transform, transform_2d)
+ * and compress_zeros selects zero-run tokens.  *n_points receives the number
+ * of grid points (1600); points may be NULL to ask for it.  Difference: a
+ * threshold whose sorted |c| is exactly 0 is taken as 1e-16, as the
+ * compression path does (the reference's sweep would use 0). */
+typedef struct {
+  float threshold_fraction;
+  int bin_count;
+  int size_bytes;
+  float psnr;
+} wl_opt_point;
+wl_status wl_optimize(wl_ctx *ctx, const void *data, const int size[3], int data_on_device,
+                      const wl_params *params, wl_opt_point *points, int cap, int *n_points);
+/* The same on the first uncompressed cubelet of a .cube file (the
+ * reference's `test_compress_cpu -opt in out`, which writes no output). */
+wl_status wl_optimize_file(wl_ctx *ctx, const char *in_path, const wl_params *params,
+                           wl_opt_point *points, int cap, int *n_points);
+
 /* ---- Tile autotuner ------------------------------------------------------
  * No reference counterpart (the reference's GPU transform has fixed block
  * shapes, dwt_gpu.cu).  The column-tile transform runs the rows of each size

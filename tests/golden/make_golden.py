@@ -10,8 +10,9 @@ the reference.
 
 Writes, per case: ``<case>.in.cube`` (input), ``<case>.<p>.cube`` (reference
 compressed output), ``<case>.<p>.d.cube`` (reference decompression of it),
-``<case>.<p>.coeffs.f32`` (reference transform output, rotated Z-X-Y order)
-and ``manifest.json`` (flags, sizes, threshold statistics, hashes).
+``<case>.<p>.coeffs.f32`` (reference transform output, rotated Z-X-Y order),
+``<case>.<o>.opt.txt`` (the table the reference's -opt sweep prints) and
+``manifest.json`` (flags, sizes, threshold statistics, hashes).
 """
 import hashlib
 import json
@@ -45,6 +46,11 @@ PARAMS = {
     # x steps 0 mean the maximum in 2-D mode; z steps still pad the layers
     "p10": ["-2d", "-steps", "0,2,3", "-thresh", "0.7", "-qalg", "log", "-qcount", "255"],
 }
+
+# -opt sweeps (optimizeParameters -> plotAll): the printed table is the fixture
+OPT = {"o1": ["-opt"], "o2": ["-opt", "-2d", "-steps", "3,2"],
+       "o3": ["-opt", "-noz", "-wave", "haar", "-steps", "2,2,2"]}
+OPT_CASES = {"uint8_1x64x64": ["o1", "o2", "o3"], "uint8_2x33x17": ["o1"]}
 
 # extra -2d parameter sets per case
 PLANS_2D = {"uint8_1x64x64": ["p8", "p10"], "float32_12x20x24": ["p9"],
@@ -132,6 +138,18 @@ def main():
                     "coeffs": f"{name}.{p}.coeffs.f32",
                     "stats": stats,
                     "sha256": {"output": sha(out), "decompressed": sha(dec)}})
+        manifest["opt"] = {"params": OPT, "cases": []}
+        for name, plan in OPT_CASES.items():
+            inp = os.path.join(HERE, name + ".in.cube")
+            for o in plan:
+                txt = os.path.join(HERE, f"{name}.{o}.opt.txt")
+                r = subprocess.run([cli, "-q", *OPT[o], inp, os.path.join(tmp, "none.cube")],
+                                   capture_output=True, text=True, check=True)
+                with open(txt, "w") as f:
+                    f.write(r.stdout)
+                manifest["opt"]["cases"].append({"case": name, "params": o,
+                                                 "input": os.path.basename(inp),
+                                                 "table": os.path.basename(txt)})
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     print("wrote", len(manifest["cases"]), "cases")

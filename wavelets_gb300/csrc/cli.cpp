@@ -4,9 +4,9 @@
 //
 // Flags and defaults follow parseOptions / printHelp
 // (test_compress_common.cc:35-192): -d, -steps, -thresh, -qcount, -wave,
-// -qalg, -noz, -2d, -q, -v; -exact selects the reference float order for the
-// CDF 9/7 transform (bit-identical output files).  Flags of the reference
-// that only print diagnostics (-err, -pb, -enc, -bq, -aq, -opt) are
+// -qalg, -noz, -2d, -opt, -q, -v; -exact selects the reference float order
+// for the CDF 9/7 transform (bit-identical output files).  Flags of the
+// reference that only print diagnostics (-err, -pb, -enc, -bq, -aq) are
 // rejected with a message rather than silently ignored.
 #include <chrono>
 #include <cstdio>
@@ -29,6 +29,7 @@ static void help() {
           "    -qalg <algorithm> : uniform, log, or lloyd (default = log)\n"
           "    -noz : disable compression of long strings of zeros\n"
           "    -2d : rather than 3d transform, do 2d transform at each layer\n"
+          "    -opt : print the threshold / bin count sweep (8-bit input; no output)\n"
           "    -exact : CDF9/7 in the reference's float order\n"
           "    -q : be quiet\n\n");
   exit(1);
@@ -37,7 +38,7 @@ static void help() {
 int main(int argc, char **argv) {
   wl_params p;
   wl_params_default(&p);
-  bool decompress = false, quiet = false;
+  bool decompress = false, quiet = false, optimize = false;
   int i = 1;
   for (; i < argc && argv[i][0] == '-'; i++) {
     const char *a = argv[i];
@@ -51,6 +52,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(a, "-noz")) p.compress_zeros = 0;
     else if (!strcmp(a, "-exact")) p.exact_transform = 1;
     else if (!strcmp(a, "-2d")) p.transform_2d = 1;
+    else if (!strcmp(a, "-opt")) optimize = true;
     else if (!strcmp(a, "-steps")) {
       const char *v = need();
       int x = 1, y = 1, z = 1;
@@ -95,6 +97,26 @@ int main(int argc, char **argv) {
     return 1;
   }
   auto t0 = std::chrono::steady_clock::now();
+  if (optimize && !decompress) {
+    // the reference's plotAll table (optimize.cc:96-122); no output file
+    int n = 0;
+    wl_status st = wl_optimize_file(ctx, argv[i], &p, nullptr, 0, &n);
+    wl_opt_point *pts = st == WL_OK ? new wl_opt_point[n] : nullptr;
+    if (st == WL_OK) st = wl_optimize_file(ctx, argv[i], &p, pts, n, &n);
+    if (st != WL_OK) {
+      fprintf(stderr, "error: %s\n", wl_last_error(ctx));
+      delete[] pts;
+      wl_destroy(ctx);
+      return 1;
+    }
+    printf("Threshold\tBins\tsize\tpSNR\n");
+    for (int k = 0; k < n; k++)
+      printf("%.3f\t%d\t%d\t%.6g\n", pts[k].threshold_fraction, pts[k].bin_count,
+             pts[k].size_bytes, pts[k].psnr);
+    delete[] pts;
+    wl_destroy(ctx);
+    return 0;
+  }
   wl_status st = decompress ? wl_decompress_file(ctx, argv[i], argv[i + 1])
                             : wl_compress_file(ctx, argv[i], argv[i + 1], &p);
   auto t1 = std::chrono::steady_clock::now();

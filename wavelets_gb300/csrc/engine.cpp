@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -203,7 +204,7 @@ struct wl_ctx {
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
-      words, passes, logHdr, outbuf, decWords, decTable, decWs, meta;
+      words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr;
   HostBuf hState, hWords, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
   // and replay it from then on
@@ -1465,6 +1466,77 @@ wl_status autotune_impl(wl_ctx *ctx, int maxLen, int reps) {
   return WL_OK;
 }
 
+// ---- parameter sweep (-opt) ------------------------------------------------------
+// optimizeParameters -> plotAll (optimize.cc:96-133): every threshold fraction
+// 0.50, 0.51, ... (float steps) below 0.999 with every bin count 100, 110, ...
+// ((int)(b * 1.1)) up to 2000, log quantization; each point's Huffman-coded
+// size and the PSNR of the restored bytes.  A
+// row of bin counts is one batched compression of the same device-resident
+// cubelet; each point is then restored on the device and compared there.
+wl_status optimize_impl(wl_ctx *ctx, const void *data, const int size[3], int onDevice,
+                        const wl_params &base, wl_opt_point *pts, int cap, int *count) {
+  std::vector<float> fracs;
+  for (float f = .5f; f < .999f; f += 0.01f) fracs.push_back(f);
+  std::vector<int> binsList;
+  for (int b = 100; b <= 2000; b = (int)(b * 1.1)) binsList.push_back(b);
+  const int total = (int)(fracs.size() * binsList.size());
+  if (count) *count = total;
+  if (!pts) return WL_OK;
+  if (cap < total) return fail(ctx, WL_EINVAL, "room for %d points, %d needed", cap, total);
+  TRY(check_params(ctx, base));
+  CU(cudaSetDevice(ctx->device));
+  const long long N = (long long)size[0] * size[1] * size[2];
+  if (size[0] < 1 || size[1] < 1 || size[2] < 1) return fail(ctx, WL_EINVAL, "empty size");
+  TRY(ensure(ctx, ctx->optIn, (size_t)N));
+  TRY(ensure(ctx, ctx->optOut, (size_t)N));
+  TRY(ensure(ctx, ctx->optErr, 16));
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemcpyAsync(ctx->optIn.p, data, (size_t)N,
+                     onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  const int m = (int)binsList.size();
+  std::vector<wl_cubelet> items(m);
+  std::vector<wl_result> outs(m);
+  int k = 0;
+  for (float f : fracs) {
+    for (int i = 0; i < m; i++) {
+      wl_cubelet &c = items[i];
+      memset(&c, 0, sizeof c);
+      c.data = ctx->optIn.p;
+      c.dtype = WL_U8;
+      c.size[0] = size[0]; c.size[1] = size[1]; c.size[2] = size[2];
+      c.params = base;
+      c.params.threshold_fraction = f;
+      c.params.bin_count = binsList[i];
+      c.params.quant_alg = WL_LOG;
+    }
+    TRY(compress_impl(ctx, items.data(), m, 1, outs.data()));
+    wl_status st = WL_OK;
+    for (int i = 0; i < m && st == WL_OK; i++) {
+      st = decompress_impl(ctx, &outs[i], WL_U8, ctx->optOut.p, 1);
+      if (st != WL_OK) break;
+      launch_sq_err_u8(P<uint8_t>(ctx->optIn), P<uint8_t>(ctx->optOut), N,
+                       P<unsigned long long>(ctx->optErr), s);
+      unsigned long long sq = 0;
+      cudaError_t e = cudaMemcpyAsync(&sq, ctx->optErr.p, 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) { st = fail(ctx, WL_ECUDA, "sweep error sum: %s", cudaGetErrorString(e)); break; }
+      // ErrorAccumulator::getPeakSignalToNoiseRatio (test_compress_common.h:148-153)
+      const float mse = (float)((double)sq / (double)N);
+      wl_opt_point &pt = pts[k + i];
+      pt.threshold_fraction = f;
+      pt.bin_count = binsList[i];
+      // totalEncodedLengthBytes (huffman.cc:241-251): every token's code,
+      // dup tokens with their length bits, in 32-bit words -- the stream
+      pt.size_bytes = outs[i].n_words * 4;
+      pt.psnr = mse == 0.f ? 0.f : 10.f * log10f(255.f * 255.f / mse);
+    }
+    for (wl_result &r : outs) wl_result_free(&r);
+    if (st != WL_OK) return st;
+    k += m;
+  }
+  return WL_OK;
+}
+
 wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
   m.width = r->size[0]; m.height = r->size[1]; m.depth = r->size[2];
   m.transform_2d = r->transform_2d != 0;
@@ -1567,7 +1639,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->state,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkCub, &ctx->groupCub,
-                   &ctx->chunkSpan,
+                   &ctx->chunkSpan, &ctx->optIn, &ctx->optOut, &ctx->optErr,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
                    &ctx->meta};
@@ -1662,6 +1734,27 @@ wl_status wl_compress_file(wl_ctx *ctx, const char *inPath, const char *outPath,
   return fail(ctx, WL_EFORMAT, "No uncompressed cubelets in the input data.");
 }
 
+wl_status wl_optimize_file(wl_ctx *ctx, const char *inPath, const wl_params *params,
+                           wl_opt_point *points, int cap, int *n_points) {
+  if (!ctx || !inPath || !params) return fail(ctx, WL_EINVAL, "null argument");
+  std::string buf, err;
+  if (!read_whole_file(inPath, buf)) return fail(ctx, WL_EIO, "cannot read %s", inPath);
+  std::vector<CubeMeta> metas;
+  std::vector<std::string> datas;
+  if (!decode_file(buf, metas, datas, err)) return fail(ctx, WL_EFORMAT, "%s: %s", inPath, err.c_str());
+  for (size_t i = 0; i < metas.size(); i++) {
+    const CubeMeta &m = metas[i];
+    if (m.compressed) continue;
+    // the reference's sweep takes 8-bit data only (test_compress_cpu.cc:107)
+    if (m.data_type != kPbUint8) return fail(ctx, WL_EINVAL, "-opt needs 8-bit data");
+    if (datas[i].size() < (size_t)m.width * m.height * m.depth)
+      return fail(ctx, WL_EFORMAT, "cubelet data truncated");
+    int size[3] = {m.width, m.height, m.depth};
+    return wl_optimize(ctx, datas[i].data(), size, 0, params, points, cap, n_points);
+  }
+  return fail(ctx, WL_EFORMAT, "No uncompressed cubelets in the input data.");
+}
+
 wl_status wl_decompress_file(wl_ctx *ctx, const char *inPath, const char *outPath) {
   if (!ctx || !inPath || !outPath) return fail(ctx, WL_EINVAL, "null argument");
   std::string buf, err;
@@ -1745,6 +1838,12 @@ wl_status wl_inverse_transform(wl_ctx *ctx, const float *coeffs, const int store
   TRY(ensure(ctx, ctx->coef2, n * 4 + 256));
   CU(cudaMemcpyAsync(ctx->coef.p, coeffs, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
   return inverse_impl(ctx, stored, steps, wavelet, orig, outType, out, 0);
+}
+
+wl_status wl_optimize(wl_ctx *ctx, const void *data, const int size[3], int data_on_device,
+                      const wl_params *params, wl_opt_point *points, int cap, int *n_points) {
+  if (!ctx || !data || !size || !params) return fail(ctx, WL_EINVAL, "null argument");
+  return optimize_impl(ctx, data, size, data_on_device, *params, points, cap, n_points);
 }
 
 wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps) {

@@ -239,6 +239,9 @@ void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
 // launchers (quant.cu)
 void launch_quant_params(DevBatch &b, cudaStream_t s);
 void launch_lloyd(DevBatch &b, const float *coef, int maxBins, cudaStream_t s);
+// sum of squared differences of two u8 arrays into *out (opt.cu)
+void launch_sq_err_u8(const uint8_t *a, const uint8_t *b, long long n, unsigned long long *out,
+                      cudaStream_t s);
 void launch_quantize(DevBatch &b, const float *coef, int maxTable, int maxSymbols,
                      cudaStream_t s);
 void launch_runs(DevBatch &b, cudaStream_t s);

@@ -76,6 +76,11 @@ class WlRequest(ctypes.Structure):
                 ("out", ctypes.c_void_p), ("out_on_device", ctypes.c_int)]
 
 
+class WlOptPoint(ctypes.Structure):
+    _fields_ = [("threshold_fraction", ctypes.c_float), ("bin_count", ctypes.c_int),
+                ("size_bytes", ctypes.c_int), ("psnr", ctypes.c_float)]
+
+
 class WlRequestInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("queue_ms", ctypes.c_double),
                 ("service_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
@@ -140,6 +145,13 @@ EXPORTS = {
     "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_serve_destroy": (None, [ctypes.c_void_p]),
     "wl_results_free": (None, [ctypes.POINTER(WlResult), ctypes.c_int]),
+    "wl_optimize": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                   ctypes.c_int, ctypes.POINTER(WlParams),
+                                   ctypes.POINTER(WlOptPoint), ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_int)]),
+    "wl_optimize_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p,
+                                        ctypes.POINTER(WlParams), ctypes.POINTER(WlOptPoint),
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "wl_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "wl_tune_export": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t,
                                       ctypes.POINTER(ctypes.c_size_t)]),
@@ -605,6 +617,20 @@ class Context:
         the table as text (see tune_table)."""
         self._check(self.lib.wl_autotune(self.h, int(max_len), int(reps)))
         return tune_table()
+
+    def optimize(self, arr: np.ndarray, params: Optional[P.Params] = None):
+        """The reference's -opt sweep on an 8-bit cubelet: a list of
+        (threshold fraction, bin count, size in bytes, PSNR)."""
+        a = np.ascontiguousarray(arr, np.uint8)
+        sz = (ctypes.c_int * 3)(*_size_of(a))
+        n = ctypes.c_int()
+        prm = make_params(params)
+        self._check(self.lib.wl_optimize(self.h, ctypes.c_void_p(a.ctypes.data), sz, 0,
+                                         ctypes.byref(prm), None, 0, ctypes.byref(n)))
+        pts = (WlOptPoint * n.value)()
+        self._check(self.lib.wl_optimize(self.h, ctypes.c_void_p(a.ctypes.data), sz, 0,
+                                         ctypes.byref(prm), pts, n.value, ctypes.byref(n)))
+        return [(p.threshold_fraction, p.bin_count, p.size_bytes, p.psnr) for p in pts]
 
     def set_host_input_mode(self, mode: int):
         """0: read page-locked host inputs in place; 1: copy them with the
