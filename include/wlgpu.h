@@ -270,6 +270,31 @@ int wl_last_launch_count(const wl_ctx *ctx);
 wl_status wl_set_profiling(wl_ctx *ctx, int on);
 wl_status wl_kernel_timings(const wl_ctx *ctx, float out[9]);
 
+/* ---- Whole containers -------------------------------------------------------
+ * Every cubelet of a .cube file compressed into a new .cube file (or every
+ * compressed cubelet restored), in order, with the index footer
+ * (cubelet_file.cc:303-327) and each cubelet's x/y/z offset kept.  The
+ * reference compresses only the first cubelet of a file per run
+ * (test_compress_common.cc:296-302).  Reading, GPU work and writing overlap:
+ * a reader thread fills one of two page-locked buffers of batch_bytes
+ * (0 = 256 MiB) while the GPU compresses the other as one batch, and a writer
+ * thread appends finished batches.  Cubelets already in the target form are
+ * copied unchanged.  16-bit data travels in .cube files as INT32, as the
+ * reference stores it. */
+typedef struct {
+  int cubelets;                 /* written */
+  int copied;                   /* of those, copied unchanged */
+  unsigned long long bytes_in;  /* cubelet data read */
+  unsigned long long bytes_out; /* cubelet data written */
+  double seconds;               /* wall time of the call */
+  double read_seconds, compute_seconds, write_seconds; /* busy time per stage */
+} wl_container_stats;
+wl_status wl_compress_container(wl_ctx *ctx, const char *in_path, const char *out_path,
+                                const wl_params *params, size_t batch_bytes,
+                                wl_container_stats *stats);
+wl_status wl_decompress_container(wl_ctx *ctx, const char *in_path, const char *out_path,
+                                  size_t batch_bytes, wl_container_stats *stats);
+
 /* ---- Parameter sweep (-opt) -----------------------------------------------
  * The reference's -opt (optimizeParameters -> plotAll, optimize.cc:96-133;
  * testParameters optimize_cpu.cc:47-130), on the GPU: for every threshold

@@ -153,9 +153,9 @@ std::string encode_meta(const CubeMeta &m, uint64_t data_file_offset) {
   put_int(o, 1, m.width);
   put_int(o, 2, m.height);
   put_int(o, 3, m.depth);
-  put_int(o, 4, 0);
-  put_int(o, 5, 0);
-  put_int(o, 6, 0);
+  put_int(o, 4, m.offset[0]);
+  put_int(o, 5, m.offset[1]);
+  put_int(o, 6, m.offset[2]);
   put_int(o, 7, m.data_type);
   put_int(o, 8, (int64_t)m.byte_count);
   put_int(o, 9, m.compressed ? 2 : 0);
@@ -176,6 +176,9 @@ bool decode_meta(const void *buf, size_t n, CubeMeta &m) {
       case 1: m.width = (int)r.varint(); break;
       case 2: m.height = (int)r.varint(); break;
       case 3: m.depth = (int)r.varint(); break;
+      case 4: m.offset[0] = (int)r.varint(); break;
+      case 5: m.offset[1] = (int)r.varint(); break;
+      case 6: m.offset[2] = (int)r.varint(); break;
       case 7: m.data_type = (int)r.varint(); break;
       case 8: m.byte_count = r.varint(); break;
       case 9: m.compressed = r.varint() == 2; break;

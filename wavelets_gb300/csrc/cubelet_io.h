@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include "wlgpu.h"
+
 namespace wl {
 
 constexpr const char *kCubeHeader = "SCU cubelets 1.0\n";
@@ -16,6 +18,7 @@ constexpr int kPbLog = 1, kPbUniform = 2, kPbLloyd = 3;
 // CubeletBuffer + CompressionParametersBuffer fields used by this path.
 struct CubeMeta {
   int width = 0, height = 0, depth = 0;
+  int offset[3] = {0, 0, 0};    // position in the parent volume (x, y, z)
   int data_type = 0;            // wire DataType
   uint64_t byte_count = 0;
   int32_t maximum_value = 0;
@@ -42,6 +45,10 @@ std::string encode_file(const std::vector<CubeMeta> &metas,
 bool decode_file(const std::string &buf, std::vector<CubeMeta> &metas,
                  std::vector<std::string> &datas, std::string &err);
 bool read_whole_file(const char *path, std::string &out);
+// conversions between a compressed cubelet's metadata and a wl_result
+// (engine.cpp); meta_to_result points the result's arrays into m and words
+wl_status result_to_meta(const wl_result *r, CubeMeta &m);
+void meta_to_result(CubeMeta &m, const std::string &words, wl_result &r);
 bool write_whole_file(const char *path, const std::string &data);
 
 }  // namespace wl

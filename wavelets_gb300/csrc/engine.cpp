@@ -1537,6 +1537,9 @@ wl_status optimize_impl(wl_ctx *ctx, const void *data, const int size[3], int on
   return WL_OK;
 }
 
+}  // namespace
+
+namespace wl {
 wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
   m.width = r->size[0]; m.height = r->size[1]; m.depth = r->size[2];
   m.transform_2d = r->transform_2d != 0;
@@ -1562,6 +1565,39 @@ wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
   m.dup_value = r->dup_value;
   return WL_OK;
 }
+
+// A wl_result over a compressed cubelet's metadata and words (the arrays stay
+// in m and words).
+void meta_to_result(CubeMeta &m, const std::string &words, wl_result &r) {
+  memset(&r, 0, sizeof r);
+  r.size[0] = m.width; r.size[1] = m.height; r.size[2] = m.depth;
+  r.original_size[0] = m.original_size[0];
+  r.original_size[1] = m.original_size[1];
+  r.original_size[2] = m.original_size[2];
+  r.original_dtype = m.original_data_type == kPbUint8 ? WL_U8
+                     : m.original_data_type == kPbInt32 ? WL_I32 : WL_F32;
+  r.steps[0] = m.steps[0]; r.steps[1] = m.steps[1]; r.steps[2] = m.steps[2];
+  r.wavelet = m.wavelet;
+  r.transform_2d = m.transform_2d ? 1 : 0;
+  r.quant_alg = m.pb_quant_alg == kPbUniform ? WL_UNIFORM : m.pb_quant_alg == kPbLog ? WL_LOG : WL_LLOYD;
+  r.bin_count = m.bin_count;
+  r.threshold_fraction = m.threshold_fraction;
+  r.threshold_value = m.threshold_value;
+  r.max_value = m.quant_max_value;
+  r.dup_key = m.dup_key;
+  r.dup_value = m.dup_value;
+  r.n_words = (int)(words.size() / 4);
+  r.words = (uint32_t *)const_cast<char *>(words.data());
+  r.n_decode = (int)m.decode.size();
+  r.decode = m.decode.data();
+  r.n_values = (int)m.values.size();
+  r.values = m.values.data();
+  r.n_boundaries = (int)m.boundaries.size();
+  r.boundaries = m.boundaries.data();
+}
+}  // namespace wl
+
+namespace {
 
 }  // namespace
 
@@ -1767,30 +1803,8 @@ wl_status wl_decompress_file(wl_ctx *ctx, const char *inPath, const char *outPat
     CubeMeta &m = metas[i];
     if (!m.compressed || m.data_type != kPbInt32) continue;
     wl_result r;
-    memset(&r, 0, sizeof r);
-    r.size[0] = m.width; r.size[1] = m.height; r.size[2] = m.depth;
-    r.original_size[0] = m.original_size[0];
-    r.original_size[1] = m.original_size[1];
-    r.original_size[2] = m.original_size[2];
-    int odt = m.original_data_type == kPbUint8 ? WL_U8
-              : m.original_data_type == kPbInt32 ? WL_I32 : WL_F32;
-    r.original_dtype = odt;
-    r.steps[0] = m.steps[0]; r.steps[1] = m.steps[1]; r.steps[2] = m.steps[2];
-    r.wavelet = m.wavelet;
-    r.transform_2d = m.transform_2d ? 1 : 0;
-    r.quant_alg = m.pb_quant_alg == kPbUniform ? WL_UNIFORM : m.pb_quant_alg == kPbLog ? WL_LOG : WL_LLOYD;
-    r.bin_count = m.bin_count;
-    r.threshold_fraction = m.threshold_fraction;
-    r.threshold_value = m.threshold_value;
-    r.max_value = m.quant_max_value;
-    r.dup_key = m.dup_key;
-    r.dup_value = m.dup_value;
-    r.n_words = (int)(datas[i].size() / 4);
-    r.words = (uint32_t *)const_cast<char *>(datas[i].data());
-    r.n_decode = (int)m.decode.size();
-    r.decode = m.decode.data();
-    r.n_values = (int)m.values.size();
-    r.values = m.values.data();
+    meta_to_result(m, datas[i], r);
+    const int odt = r.original_dtype;
     if (r.original_size[0] == 0) {
       return fail(ctx, WL_EFORMAT, "compressed cubelet lacks its original size");
     }

@@ -76,6 +76,13 @@ class WlRequest(ctypes.Structure):
                 ("out", ctypes.c_void_p), ("out_on_device", ctypes.c_int)]
 
 
+class WlContainerStats(ctypes.Structure):
+    _fields_ = [("cubelets", ctypes.c_int), ("copied", ctypes.c_int),
+                ("bytes_in", ctypes.c_ulonglong), ("bytes_out", ctypes.c_ulonglong),
+                ("seconds", ctypes.c_double), ("read_seconds", ctypes.c_double),
+                ("compute_seconds", ctypes.c_double), ("write_seconds", ctypes.c_double)]
+
+
 class WlOptPoint(ctypes.Structure):
     _fields_ = [("threshold_fraction", ctypes.c_float), ("bin_count", ctypes.c_int),
                 ("size_bytes", ctypes.c_int), ("psnr", ctypes.c_float)]
@@ -145,6 +152,12 @@ EXPORTS = {
     "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_serve_destroy": (None, [ctypes.c_void_p]),
     "wl_results_free": (None, [ctypes.POINTER(WlResult), ctypes.c_int]),
+    "wl_compress_container": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                             ctypes.POINTER(WlParams), ctypes.c_size_t,
+                                             ctypes.POINTER(WlContainerStats)]),
+    "wl_decompress_container": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p,
+                                               ctypes.c_char_p, ctypes.c_size_t,
+                                               ctypes.POINTER(WlContainerStats)]),
     "wl_optimize": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                    ctypes.c_int, ctypes.POINTER(WlParams),
                                    ctypes.POINTER(WlOptPoint), ctypes.c_int,
@@ -631,6 +644,23 @@ class Context:
         self._check(self.lib.wl_optimize(self.h, ctypes.c_void_p(a.ctypes.data), sz, 0,
                                          ctypes.byref(prm), pts, n.value, ctypes.byref(n)))
         return [(p.threshold_fraction, p.bin_count, p.size_bytes, p.psnr) for p in pts]
+
+    def compress_container(self, in_path: str, out_path: str, params=None,
+                           batch_bytes: int = 0) -> dict:
+        """Compress every cubelet of a .cube file into a new .cube file
+        (reading, GPU work and writing overlapped); returns the stage times."""
+        st = WlContainerStats()
+        self._check(self.lib.wl_compress_container(self.h, in_path.encode(), out_path.encode(),
+                                                   ctypes.byref(make_params(params)),
+                                                   int(batch_bytes), ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in WlContainerStats._fields_}
+
+    def decompress_container(self, in_path: str, out_path: str, batch_bytes: int = 0) -> dict:
+        """Restore every compressed cubelet of a .cube file into a new one."""
+        st = WlContainerStats()
+        self._check(self.lib.wl_decompress_container(self.h, in_path.encode(), out_path.encode(),
+                                                     int(batch_bytes), ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in WlContainerStats._fields_}
 
     def set_host_input_mode(self, mode: int):
         """0: read page-locked host inputs in place; 1: copy them with the
