@@ -19,6 +19,10 @@
 // its maximum value.
 #include <cuda_runtime.h>
 
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -80,6 +84,7 @@ struct Item {
   const char *staged = nullptr;  // data in a staging buffer, or null
   size_t bytes = 0;
   std::string own;               // data read outside the staging buffers
+  long long fileOff = 0;         // where the data starts in the input file
   bool through = false;          // copied to the output unchanged
   // the cubelet's data (taken when used: `own` moves with the item)
   const char *data() const { return staged ? staged : own.data(); }
@@ -101,25 +106,19 @@ int wl_type(int pb) {
 }
 int elem_size(int pb) { return pb == kPbUint8 ? 1 : 4; }
 
-// Page-locked double buffer shared by the reader and the compute stage.
+// Page-locked double buffer shared by the reader and the compute stage (the
+// context's, kept across calls: page-locking hundreds of MB per call would
+// cost more than the transfers).
 struct Staging {
   char *buf[2] = {nullptr, nullptr};
   size_t cap = 0;
   bool busy[2] = {false, false};
   std::mutex mu;
   std::condition_variable cv;
-  ~Staging() {
-    for (char *b : buf)
-      if (b) cudaFreeHost(b);
-  }
-  bool init(size_t bytes) {
+  bool init(wl_ctx *ctx, size_t bytes) {
     cap = bytes;
-    for (char *&b : buf)
-      if (cudaHostAlloc(reinterpret_cast<void **>(&b), cap, cudaHostAllocDefault) != cudaSuccess) {
-        cudaGetLastError();
-        b = nullptr;
-        return false;
-      }
+    for (int i = 0; i < 2; i++)
+      if (!(buf[i] = ctx_staging(ctx, i, bytes))) return false;
     return true;
   }
   void acquire(int i) {
@@ -151,16 +150,64 @@ struct Shared {
 
 // Reader: parse the input container into batches.  restoring: compressed
 // cubelets are the work (read into `own`), uncompressed ones are copied;
-// compressing: uncompressed cubelets go to the staging buffers.
+// compressing: uncompressed cubelets go to the staging buffers.  The
+// metadata is parsed in order (the data is skipped); a batch's data is then
+// read by several threads at once (pread at the known offsets), which moves
+// a page-cached file several times faster than one thread.
+struct ReadTask {
+  long long off;
+  char *dst;
+  size_t bytes;
+};
+
+bool read_parallel(int fd, std::vector<ReadTask> &tasks) {
+  if (tasks.empty()) return true;
+  size_t total = 0;
+  for (const ReadTask &t : tasks) total += t.bytes;
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nThreads = (int)std::min<size_t>({(size_t)std::min(hw, 8), tasks.size(),
+                                               total / (1 << 20) + 1});
+  // split into pieces of at most 8 MB so that one large cubelet spreads too
+  std::vector<ReadTask> pieces;
+  for (const ReadTask &t : tasks)
+    for (size_t o = 0; o < t.bytes; o += (8 << 20))
+      pieces.push_back({t.off + (long long)o, t.dst + o, std::min<size_t>(8 << 20, t.bytes - o)});
+  std::atomic<size_t> next{0};
+  std::atomic<bool> ok{true};
+  auto work = [&]() {
+    for (size_t k; (k = next.fetch_add(1)) < pieces.size();) {
+      const ReadTask &t = pieces[k];
+      size_t done = 0;
+      while (done < t.bytes) {
+        const ssize_t r = pread(fd, t.dst + done, t.bytes - done, (off_t)(t.off + done));
+        if (r <= 0) { ok = false; return; }
+        done += (size_t)r;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nThreads; i++) pool.emplace_back(work);
+  work();
+  for (std::thread &th : pool) th.join();
+  tasks.clear();
+  return ok.load();
+}
+
 void reader(FILE *f, bool restoring, Staging *st, size_t batchBytes, Queue<Batch> *out,
             Shared *sh, double *readSecs) {
   const Clock::time_point t0 = Clock::now();
+  const int fd = fileno(f);
   Batch b;
+  std::vector<ReadTask> tasks;
   int cur = 0;
   size_t used = 0;
   bool haveBuf = false;
   auto flush = [&]() {
     if (b.items.empty()) return;
+    // `own` buffers are final now (no more pushes into this batch)
+    for (Item &it : b.items)
+      if (!it.staged && it.bytes) tasks.push_back({it.fileOff, &it.own[0], it.bytes});
+    if (!read_parallel(fd, tasks)) sh->fail("truncated cubelet data");
     b.buf = haveBuf ? cur : -1;
     out->push(std::move(b));
     b = Batch();
@@ -169,15 +216,20 @@ void reader(FILE *f, bool restoring, Staging *st, size_t batchBytes, Queue<Batch
     used = 0;
   };
   size_t batchWork = 0;
+  long long pos = 64;
   for (;;) {
     if (sh->failed()) break;
     uint32_t len;
     if (fread(&len, 4, 1, f) != 1 || len == 0xFFFFFFFFu) break;
     std::string msg(len, '\0');
     if (len && fread(&msg[0], 1, len, f) != len) { sh->fail("truncated cubelet metadata"); break; }
+    pos += 4 + (long long)len;
     Item it;
     if (!decode_meta(msg.data(), msg.size(), it.meta)) { sh->fail("malformed cubelet metadata"); break; }
     it.bytes = (size_t)it.meta.byte_count;
+    it.fileOff = pos;
+    if (fseeko(f, (off_t)it.bytes, SEEK_CUR) != 0) { sh->fail("truncated cubelet data"); break; }
+    pos += (long long)it.bytes;
     const bool work = restoring ? it.meta.compressed : !it.meta.compressed;
     it.through = !work;
     if (work && !restoring) {
@@ -191,19 +243,12 @@ void reader(FILE *f, bool restoring, Staging *st, size_t batchBytes, Queue<Batch
           st->acquire(cur);
           haveBuf = true;
         }
-        char *dst = st->buf[cur] + used;
-        if (fread(dst, 1, it.bytes, f) != it.bytes) { sh->fail("truncated cubelet data"); break; }
-        it.staged = dst;
+        it.staged = st->buf[cur] + used;
+        tasks.push_back({it.fileOff, const_cast<char *>(it.staged), it.bytes});
         used += slot;
       }
     }
-    if (!it.staged) {  // copied cubelet, compressed input, or one larger than a buffer
-      it.own.resize(it.bytes);
-      if (it.bytes && fread(&it.own[0], 1, it.bytes, f) != it.bytes) {
-        sh->fail("truncated cubelet data");
-        break;
-      }
-    }
+    if (!it.staged) it.own.resize(it.bytes);  // filled at the batch's flush
     batchWork += it.bytes;
     b.items.push_back(std::move(it));
     // restoring: batches by input bytes (no staging buffers)
@@ -315,8 +360,11 @@ wl_status run(wl_ctx *ctx, const char *inPath, const char *outPath, const wl_par
     fclose(fi);
     return WL_EIO;
   }
+  // the writer appends many small pieces (lengths, messages, words)
+  std::vector<char> obuf((size_t)16 << 20);
+  setvbuf(fo, obuf.data(), _IOFBF, obuf.size());
   Staging st;
-  if (!restoring && !st.init(batchBytes)) {
+  if (!restoring && !st.init(ctx, batchBytes)) {
     fclose(fi);
     fclose(fo);
     return WL_ENOMEM;

@@ -49,6 +49,8 @@ bool read_whole_file(const char *path, std::string &out);
 // (engine.cpp); meta_to_result points the result's arrays into m and words
 wl_status result_to_meta(const wl_result *r, CubeMeta &m);
 void meta_to_result(CubeMeta &m, const std::string &words, wl_result &r);
+// a page-locked staging buffer of the context, kept across calls (engine.cpp)
+char *ctx_staging(wl_ctx *ctx, int slot, size_t bytes);
 bool write_whole_file(const char *path, const std::string &data);
 
 }  // namespace wl

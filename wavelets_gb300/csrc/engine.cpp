@@ -206,6 +206,7 @@ struct wl_ctx {
       hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr;
   HostBuf hState, hWords, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
+  HostBuf hStage[2];  // staging buffers of the container pipeline
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
   // and replay it from then on
   int graphMode = 1;
@@ -1540,6 +1541,14 @@ wl_status optimize_impl(wl_ctx *ctx, const void *data, const int size[3], int on
 }  // namespace
 
 namespace wl {
+// A page-locked buffer of at least `bytes` owned by the context (grow-only,
+// kept across calls), for the container pipeline's staging.
+char *ctx_staging(wl_ctx *ctx, int slot, size_t bytes) {
+  if (!ctx || slot < 0 || slot > 1) return nullptr;
+  if (ensure_host(ctx, ctx->hStage[slot], bytes) != WL_OK) return nullptr;
+  return H<char>(ctx->hStage[slot]);
+}
+
 wl_status result_to_meta(const wl_result *r, CubeMeta &m) {
   m.width = r->size[0]; m.height = r->size[1]; m.depth = r->size[2];
   m.transform_2d = r->transform_2d != 0;
@@ -1681,7 +1690,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->meta};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
   for (GraphEntry &g : ctx->graphs) drop_graph(g);
-  HostBuf *hbs[] = {&ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses,
+  HostBuf *hbs[] = {&ctx->hStage[0], &ctx->hStage[1], &ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses,
                     &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals,
                     &ctx->hFlags};
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);
