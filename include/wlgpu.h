@@ -142,6 +142,15 @@ wl_status wl_compress_batch(wl_ctx *ctx, const wl_cubelet *items, int n,
 wl_status wl_decompress_cubelet(wl_ctx *ctx, const wl_result *in, int out_dtype,
                                 void *out, int out_on_device);
 
+/* Decompress n cubelets in one pass of batched launches (every stream decoded
+ * by one set of decoder launches, one dequantization launch, the inverse
+ * transform in concurrent launch groups).  out_dtypes: per cubelet (NULL =
+ * each one's original type); outs[i]: original_size elements of that type,
+ * all host or all device memory (outs_on_device).  Results are those of
+ * wl_decompress_cubelet on each. */
+wl_status wl_decompress_batch(wl_ctx *ctx, const wl_result *in, int n, const int *out_dtypes,
+                              void *const *outs, int outs_on_device);
+
 /* The transform alone (waveletTransform, test_compress_common.cc:492-564).
  * Forward: data (X*Y*Z elements of dtype, x fastest) is padded by repeating
  * edge values to a multiple of 2^steps per axis and transformed; coeffs

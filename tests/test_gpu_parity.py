@@ -402,3 +402,43 @@ def test_2d_mode_batched_equals_single_and_round_trips(ctx, two_d_steps, tmp_pat
         rms_ref = float(np.sqrt(np.mean((ref - x) ** 2)))
         span = float(x.max() - x.min()) or 1.0
         assert rms_gpu <= 1.02 * rms_ref + 1e-3 * span, (k, rms_gpu, rms_ref)
+
+
+def test_decompress_batch_equals_single(ctx):
+    """wl_decompress_batch over mixed cubelets (sizes, element types, both
+    wavelets, 3-D and -2d, all three quantizers, a single-symbol stream, the
+    reference's own files) restores each exactly as wl_decompress_cubelet."""
+    rng = np.random.default_rng(51)
+    items = []
+    for i, shape in enumerate([(8, 32, 16), (2, 64, 64), (16, 16, 16), (3, 5, 7), (32, 48, 40),
+                               (1, 9, 130), (4, 40, 24)]):
+        dt = [np.uint8, np.uint16, np.float32][i % 3]
+        a = synth.scaled_blob_cubelet(rng, shape, dt)
+        items.append((a, P.Params(steps=(2, 2, 2) if i % 2 else (-1, -1, -1),
+                                  wavelet=P.HAAR if i % 3 == 0 else P.CDF97,
+                                  quant_alg=[P.LOG, P.UNIFORM, P.LLOYD][i % 3],
+                                  transform_2d=(i == 6), threshold_fraction=0.8)))
+    items.append((np.full((4, 8, 8), 7, np.uint8), P.Params(steps=(2, 2, 2))))  # one symbol
+    comp = ctx.compress_batch(items)
+    for name in ("uint8_1x64x64.p1.cube", "float32_12x20x24.p2.cube", "uint8_5x7x9.p8.cube"):
+        c = cubefile.read_file(os.path.join(GOLDEN, name))[0]
+        tmp = lib.Compressed(
+            (c.width, c.height, c.depth), tuple(c.params.original_size),
+            {cubefile.UINT8: lib.NP_TO_WL[np.dtype(np.uint8)],
+             cubefile.INT32: lib.NP_TO_WL[np.dtype(np.int32)],
+             cubefile.FLOAT32: lib.NP_TO_WL[np.dtype(np.float32)]}[c.params.original_data_type],
+            tuple(c.params.steps), c.params.wavelet,
+            {cubefile.PB_LOG: P.LOG, cubefile.PB_UNIFORM: P.UNIFORM,
+             cubefile.PB_LLOYD: P.LLOYD}[c.params.quant_alg],
+            c.params.bin_count, c.params.threshold_fraction, c.params.threshold_value,
+            c.params.quant_max_value or 0.0, 0.0, 0.0, 0,
+            c.params.huffman_dup_key if c.params.huffman_dup_key is not None else -1,
+            c.params.huffman_dup_value if c.params.huffman_dup_value is not None else -1, 0,
+            c.words().copy(), np.array(c.params.huffman_decode_table, np.int32),
+            np.array(c.params.bin_boundaries or [], np.float32),
+            np.array(c.params.bin_values or [], np.float32), bool(c.params.transform_2d))
+        comp.append(tmp)
+    single = [ctx.decompress(c) for c in comp]
+    batch = ctx.decompress_batch(comp)
+    for i, (x, y) in enumerate(zip(batch, single)):
+        assert x.dtype == y.dtype and np.array_equal(x, y), i

@@ -17,6 +17,7 @@
 // output offset, and a last pass decodes again and writes the elements.
 // A 12-bit lookup table resolves most codes in one step.
 #include <cstring>
+#include <vector>
 
 #include "wl_internal.h"
 
@@ -221,19 +222,20 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
 }
 
 // Fallback when rounds do not converge (codes that never resynchronise, e.g.
-// all of one length): one thread fixes the subsequences in order.
+// all of one length): one thread per cubelet fixes its subsequences in order.
 __global__ void seq_fix_kernel(const DecCub *cubs, const unsigned *lut, long long *start,
                                long long *exitPos, long long *elems, int buf, int *flags) {
-  const DecCub c = cubs[0];
-  for (long long i = 1; i < c.nSub; i++) {
+  const DecCub c = cubs[blockIdx.x];
+  for (long long j = 1; j < c.nSub; j++) {
+    const long long i = c.subBase + j;
     const long long s = exitPos[2 * (i - 1) + buf];
     if (s == start[i]) continue;
     start[i] = s;
     bool bad = false;
     long long e;
-    exitPos[2 * i + buf] = decode_span(c, lut + c.lutOff, s, (i + 1) * kSubBits, e, bad);
+    exitPos[2 * i + buf] = decode_span(c, lut + c.lutOff, s, (j + 1) * kSubBits, e, bad);
     elems[i] = e;
-    if (bad) flags[1]++;
+    if (bad) atomicAdd(&flags[1], 1);
   }
 }
 
@@ -244,6 +246,74 @@ __global__ void fill_kernel(int *out, long long n, int v) {
 }
 
 }  // namespace
+
+// Decode n streams at once (the DecCub records and scratch in ws: see
+// decode_batch_workspace_bytes).  Streams are the items with a real tree
+// (items whose table is one node are filled by the caller).  Returns 0 on
+// success, 1 when a stream is malformed or holds fewer elements than its
+// cubelet, -1 on a CUDA error; bad[i] (host, may be NULL) marks the items.
+size_t decode_batch_workspace_bytes(int n, long long totalSub) {
+  return (size_t)n * sizeof(DecCub) + 256 + (size_t)n * 4096 * 4 + (size_t)totalSub * 8 * 4 +
+         (size_t)n * 8 + 64 + 256;
+}
+
+int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags,
+                   long long *hostTotals, cudaStream_t s) {
+  if (n <= 0) return 0;
+  std::vector<DecCub> cs(n);
+  long long totalSub = 0;
+  for (int i = 0; i < n; i++) {
+    const DecodeItem &it = items[i];
+    DecCub &c = cs[i];
+    const long long nSub = (it.nWords * 32 + kSubBits - 1) / kSubBits > 0
+                               ? (it.nWords * 32 + kSubBits - 1) / kSubBits : 1;
+    c.words = it.words; c.nWords = it.nWords; c.table = it.table; c.nTable = it.nTable;
+    c.dupKey = it.dupKey; c.dupValue = it.dupValue; c.binCount = it.binCount; c.n = it.n;
+    c.out = it.out; c.subBase = totalSub; c.nSub = nSub; c.lutOff = i * 4096;
+    totalSub += nSub;
+  }
+  char *p = static_cast<char *>(ws);
+  DecCub *dc = reinterpret_cast<DecCub *>(p);
+  p += ((size_t)n * sizeof(DecCub) + 255) & ~(size_t)255;
+  unsigned *lut = reinterpret_cast<unsigned *>(p); p += (size_t)n * 4096 * 4;
+  long long *start = reinterpret_cast<long long *>(p); p += totalSub * 8;
+  long long *exitPos = reinterpret_cast<long long *>(p); p += totalSub * 16;
+  long long *elems = reinterpret_cast<long long *>(p); p += totalSub * 8;
+  long long *total = reinterpret_cast<long long *>(p); p += (size_t)n * 8;
+  int *flags = reinterpret_cast<int *>(p);
+  if (cudaMemcpyAsync(dc, cs.data(), (size_t)n * sizeof(DecCub), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return -1;
+  build_lut_kernel<<<n, 1024, 0, s>>>(dc, lut);
+  const unsigned grid = (unsigned)((totalSub + kThreads - 1) / kThreads);
+  constexpr int kRounds = 6;
+  int round = 0;
+  cudaMemsetAsync(flags, 0, 8, s);
+  spec_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, flags, 0);
+  bool converged = false;
+  for (round = 1; round <= kRounds; round++) {
+    cudaMemsetAsync(flags, 0, 4, s);
+    spec_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, flags,
+                                          round);
+    cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (hostFlags[0] == 0) { converged = true; break; }
+  }
+  if (!converged) {
+    round = kRounds;
+    seq_fix_kernel<<<n, 1, 0, s>>>(dc, lut, start, exitPos, elems, round & 1, flags);
+    cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  }
+  if (hostFlags[1]) return 1;
+  elem_scan_kernel<<<n, 1024, 0, s>>>(dc, elems, total);
+  cudaMemcpyAsync(hostTotals, total, (size_t)n * 8, cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  for (int i = 0; i < n; i++)
+    if (hostTotals[i] < items[i].n) return 1;  // fewer values than the cubelet holds
+  write_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, round);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 // Decode one stream (device words/table) into n ints at out.  Synchronizes
 // the stream between rounds.  Returns 0 on success, 1 malformed stream,

@@ -1185,10 +1185,15 @@ int inverse_passes_cols(int Xp, int Yp, int Zp, const int orig[3], const int ste
 
 // Inverse transform of the coefficients already in ctx->coef (stored order)
 // into out (original size, outType), then synchronize.
-wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int wavelet,
-                       const int original_size[3], int outType, void *out, int outOnDevice,
-                       bool two_d = false) {
-  cudaStream_t s = ctx->stream;
+// Inverse transform passes of one cubelet, sorted into three phases that run
+// in order (phase k of every cubelet of a batch may run concurrently):
+// 0 the z levels, 1 the y levels (2-D mode: the x levels), 2 the last pass
+// into the output with the crop and the element type (2-D mode: the y
+// levels).  c1 holds the coefficients in the stored order, c2 is scratch of
+// the same size, dst receives original_size elements of outType.  Groups are
+// keyed like the forward ones, with the output type in the type field.
+void inverse_passes(const int size[3], const int steps[3], int wavelet, const int original_size[3],
+                    int outType, bool two_d, float *c1, float *c2, void *dst, PassGroups ph[3]) {
   bool identity = steps[0] == 0 && steps[1] == 0 && steps[2] == 0;
   const bool unrotated = identity || two_d;
   const int Xp = unrotated ? size[0] : size[1];
@@ -1197,23 +1202,16 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
   int sx2 = 0, sy2 = 0;
   if (two_d && !identity && !twod_steps(Xp, Yp, steps[0], steps[1], sx2, sy2)) identity = true;
   const int X = original_size[0], Y = original_size[1], Z = original_size[2];
-  const size_t outBytes = (size_t)X * Y * Z * dtype_size(outType);
-  if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, outBytes));
-  TRY(ensure(ctx, ctx->passes, 8 * 4096));
-  TRY(ensure_host(ctx, ctx->hPasses, 8 * 4096));
-  void *dst = outOnDevice ? out : ctx->outbuf.p;
   const int big = 0x7fffffff;
-  float *c1 = P<float>(ctx->coef), *c2 = P<float>(ctx->coef2);
-  size_t hoff = 0;
   auto mk = [&]() { PassDesc d; memset(&d, 0, sizeof d); d.cropL = d.cropB = d.cropA = big;
                     d.clampL = d.clampB = d.clampA = big; d.wavelet = wavelet; d.exact = 0;
                     d.inSC = 1; return d; };
-  const bool exactCdf = false;
+  auto put = [&](int phase, bool cols, const PassDesc &d) {
+    ph[phase][group_key(cols, phase == 2 ? outType : WL_F32, d.L)].push_back(d);
+  };
   wl_params wp;
   memset(&wp, 0, sizeof wp);
   wp.wavelet = wavelet;
-  // descriptors of up to three passes, uploaded in one copy
-  std::vector<GroupLaunch> gl;
   if (two_d && !identity) {
     // x levels first ([z][y][x] -> [z][x][y]), then y levels into the output
     // (the reference undoes y first; the 1-D transforms along different axes
@@ -1224,21 +1222,19 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
     a.in = c1; a.inSA = (long long)Xp * Yp; a.inSB = Xp; a.inSC = 1;
     a.out = c2; a.outSA = (long long)Xp * Yp; a.outSB = 1; a.outSC = Yp;
     a.L = Xp; a.B = Yp; a.rows = Yp * Zp; a.steps = sx2;
-    a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
-    TRY(stage_group(ctx, {a}, hoff, kTuneInvY, WL_F32, WL_F32, true, cols, false, gl));
+    a.T = dwt_tile_rows(a.L, false); a.tiles = (a.rows + a.T - 1) / a.T;
+    put(1, cols, a);
     PassDesc b = mk();
     b.in = c2; b.inSA = (long long)Xp * Yp; b.inSB = Yp; b.inSC = 1;
     b.out = dst; b.outSA = (long long)X * Y; b.outSB = 1; b.outSC = X;
     b.cropL = Y; b.cropA = Z; b.cropB = X;
     b.L = Yp; b.B = Xp; b.rows = Xp * Zp; b.steps = sy2;
-    b.T = dwt_tile_rows(b.L, exactCdf); b.tiles = (b.rows + b.T - 1) / b.T;
-    TRY(stage_group(ctx, {b}, hoff, kTuneInvX, WL_F32, outType, true, cols, false, gl));
+    b.T = dwt_tile_rows(b.L, false); b.tiles = (b.rows + b.T - 1) / b.T;
+    put(2, cols, b);
   } else if (use_cols(Xp, Yp, Zp, identity, wp)) {
     PassDesc d[3];
     const int np = inverse_passes_cols(Xp, Yp, Zp, original_size, steps, wavelet, c1, c2, dst, d);
-    for (int i = 0; i < np; i++)
-      TRY(stage_group(ctx, {d[i]}, hoff, kTuneInvX - (np - 1 - i), WL_F32,
-                      i == np - 1 ? outType : WL_F32, true, true, false, gl));
+    for (int i = 0; i < np; i++) put(3 - np + i, true, d[i]);
   } else {
     if (!identity) {
       // inverse z pass: z-x-y -> y-z-x
@@ -1247,16 +1243,16 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
       a.L = Zp; a.B = Yp; a.rows = Xp * Yp;
       a.out = c2; a.outSA = (long long)Yp * Zp; a.outSB = 1; a.outSC = Yp;
       a.steps = steps[2];
-      a.T = dwt_tile_rows(a.L, exactCdf); a.tiles = (a.rows + a.T - 1) / a.T;
-      TRY(stage_group(ctx, {a}, hoff, kTuneInvZ, WL_F32, WL_F32, true, false, false, gl));
+      a.T = dwt_tile_rows(a.L, false); a.tiles = (a.rows + a.T - 1) / a.T;
+      put(0, false, a);
       // inverse y pass: y-z-x -> x-y-z
       PassDesc bq = mk();
       bq.in = c2; bq.inSA = Yp; bq.inSB = (long long)Zp * Yp;
       bq.L = Yp; bq.B = Xp; bq.rows = Zp * Xp;
       bq.out = c1; bq.outSA = (long long)Xp * Yp; bq.outSB = 1; bq.outSC = Xp;
       bq.steps = steps[1];
-      bq.T = dwt_tile_rows(bq.L, exactCdf); bq.tiles = (bq.rows + bq.T - 1) / bq.T;
-      TRY(stage_group(ctx, {bq}, hoff, kTuneInvY, WL_F32, WL_F32, true, false, false, gl));
+      bq.T = dwt_tile_rows(bq.L, false); bq.tiles = (bq.rows + bq.T - 1) / bq.T;
+      put(1, false, bq);
     }
     // inverse x pass + crop + dtype
     PassDesc x = mk();
@@ -1265,11 +1261,48 @@ wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int w
     x.out = dst; x.outSA = (long long)X * Y; x.outSB = X; x.outSC = 1;
     x.cropL = X; x.cropB = Y; x.cropA = Z;
     x.steps = identity ? 0 : steps[0];
-    x.T = dwt_tile_rows(x.L, exactCdf); x.tiles = (x.rows + x.T - 1) / x.T;
-    TRY(stage_group(ctx, {x}, hoff, kTuneInvX, WL_F32, outType, true, false, false, gl));
+    x.T = dwt_tile_rows(x.L, false); x.tiles = (x.rows + x.T - 1) / x.T;
+    put(2, false, x);
   }
-  CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, hoff, cudaMemcpyHostToDevice, s));
-  TRY(launch_groups(ctx, gl, 0, gl.size()));
+}
+
+// Stage the three inverse phases (one upload) and launch them in order; the
+// groups of a phase run concurrently.  pb receives the phase boundaries.
+wl_status run_inverse_phases(wl_ctx *ctx, PassGroups ph[3]) {
+  size_t hoff = 0, count = 0;
+  for (int k = 0; k < 3; k++)
+    for (const auto &kv : ph[k]) count += kv.second.size();
+  const size_t need = count * (sizeof(PassDesc) + sizeof(int) + 260) + 4096;
+  TRY(ensure(ctx, ctx->passes, need));
+  TRY(ensure_host(ctx, ctx->hPasses, need));
+  std::vector<GroupLaunch> gl;
+  size_t bound[4] = {0, 0, 0, 0};
+  const int kinds[3] = {kTuneInvZ, kTuneInvY, kTuneInvX};
+  for (int k = 0; k < 3; k++) {
+    for (const auto &kv : ph[k]) {
+      const bool cols = (kv.first >> 12) & 1;
+      const int outT = (kv.first >> 8) & 15;
+      TRY(stage_group(ctx, kv.second, hoff, kinds[k], WL_F32, outT, true, cols, false, gl));
+    }
+    bound[k + 1] = gl.size();
+  }
+  CU(cudaMemcpyAsync(ctx->passes.p, ctx->hPasses.p, hoff, cudaMemcpyHostToDevice, ctx->stream));
+  for (int k = 0; k < 3; k++) TRY(launch_phase(ctx, gl, bound[k], bound[k + 1]));
+  return WL_OK;
+}
+
+wl_status inverse_impl(wl_ctx *ctx, const int size[3], const int steps[3], int wavelet,
+                       const int original_size[3], int outType, void *out, int outOnDevice,
+                       bool two_d = false) {
+  cudaStream_t s = ctx->stream;
+  const int X = original_size[0], Y = original_size[1], Z = original_size[2];
+  const size_t outBytes = (size_t)X * Y * Z * dtype_size(outType);
+  if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, outBytes));
+  void *dst = outOnDevice ? out : ctx->outbuf.p;
+  PassGroups ph[3];
+  inverse_passes(size, steps, wavelet, original_size, outType, two_d, P<float>(ctx->coef),
+                 P<float>(ctx->coef2), dst, ph);
+  TRY(run_inverse_phases(ctx, ph));
   if (!outOnDevice) CU(cudaMemcpyAsync(out, dst, outBytes, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   return WL_OK;
@@ -1291,16 +1324,17 @@ wl_status check_sizes(wl_ctx *ctx, const int size[3], const int steps[3], const 
   return WL_OK;
 }
 
-wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *out, int outOnDevice) {
-  CU(cudaSetDevice(ctx->device));
-  if (!r || !out) return fail(ctx, WL_EINVAL, "null argument");
+// Checks of a compressed cubelet before decoding; n = its padded element count.
+wl_status check_result(wl_ctx *ctx, const wl_result *r, int outType, long long &n) {
+  if (!r) return fail(ctx, WL_EINVAL, "null argument");
   if (dtype_size(outType) == 0) return fail(ctx, WL_EINVAL, "bad output dtype %d", outType);
-  long long n;
   TRY(check_sizes(ctx, r->size, r->steps, r->original_size, n, r->transform_2d != 0));
   if (r->size[0] > kMaxAxis || r->size[1] > kMaxAxis || r->size[2] > kMaxAxis)
     return fail(ctx, WL_EINVAL, "axis length above %d", kMaxAxis);
   if (r->bin_count < 2 || r->bin_count > kMaxBins) return fail(ctx, WL_EFORMAT, "bad bin count");
   if (r->n_decode < 2 || !r->decode) return fail(ctx, WL_EFORMAT, "empty Huffman decode table");
+  if (r->n_words < 0 || (r->n_words > 0 && !r->words))
+    return fail(ctx, WL_EFORMAT, "missing Huffman stream");
   if (r->dup_key >= 0 && (r->dup_value < 0 || r->dup_value >= r->bin_count))
     return fail(ctx, WL_EFORMAT, "zero-run value out of range");
   for (int i = 0; i < r->n_decode; i += 2) {  // every entry must be a node or a symbol
@@ -1309,6 +1343,21 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
                : (a < 0 || 2 * a >= r->n_decode || b < 0 || 2 * b >= r->n_decode))
       return fail(ctx, WL_EFORMAT, "corrupt Huffman decode table");
   }
+  if (r->quant_alg == WL_LLOYD && (!r->values || r->n_values != r->bin_count))
+    return fail(ctx, WL_EFORMAT, "codebook values missing");
+  return WL_OK;
+}
+
+// one symbol coded with zero bits: every element is that symbol
+bool single_symbol(const wl_result *r) {
+  return r->n_decode == 2 && r->decode[0] == 0 && r->decode[1] != r->dup_key;
+}
+
+wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *out, int outOnDevice) {
+  CU(cudaSetDevice(ctx->device));
+  if (!r || !out) return fail(ctx, WL_EINVAL, "null argument");
+  long long n;
+  TRY(check_result(ctx, r, outType, n));
   std::vector<float> dq(r->bin_count);
   if (r->quant_alg == WL_LLOYD && (!r->values || r->n_values != r->bin_count))
     return fail(ctx, WL_EFORMAT, "codebook values missing");
@@ -1538,6 +1587,117 @@ wl_status optimize_impl(wl_ctx *ctx, const void *data, const int size[3], int on
   return WL_OK;
 }
 
+// Decompress n cubelets at once: one copy of all streams, decode tables and
+// dequantization tables; every stream decoded by one set of decoder launches;
+// one dequantization launch; the inverse transform as three phases of
+// concurrent launch groups; the outputs copied back per cubelet.
+wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const int *outTypes,
+                                void *const *outs, int outOnDevice) {
+  CU(cudaSetDevice(ctx->device));
+  if (n <= 0) return fail(ctx, WL_EINVAL, "empty batch");
+  if (!rs || !outs) return fail(ctx, WL_EINVAL, "null argument");
+  std::vector<long long> N(n), coefOff(n), wordsOff(n), tableOff(n), outOff(n);
+  std::vector<int> ot(n);
+  long long coefTotal = 0, wordsTotal = 0, tableTotal = 0, outTotal = 0, totalSub = 0;
+  int nStreams = 0;
+  for (int i = 0; i < n; i++) {
+    const wl_result *r = rs + i;
+    ot[i] = outTypes ? outTypes[i] : r->original_dtype;
+    if (!outs[i]) return fail(ctx, WL_EINVAL, "cubelet %d: null output", i);
+    TRY(check_result(ctx, r, ot[i], N[i]));
+    coefOff[i] = coefTotal;
+    coefTotal += (N[i] + 63) & ~63LL;
+    wordsOff[i] = wordsTotal;
+    wordsTotal += ((long long)r->n_words + 3) & ~3LL;
+    tableOff[i] = tableTotal;
+    tableTotal += ((long long)r->n_decode + 3) & ~3LL;
+    outOff[i] = outTotal;
+    outTotal += ((long long)r->original_size[0] * r->original_size[1] * r->original_size[2] *
+                     dtype_size(ot[i]) + 255) & ~255LL;
+    if (!single_symbol(r)) {
+      nStreams++;
+      totalSub += decode_subsequences(r->n_words);
+    }
+  }
+  const size_t decWsBytes = decode_batch_workspace_bytes(nStreams, totalSub);
+  const size_t dqItemsOff = (decWsBytes + 255) & ~(size_t)255;
+  TRY(ensure(ctx, ctx->coef, (size_t)coefTotal * 4 + 256));
+  TRY(ensure(ctx, ctx->coef2, (size_t)coefTotal * 4 + 256));
+  TRY(ensure(ctx, ctx->bins, (size_t)coefTotal * 4 + 256));
+  TRY(ensure(ctx, ctx->decWords, (size_t)wordsTotal * 4 + 16));
+  TRY(ensure(ctx, ctx->decTable, (size_t)tableTotal * 4 + 16));
+  TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
+  TRY(ensure(ctx, ctx->decWs, dqItemsOff + (size_t)n * sizeof(DqItem)));
+  if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, (size_t)outTotal + 16));
+  TRY(ensure_host(ctx, ctx->hWords, (size_t)wordsTotal * 4 + 16));
+  TRY(ensure_host(ctx, ctx->hDecode, (size_t)tableTotal * 4 + 16));
+  TRY(ensure_host(ctx, ctx->hVals, (size_t)n * kMaxBins * 4 + (size_t)n * sizeof(DqItem)));
+  TRY(ensure_host(ctx, ctx->hFlags, 64 + (size_t)n * 8));
+  cudaStream_t s = ctx->stream;
+  // gather the host arrays into page-locked staging: three copies in all
+  uint32_t *hw = H<uint32_t>(ctx->hWords);
+  int *ht = H<int>(ctx->hDecode);
+  float *hq = H<float>(ctx->hVals);
+  DqItem *hdq = reinterpret_cast<DqItem *>(hq + (size_t)n * kMaxBins);
+  long long blocks = 0;
+  std::vector<DecodeItem> items;
+  items.reserve(nStreams);
+  for (int i = 0; i < n; i++) {
+    const wl_result *r = rs + i;
+    if (r->n_words) memcpy(hw + wordsOff[i], r->words, (size_t)r->n_words * 4);
+    memcpy(ht + tableOff[i], r->decode, (size_t)r->n_decode * 4);
+    dequant_values(r->quant_alg, r->bin_count, r->threshold_value, r->max_value, r->values,
+                   hq + (size_t)i * kMaxBins);
+    int *bins = P<int>(ctx->bins) + coefOff[i];
+    hdq[i] = DqItem{bins, P<float>(ctx->coef) + coefOff[i], N[i],
+                    P<float>(ctx->dqtable) + (size_t)i * kMaxBins, r->bin_count, blocks};
+    blocks += (N[i] + 2047) / 2048;
+    if (!single_symbol(r))
+      items.push_back(DecodeItem{P<uint32_t>(ctx->decWords) + wordsOff[i], r->n_words,
+                                 P<int>(ctx->decTable) + tableOff[i], r->n_decode, r->dup_key,
+                                 r->dup_value, r->bin_count, N[i], bins});
+  }
+  CU(cudaMemcpyAsync(ctx->decWords.p, hw, (size_t)wordsTotal * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->decTable.p, ht, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(ctx->dqtable.p, hq, (size_t)n * kMaxBins * 4, cudaMemcpyHostToDevice, s));
+  DqItem *ddq = reinterpret_cast<DqItem *>(P<char>(ctx->decWs) + dqItemsOff);
+  CU(cudaMemcpyAsync(ddq, hdq, (size_t)n * sizeof(DqItem), cudaMemcpyHostToDevice, s));
+  ctx->launches = 0;
+  for (int i = 0; i < n; i++)
+    if (single_symbol(rs + i)) {
+      fill_value(P<int>(ctx->bins) + coefOff[i], N[i], rs[i].decode[1], s);
+      ctx->launches++;
+    }
+  if (!items.empty()) {
+    int *hf = H<int>(ctx->hFlags);
+    long long *totals = reinterpret_cast<long long *>(hf + 16);
+    const int rc = decode_streams(items.data(), (int)items.size(), ctx->decWs.p, hf, totals, s);
+    if (rc < 0) return fail(ctx, WL_ECUDA, "decode failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc > 0) return fail(ctx, WL_EFORMAT, "corrupt Huffman stream in the batch");
+    ctx->launches += 5;
+  }
+  launch_dequant_batch(ddq, n, blocks, s);
+  CU(cudaGetLastError());
+  PassGroups ph[3];
+  for (int i = 0; i < n; i++) {
+    void *dst = outOnDevice ? outs[i] : (void *)(P<char>(ctx->outbuf) + outOff[i]);
+    inverse_passes(rs[i].size, rs[i].steps, rs[i].wavelet, rs[i].original_size, ot[i],
+                   rs[i].transform_2d != 0, P<float>(ctx->coef) + coefOff[i],
+                   P<float>(ctx->coef2) + coefOff[i], dst, ph);
+  }
+  TRY(run_inverse_phases(ctx, ph));
+  if (!outOnDevice)
+    for (int i = 0; i < n; i++) {
+      const wl_result *r = rs + i;
+      const size_t bytes = (size_t)r->original_size[0] * r->original_size[1] *
+                           r->original_size[2] * dtype_size(ot[i]);
+      CU(cudaMemcpyAsync(outs[i], P<char>(ctx->outbuf) + outOff[i], bytes,
+                         cudaMemcpyDeviceToHost, s));
+    }
+  CU(cudaStreamSynchronize(s));
+  return WL_OK;
+}
+
 }  // namespace
 
 namespace wl {
@@ -1729,6 +1889,12 @@ wl_status wl_decompress_cubelet(wl_ctx *ctx, const wl_result *in, int outType, v
                                 int outOnDevice) {
   if (!ctx) return WL_EINVAL;
   return decompress_impl(ctx, in, outType, out, outOnDevice);
+}
+
+wl_status wl_decompress_batch(wl_ctx *ctx, const wl_result *in, int n, const int *out_dtypes,
+                              void *const *outs, int outs_on_device) {
+  if (!ctx) return WL_EINVAL;
+  return decompress_batch_impl(ctx, in, n, out_dtypes, outs, outs_on_device);
 }
 
 wl_status wl_encode_cube(const wl_result *r, int footer, uint8_t **buf, size_t *len) {

@@ -2,10 +2,10 @@
 //
 // Each lane is an ordinary context (its own stream and grow-only buffers)
 // driven by its own host thread, so a batch on one lane overlaps on the GPU
-// with batches and decompressions on the others.  Requests wait in one FIFO
-// queue.  A free lane takes either the decompress request at the head of the
-// queue, or every compress request at the head that fits (continuous
-// batching: whatever arrived while the lanes were busy forms the next batch).
+// with batches on the others.  Requests wait in one FIFO queue.  A free lane
+// takes every request of the head's kind at the head of the queue that fits
+// (continuous batching: whatever arrived while the lanes were busy forms the
+// next batch); compress and decompress batches each run as one batched call.
 // Admission is gated by an estimate of each request's device working memory
 // against the configured budget; a request larger than the whole budget runs
 // alone once nothing else is in flight.
@@ -134,20 +134,20 @@ void worker(wl_server *s, int lane) {
       if (s->stop && s->pending.empty()) return;
       if (!head_fits(s)) continue;
       const double budget = (double)s->cfg.memory_budget;
-      if (s->pending.front()->req.kind == WL_REQ_DECOMPRESS) {
-        batch.push_back(s->pending.front());
+      // every request of the head's kind that waited behind it and fits
+      // (decompress requests whose outputs are all on the host, or all on
+      // the device, batch together)
+      const int kind = s->pending.front()->req.kind;
+      const int dev = s->pending.front()->req.out_on_device;
+      while (!s->pending.empty() && (int)batch.size() < s->cfg.max_batch) {
+        Job *j = s->pending.front();
+        if (j->req.kind != kind) break;
+        if (kind == WL_REQ_DECOMPRESS && j->req.out_on_device != dev) break;
+        if (!batch.empty() && s->inflight + est + j->est > budget) break;
+        if (batch.empty() && s->inflight > 0 && s->inflight + j->est > budget) break;
+        batch.push_back(j);
+        est += j->est;
         s->pending.pop_front();
-        est = batch[0]->est;
-      } else {
-        while (!s->pending.empty() && (int)batch.size() < s->cfg.max_batch) {
-          Job *j = s->pending.front();
-          if (j->req.kind != WL_REQ_COMPRESS) break;
-          if (!batch.empty() && s->inflight + est + j->est > budget) break;
-          if (batch.empty() && s->inflight > 0 && s->inflight + j->est > budget) break;
-          batch.push_back(j);
-          est += j->est;
-          s->pending.pop_front();
-        }
       }
       s->inflight += est;
       const Clock::time_point now = Clock::now();
@@ -161,9 +161,25 @@ void worker(wl_server *s, int lane) {
     }
 
     if (batch[0]->req.kind == WL_REQ_DECOMPRESS) {
-      Job *j = batch[0];
-      j->st = wl_decompress_cubelet(ctx, j->req.compressed, j->req.out_dtype, j->req.out,
-                                    j->req.out_on_device);
+      const int n = (int)batch.size();
+      std::vector<wl_result> rs(n);
+      std::vector<int> dts(n);
+      std::vector<void *> outs(n);
+      for (int i = 0; i < n; i++) {
+        rs[i] = *batch[i]->req.compressed;
+        dts[i] = batch[i]->req.out_dtype;
+        outs[i] = batch[i]->req.out;
+      }
+      wl_status st = wl_decompress_batch(ctx, rs.data(), n, dts.data(), outs.data(),
+                                         batch[0]->req.out_on_device);
+      // a bad request fails its batch: retry the batch one by one so the
+      // others still succeed and the bad one gets its own status
+      if (st != WL_OK && n > 1)
+        for (Job *j : batch)
+          j->st = wl_decompress_cubelet(ctx, j->req.compressed, j->req.out_dtype, j->req.out,
+                                        j->req.out_on_device);
+      else
+        for (Job *j : batch) j->st = st;
     } else {
       const int n = (int)batch.size();
       items.resize(n);

@@ -253,6 +253,34 @@ void launch_pack_meta(DevBatch &b, cudaStream_t s);
 
 // GPU Huffman decoding (decode.cu)
 size_t decode_workspace_bytes(long long nWords);
+// batched decoding (decode.cu)
+struct DecodeItem {
+  const uint32_t *words;  // device
+  long long nWords;
+  const int *table;       // device
+  int nTable;
+  int dupKey, dupValue, binCount;
+  long long n;            // elements
+  int *out;               // device bins
+};
+inline long long decode_subsequences(long long nWords) {
+  const long long k = (nWords * 32 + 1023) / 1024;
+  return k > 0 ? k : 1;
+}
+size_t decode_batch_workspace_bytes(int n, long long totalSub);
+// dequantize many cubelets in one launch (dwt.cu); blockBase counts blocks
+// of 2048 elements
+struct DqItem {
+  const int *bins;
+  float *out;
+  long long n;
+  const float *table;
+  int nTable;
+  long long blockBase;
+};
+void launch_dequant_batch(const DqItem *items, int nItems, long long totalBlocks, cudaStream_t s);
+int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags, long long *hostTotals,
+                   cudaStream_t s);
 int decode_stream(const uint32_t *words, long long nWords, const int *table, int nTable,
                   int dupKey, int dupValue, int binCount, long long n, int *out, void *ws,
                   int *hostFlags, cudaStream_t s);

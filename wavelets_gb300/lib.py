@@ -152,6 +152,9 @@ EXPORTS = {
     "wl_serve_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_serve_destroy": (None, [ctypes.c_void_p]),
     "wl_results_free": (None, [ctypes.POINTER(WlResult), ctypes.c_int]),
+    "wl_decompress_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlResult), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "wl_compress_container": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
                                              ctypes.POINTER(WlParams), ctypes.c_size_t,
                                              ctypes.POINTER(WlContainerStats)]),
@@ -559,6 +562,29 @@ class Context:
                                             ctypes.c_void_p(out.ctypes.data), 0)
         self._check(st)
         return out
+
+    def decompress_batch(self, cs: Sequence[Compressed], dtypes=None) -> List[np.ndarray]:
+        """Restore many cubelets in one batched call (dtypes default to each
+        one's original)."""
+        n = len(cs)
+        rs = (WlResult * n)()
+        keep = []
+        outs, ptrs = [], (ctypes.c_void_p * n)()
+        dts = (ctypes.c_int * n)()
+        for i, c in enumerate(cs):
+            r = c.to_struct()
+            keep.append(c)
+            ctypes.memmove(ctypes.byref(rs, i * ctypes.sizeof(WlResult)), ctypes.byref(r),
+                           ctypes.sizeof(WlResult))
+            wl_dt = (NP_TO_WL[np.dtype(dtypes[i])] if dtypes is not None and dtypes[i] is not None
+                     else c.original_dtype)
+            X, Y, Z = c.original_size
+            o = np.empty((Z, Y, X), WL_TO_NP[wl_dt])
+            outs.append(o)
+            ptrs[i] = o.ctypes.data
+            dts[i] = wl_dt
+        self._check(self.lib.wl_decompress_batch(self.h, rs, n, dts, ptrs, 0))
+        return outs
 
     def forward_transform(self, arr, params: Optional[P.Params] = None):
         """Coefficients of the forward transform in the stored (rotated) order
