@@ -452,28 +452,41 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
     unsigned mine = 0;
     for (int i = t0; i < t1; i++) mine += token_len(tl[i], sLen, dupKey);
     unsigned total;
-    unsigned pos = block_excl_scan(mine, shs, total) + shift;
-    for (int i = t0; i < t1; i++) {
-      const uint16_t t = tl[i];
-      const int sym = t & 0x1fff;
-      int l = sLen[sym];
-      unsigned long long v = sCode[sym];
-      if (sym == dupKey) {
-        v |= (unsigned long long)(t >> 13) << l;
-        l += 3;
+    const unsigned pos = block_excl_scan(mine, shs, total) + shift;
+    // The slice's bits are packed in a register and leave a word at a time:
+    // words wholly inside the slice are stored, the first and the last
+    // (shared with the neighbouring slices) are OR-ed in.
+    if (mine > 0) {
+      unsigned w = pos >> 5;
+      const unsigned wFirst = w;
+      unsigned long long acc = 0;  // bit 0 = bit 0 of word w
+      int bits = (int)(pos & 31);
+      for (int i = t0; i < t1; i++) {
+        const uint16_t t = tl[i];
+        const int sym = t & 0x1fff;
+        int l = sLen[sym];
+        unsigned long long v = sCode[sym];
+        if (sym == dupKey) {
+          v |= (unsigned long long)(t >> 13) << l;
+          l += 3;
+        }
+        // up to 61 bits, appended at most 32 at a time (bits < 32 here)
+        while (l > 0) {
+          const int take = l < 32 ? l : 32;
+          acc |= (v & ((1ull << take) - 1)) << bits;
+          bits += take;
+          v >>= take;
+          l -= take;
+          if (bits >= 32) {
+            if (w == wFirst) atomicOr(&dstw[w], (unsigned)acc);
+            else dstw[w] = (unsigned)acc;
+            w++;
+            acc >>= 32;
+            bits -= 32;
+          }
+        }
       }
-      unsigned p = pos;
-      pos += l;
-      // up to 61 bits starting anywhere in a word: at most 3 words
-      while (l > 0) {
-        const int o = p & 31;
-        const int take = min(l, 32 - o);
-        const unsigned part = (unsigned)(v & ((take == 32) ? 0xffffffffull : ((1ull << take) - 1)));
-        atomicOr(&dstw[p >> 5], part << o);
-        v >>= take;
-        p += take;
-        l -= take;
-      }
+      if (bits > 0) atomicOr(&dstw[w], (unsigned)acc);
     }
     __syncthreads();
     if (staged) {
