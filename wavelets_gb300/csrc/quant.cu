@@ -456,8 +456,10 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   unsigned *hist = reinterpret_cast<unsigned *>(tab + histOff);
   __shared__ __align__(16) uint16_t sLut[kLutStride];
   // by warp region: candidate values, overwritten in place by the value list
-  __shared__ __align__(16) float sX[kChunk];
-  __shared__ uint16_t sPos[kChunk];  // candidate positions
+  // (32 extra slots: a dump for the stores of lanes without a candidate,
+  // which keeps the compaction free of branches)
+  __shared__ __align__(16) float sX[kChunk + 32];
+  __shared__ uint16_t sPos[kChunk + 32];  // candidate positions
   // per-warp summaries, two sets used by alternate chunks
   __shared__ int wLast[2][kWarps], wFirst[2][kWarps];
   __shared__ unsigned wTok[2][kWarps];
@@ -510,11 +512,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
         // zero bin iff |x| < zthr (NaN is a candidate)
         const bool cand = (kFull || pos < len) && !(fabsf(x[j]) < zthr);
         const unsigned m = __ballot_sync(kAll, cand);
-        if (cand) {
-          const int l = base + nCand + __popc(m & ltMask);
-          sX[l] = x[j];
-          sPos[l] = (uint16_t)pos;
-        }
+        const int l = cand ? base + nCand + __popc(m & ltMask) : kChunk + lane;
+        sX[l] = x[j];
+        sPos[l] = (uint16_t)pos;
         nCand += __popc(m);
       }
     };
