@@ -526,18 +526,18 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
     // write index never passes the read index of its round, and every lane
     // of the round has read before the ballot)
     int nVal = 0;  // warp-uniform
+    // (without branches: lanes past the candidates quantize whatever their
+    // slot of the warp's region holds -- every quantizer reads only its
+    // bounded tables -- and store to the dump slot)
     for (int r = 0; 32 * r < nCand; r++) {
-      const int l = 32 * r + lane;
+      const int l = 32 * r + lane;  // < 512: inside the warp's region
       const bool has = l < nCand;
-      int bin = 0;
-      unsigned pos = 0;
-      if (has) {
-        bin = quant_value(sX[base + l], q, tab, sLut);
-        pos = sPos[base + l];
-      }
+      const int bin = quant_value(sX[base + l], q, tab, sLut);
+      const unsigned pos = sPos[base + l];
       const bool v = has && bin != dupV;
       const unsigned m = __ballot_sync(kAll, v);
-      if (v) sVal[base + nVal + __popc(m & ltMask)] = (pos << 13) | (unsigned)bin;
+      const int idx = v ? base + nVal + __popc(m & ltMask) : kChunk + lane;
+      sVal[idx] = (pos << 13) | (unsigned)bin;
       nVal += __popc(m);
     }
     __syncwarp();
