@@ -397,7 +397,7 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 // tokens of the zero-bin run before it when that run starts inside the chunk.
 // Runs touching a chunk edge are left to runs_kernel (counts) and the encoder
 // (tokens).  A CTA codes kQuantGroup consecutive chunks of one cubelet; warp
-// w owns elements [512 w, 512 w + 512) of each chunk, and everything but two
+// w owns elements [512 w, 512 w + 512) of each chunk, and everything but three
 // CTA barriers per chunk is warp-local.
 //
 // Phase 1 (every element): -thr < x < thr is the zero bin for all three
@@ -413,8 +413,11 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 // lane before, or the last value of the nearest earlier warp -- is the zero
 // run in between; the token counts give each warp its place in the chunk
 // (after a CTA barrier) and each lane its place in the warp (a warp scan),
-// and every lane writes its run tokens and value token straight to the
-// chunk's token slot.
+// and every lane writes its run tokens and value token to a staging copy
+// of the chunk's tokens in shared memory.
+// Copy-out (after a CTA barrier): whole 16-byte words of tokens to the
+// chunk's slot, so the slot is written with full sectors instead of one
+// 2-byte store per token.
 // greedy split of a zero-bin run into dup tokens and single zero-bin tokens
 // (closed form of run_split; the same counts as run_token_count)
 __device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups) {
@@ -459,7 +462,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   // (32 extra slots: a dump for the stores of lanes without a candidate,
   // which keeps the compaction free of branches)
   __shared__ __align__(16) float sX[kChunk + 32];
-  __shared__ uint16_t sPos[kChunk + 32];  // candidate positions
+  // candidate positions; after phase 2 the chunk's tokens, staged for
+  // 16-byte stores
+  __shared__ __align__(16) uint16_t sPos[kChunk + 32];
   // per-warp summaries, two sets used by alternate chunks
   __shared__ int wLast[2][kWarps], wFirst[2][kWarps];
   __shared__ unsigned wTok[2][kWarps];
@@ -557,7 +562,12 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
     int lead = len;
     for (int v = kWarps - 1; v >= 0; v--)
       if (wFirst[par][v] >= 0) lead = wFirst[par][v];
-    uint16_t *dst = b.tok + cd.coefOff + start + lead;
+    // the tokens are staged in sPos (free after phase 2) from index sh on,
+    // so that index k maps to the 16-byte aligned slot element lead - sh + k
+    // (coefOff and the chunk start are multiples of 8 elements); they end at
+    // sh + nTok <= len, short of the dump slots
+    const int sh = lead & 7;
+    uint16_t *sTok = sPos + sh;
     int myTok = 0, singles = 0, dups = 0;
     {
       int carry = prevW;
@@ -568,7 +578,6 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
         const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
         const int pl = __shfl_up_sync(kAll, p, 1);
         const int prev = lane ? pl : carry;
-        const unsigned act = __ballot_sync(kAll, hasV);
         if (hasV) {
           const int gap = prev >= 0 ? p - prev - 1 : 0;
           if (gap > 0) {
@@ -579,8 +588,7 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
             dups += dp;
           }
           myTok += 1;
-          const unsigned peers = __match_any_sync(act, bin);
-          if (lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
+          atomicAdd(&hist[bin], 1u);
         }
         carry = __shfl_sync(kAll, p, 31);
       }
@@ -632,11 +640,28 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
         if (hasV) {
           unsigned t = o + (unsigned)(inc - cnt);
           if (prev >= 0 && p - prev > 1)
-            run_tokens_short(p - prev - 1, B, dupV, [&](uint16_t tk) { dst[t++] = tk; });
-          dst[t] = make_token(bin, 0);
+            run_tokens_short(p - prev - 1, B, dupV, [&](uint16_t tk) { sTok[t++] = tk; });
+          sTok[t] = make_token(bin, 0);
         }
         o += (unsigned)__shfl_sync(kAll, inc, 31);
         carry = __shfl_sync(kAll, p, 31);
+      }
+    }
+    __syncthreads();
+
+    // ---- copy-out: 16-byte words of the staged tokens to the chunk's slot;
+    // warp w copies the words of its own region of sPos, so its next
+    // phase 1 may overwrite that region without another barrier
+    {
+      const int end = sh + (int)nTok;  // <= len <= kChunk
+      uint16_t *g = b.tok + cd.coefOff + start + (lead - sh);
+      for (int qw = 64 * w + lane; qw < 64 * w + 64 && 8 * qw < end; qw += 32) {
+        const int k0 = 8 * qw;
+        if (k0 >= sh && k0 + 8 <= end) {
+          *reinterpret_cast<uint4 *>(g + k0) = *reinterpret_cast<const uint4 *>(sPos + k0);
+        } else {
+          for (int k = max(k0, sh); k < min(k0 + 8, end); k++) g[k] = sPos[k];
+        }
       }
     }
     if (threadIdx.x == 0) {
@@ -654,7 +679,7 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
     }
     // no barrier: the next chunk writes the other summary set, and a warp
     // reaches this chunk's set again only after every warp has passed the
-    // next chunk's two barriers
+    // next chunk's barriers
   }
   __syncthreads();
   unsigned long long *gh = b.hist + (size_t)ci * kMaxSymbols;
