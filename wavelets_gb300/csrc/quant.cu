@@ -397,8 +397,8 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 // tokens of the zero-bin run before it when that run starts inside the chunk.
 // Runs touching a chunk edge are left to runs_kernel (counts) and the encoder
 // (tokens).  A CTA codes kQuantGroup consecutive chunks of one cubelet; warp
-// w owns elements [512 w, 512 w + 512) of each chunk, and everything but three
-// CTA barriers per chunk is warp-local.
+// w owns elements [512 w, 512 w + 512) of each chunk, and everything but one
+// CTA barrier per chunk is warp-local.
 //
 // Phase 1 (every element): -thr < x < thr is the zero bin for all three
 // quantizers (uniform and log test |x| <= thr first; the codebook has the
@@ -406,18 +406,17 @@ __device__ __forceinline__ QParams load_qparams(const CubeletDev &cd, const Cube
 // element costs two compares.  The others are candidates, compacted into the
 // warp's region of shared memory (in word j lane l holds element
 // 512 w + 32 j + l, so loads are coalesced).
-// Phase 2 (per candidate, 32 at a time): the exact bin; candidates that are
-// not the zero bin become the warp's value list (position, bin), written in
-// place over the candidates, in position order.
-// Phase 3 (per value, 32 at a time): the gap to the previous value -- the
-// lane before, or the last value of the nearest earlier warp -- is the zero
-// run in between; the token counts give each warp its place in the chunk
-// (after a CTA barrier) and each lane its place in the warp (a warp scan),
-// and every lane writes its run tokens and value token to a staging copy
-// of the chunk's tokens in shared memory.
-// Copy-out (after a CTA barrier): whole 16-byte words of tokens to the
-// chunk's slot, so the slot is written with full sectors instead of one
-// 2-byte store per token.
+// Phase 2 (per candidate, 32 at a time): the exact bin; a candidate that is
+// not the zero bin is a value.  The zero run before a value ends at the
+// previous value -- the nearest lower lane with one, or the warp's last value
+// of earlier rounds -- so its token count is known here, a warp scan gives
+// each lane its place among the warp's tokens, and the lane stages its run
+// tokens and value token in the warp's buffer (prefilled with the single
+// zero-bin token, so only dup tokens and the value token are stored).
+// After the CTA barrier the warp summaries (first and last value, staged
+// count) give every warp the run before its first value and its place in the
+// chunk, and each warp writes that run's tokens and its staged ones to the
+// chunk's slot with coalesced stores.
 // greedy split of a zero-bin run into dup tokens and single zero-bin tokens
 // (closed form of run_split; the same counts as run_token_count)
 __device__ __forceinline__ void run_split_closed(int L, int &singles, int &dups) {
@@ -447,6 +446,21 @@ __device__ __forceinline__ void run_tokens_short(int L, int dupKey, int dupV, F 
   for (; r > 0; r--) f(make_token(dupV, 0));
 }
 
+// Token j of run_tokens_short(L, dupKey, dupV) (j below the run's count).
+__device__ __forceinline__ uint16_t run_token_at(int L, int j, int dupKey, int dupV) {
+  const int q = L >> 10;
+  if (j < q) return make_token(dupKey, 7);
+  j -= q;
+  int r = L & 1023;
+  while (r > 8) {
+    const int lg = 31 - __clz(r);
+    if (j == 0) return make_token(dupKey, lg - 3);
+    j--;
+    r -= 1 << lg;
+  }
+  return make_token(dupV, 0);
+}
+
 __global__ void __launch_bounds__(kThreads, 4)
 quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   constexpr int kWords = kChunk / kThreads;  // 16 words of 32 elements per warp
@@ -458,17 +472,17 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   extern __shared__ float tab[];
   unsigned *hist = reinterpret_cast<unsigned *>(tab + histOff);
   __shared__ __align__(16) uint16_t sLut[kLutStride];
-  // by warp region: candidate values, overwritten in place by the value list
-  // (32 extra slots: a dump for the stores of lanes without a candidate,
-  // which keeps the compaction free of branches)
+  // by warp region: candidate values and positions (32 extra slots: a dump
+  // for the stores of lanes without a candidate, which keeps the compaction
+  // free of branches)
   __shared__ __align__(16) float sX[kChunk + 32];
-  // candidate positions; after phase 2 the chunk's tokens, staged for
-  // 16-byte stores
-  __shared__ __align__(16) uint16_t sPos[kChunk + 32];
-  // per-warp summaries, two sets used by alternate chunks
-  __shared__ int wLast[2][kWarps], wFirst[2][kWarps];
-  __shared__ unsigned wTok[2][kWarps];
-  unsigned *sVal = reinterpret_cast<unsigned *>(sX);  // (position << 13) | bin
+  __shared__ uint16_t sPos[kChunk + 32];
+  // per warp: its tokens after its first value's zero run, in order (at
+  // most kSpan: each token starts at its own element of the warp's span)
+  __shared__ __align__(16) uint16_t sStage[kWarps][kSpan];
+  // per-warp summaries (first and last value position, staged tokens), two
+  // sets used by alternate chunks
+  __shared__ int wLast[2][kWarps], wFirst[2][kWarps], wTok[2][kWarps];
   const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
@@ -484,6 +498,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
   // zero-bin elements (-thr < x < thr) can be skipped only when they are
   // coded as runs; without runs every element is a candidate (|x| < 0 never)
   const float zthr = dupV >= 0 ? q.thr : 0.f;
+  uint16_t *stage = sStage[w];
+  const unsigned fill2 = dupV >= 0 ? (unsigned)make_token(dupV, 0) * 0x10001u : 0u;
+  int singles = 0, dups = 0;  // the lane's zero-run tokens, over all chunks
 
   for (int i = threadIdx.x; i < B + 1; i += kThreads) hist[i] = 0;
   for (int i = threadIdx.x; i < nTab; i += kThreads) tab[i] = b.qtable[cd.tableOff + i];
@@ -501,7 +518,14 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
     const int len = (int)min((long long)kChunk, cd.n - start);
     const float *src = coef + cd.coefOff + start;
 
-    // ---- phase 1: candidates into the warp's region
+    // ---- phase 1: candidates into the warp's region; the warp's staging
+    // buffer is prefilled with single zero-bin tokens
+    if (dupV >= 0) {
+      uint4 *s4 = reinterpret_cast<uint4 *>(stage);
+      const uint4 f4 = make_uint4(fill2, fill2, fill2, fill2);
+      s4[lane] = f4;
+      s4[lane + 32] = f4;
+    }
     int nCand = 0;  // warp-uniform
     auto phase1 = [&](auto full) {
       constexpr bool kFull = decltype(full)::value;
@@ -527,159 +551,145 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
     else phase1(std::false_type());
     __syncwarp();
 
-    // ---- phase 2: exact bins; values replace the candidates in place (a
-    // write index never passes the read index of its round, and every lane
-    // of the round has read before the ballot)
-    int nVal = 0;  // warp-uniform
-    // (without branches: lanes past the candidates quantize whatever their
-    // slot of the warp's region holds -- every quantizer reads only its
-    // bounded tables -- and store to the dump slot)
+    // ---- phase 2 (per candidate, 32 at a time): the exact bin; a value
+    // (not the zero bin) gets its token and the tokens of the zero run
+    // since the warp's previous value, staged in the warp's buffer.  Single
+    // zero-bin tokens are already there (prefilled), so a lane stores only
+    // its dup tokens (gaps above 8) and its value token.  The warp's first
+    // value stages its own token only: the run before it reaches into
+    // earlier warps and is coded at the copy-out.
+    // (without branches around the loads: lanes past the candidates
+    // quantize whatever their slot of the warp's region holds -- every
+    // quantizer reads only its bounded tables -- and are not values)
+    int nStaged = 0;                  // warp-uniform
+    int firstPos = -1, lastPos = -1;  // warp-uniform: the warp's values so far
     for (int r = 0; 32 * r < nCand; r++) {
       const int l = 32 * r + lane;  // < 512: inside the warp's region
-      const bool has = l < nCand;
       const int bin = quant_value(sX[base + l], q, tab, sLut);
-      const unsigned pos = sPos[base + l];
-      const bool v = has && bin != dupV;
+      const int pos = sPos[base + l];
+      const bool v = l < nCand && bin != dupV;
       const unsigned m = __ballot_sync(kAll, v);
-      const int idx = v ? base + nVal + __popc(m & ltMask) : kChunk + lane;
-      sVal[idx] = (pos << 13) | (unsigned)bin;
-      nVal += __popc(m);
-    }
-    __syncwarp();
-    if (lane == 0) {
-      wFirst[par][w] = nVal ? (int)(sVal[base] >> 13) : -1;
-      wLast[par][w] = nVal ? (int)(sVal[base + nVal - 1] >> 13) : -1;
-    }
-    __syncthreads();
-
-    // ---- phase 3a: token counts and the histogram
-    // the value before this warp's first: positions grow with the warp index
-    int prevW = -1;
-    for (int v = 0; v < w; v++) prevW = max(prevW, wLast[par][v]);
-    // the chunk's tokens go to its slot from the first value's position on;
-    // the lead zero run's tokens (written later by runs_kernel) fit before
-    // it, since each token starts at its own element
-    int lead = len;
-    for (int v = kWarps - 1; v >= 0; v--)
-      if (wFirst[par][v] >= 0) lead = wFirst[par][v];
-    // the tokens are staged in sPos (free after phase 2) from index sh on,
-    // so that index k maps to the 16-byte aligned slot element lead - sh + k
-    // (coefOff and the chunk start are multiples of 8 elements); they end at
-    // sh + nTok <= len, short of the dump slots
-    const int sh = lead & 7;
-    uint16_t *sTok = sPos + sh;
-    int myTok = 0, singles = 0, dups = 0;
-    {
-      int carry = prevW;
-      for (int r = 0; 32 * r < nVal; r++) {
-        const int i = 32 * r + lane;
-        const bool hasV = i < nVal;
-        const unsigned ev = hasV ? sVal[base + i] : 0u;
-        const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
-        const int pl = __shfl_up_sync(kAll, p, 1);
-        const int prev = lane ? pl : carry;
-        if (hasV) {
-          const int gap = prev >= 0 ? p - prev - 1 : 0;
-          if (gap > 0) {
-            int sg, dp;
-            run_split_closed(gap, sg, dp);
-            myTok += sg + dp;
-            singles += sg;
-            dups += dp;
-          }
-          myTok += 1;
-          atomicAdd(&hist[bin], 1u);
-        }
-        carry = __shfl_sync(kAll, p, 31);
-      }
-    }
+      if (m == 0) continue;
+      const unsigned lower = m & ltMask;
+      const int pp = __shfl_sync(kAll, pos, lower ? 31 - __clz(lower) : 0);
+      const int prev = lower ? pp : lastPos;
+      const int gap = v && prev >= 0 ? pos - prev - 1 : 0;
+      int sg, dp;
+      run_split_closed(gap, sg, dp);  // 0, 0 for gap 0
+      singles += sg;
+      dups += dp;
+      const int cnt = v ? 1 + sg + dp : 0;
+      int inc = cnt;
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      myTok += __shfl_xor_sync(kAll, myTok, d);
-      singles += __shfl_xor_sync(kAll, singles, d);
-      dups += __shfl_xor_sync(kAll, dups, d);
-    }
-    if (lane == 0) {
-      wTok[par][w] = (unsigned)myTok;
-      if (singles) atomicAdd(&hist[dupV], (unsigned)singles);
-      if (dups) atomicAdd(&hist[B], (unsigned)dups);
-    }
-    __syncthreads();
-
-    // ---- phase 3b: tokens, straight to the chunk's slot
-    unsigned o = 0, nTok = 0;
-    for (int v = 0; v < kWarps; v++) {
-      if (v < w) o += wTok[par][v];
-      nTok += wTok[par][v];
-    }
-    {
-      int carry = prevW;
-      for (int r = 0; 32 * r < nVal; r++) {
-        const int i = 32 * r + lane;
-        const bool hasV = i < nVal;
-        const unsigned ev = hasV ? sVal[base + i] : 0u;
-        const int p = (int)(ev >> 13), bin = (int)(ev & 0x1fffu);
-        const int pl = __shfl_up_sync(kAll, p, 1);
-        const int prev = lane ? pl : carry;
-        int cnt = 0;
-        if (hasV) {
-          const int gap = prev >= 0 ? p - prev - 1 : 0;
-          if (gap > 0) {
-            int sg, dp;
-            run_split_closed(gap, sg, dp);
-            cnt = sg + dp;
-          }
-          cnt += 1;
-        }
-        int inc = cnt;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const int t = __shfl_up_sync(kAll, inc, d);
-          if (lane >= d) inc += t;
-        }
-        if (hasV) {
-          unsigned t = o + (unsigned)(inc - cnt);
-          if (prev >= 0 && p - prev > 1)
-            run_tokens_short(p - prev - 1, B, dupV, [&](uint16_t tk) { sTok[t++] = tk; });
-          sTok[t] = make_token(bin, 0);
-        }
-        o += (unsigned)__shfl_sync(kAll, inc, 31);
-        carry = __shfl_sync(kAll, p, 31);
+      for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kAll, inc, d);
+        if (lane >= d) inc += t;
       }
-    }
-    __syncthreads();
-
-    // ---- copy-out: 16-byte words of the staged tokens to the chunk's slot;
-    // warp w copies the words of its own region of sPos, so its next
-    // phase 1 may overwrite that region without another barrier
-    {
-      const int end = sh + (int)nTok;  // <= len <= kChunk
-      uint16_t *g = b.tok + cd.coefOff + start + (lead - sh);
-      for (int qw = 64 * w + lane; qw < 64 * w + 64 && 8 * qw < end; qw += 32) {
-        const int k0 = 8 * qw;
-        if (k0 >= sh && k0 + 8 <= end) {
-          *reinterpret_cast<uint4 *>(g + k0) = *reinterpret_cast<const uint4 *>(sPos + k0);
+      if (v) {
+        int t = nStaged + inc - cnt;
+        if (gap > 8) {  // dup tokens, in the order of run_tokens_short
+          for (int j = gap >> 10; j > 0; j--) stage[t++] = make_token(B, 7);
+          int rr = gap & 1023;
+          while (rr > 8) {
+            const int lg = 31 - __clz(rr);
+            stage[t++] = make_token(B, lg - 3);
+            rr -= 1 << lg;
+          }
+          t += rr;
         } else {
-          for (int k = max(k0, sh); k < min(k0 + 8, end); k++) g[k] = sPos[k];
+          t += gap;
         }
+        stage[t] = make_token(bin, 0);
+        atomicAdd(&hist[bin], 1u);
       }
+      if (firstPos < 0) firstPos = __shfl_sync(kAll, pos, __ffs(m) - 1);
+      lastPos = __shfl_sync(kAll, pos, 31 - __clz(m));
+      nStaged += __shfl_sync(kAll, inc, 31);
     }
+    if (lane == 0) {
+      wFirst[par][w] = firstPos;
+      wLast[par][w] = lastPos;
+      wTok[par][w] = nStaged;
+    }
+    __syncthreads();
+
+    // ---- the chunk's layout from the warp summaries (lane u of every warp
+    // reads warp u's; lanes >= kWarps hold an empty warp)
+    int F = -1, Lu = -1, I = 0;
+    if (lane < kWarps) {
+      F = wFirst[par][lane];
+      Lu = wLast[par][lane];
+      I = wTok[par][lane];
+    }
+    // the value before warp u's first: positions grow with the warp index
+    int pv = Lu;
+#pragma unroll
+    for (int d = 1; d < kWarps; d <<= 1) {
+      const int t = __shfl_up_sync(kAll, pv, d);
+      if (lane >= d) pv = max(pv, t);
+    }
+    int prevU = __shfl_up_sync(kAll, pv, 1);
+    if (lane == 0) prevU = -1;
+    // warp u's first run lies inside the chunk when a value precedes it
+    const int g0 = F >= 0 && prevU >= 0 ? F - prevU - 1 : 0;
+    int sg0, dp0;
+    run_split_closed(g0, sg0, dp0);
+    if (w == 0) {  // counted once per chunk
+      singles += sg0;
+      dups += dp0;
+    }
+    const int tok = sg0 + dp0 + I;
+    int incT = tok;
+#pragma unroll
+    for (int d = 1; d < kWarps; d <<= 1) {
+      const int t = __shfl_up_sync(kAll, incT, d);
+      if (lane >= d) incT += t;
+    }
+    const int nTok = __shfl_sync(kAll, incT, kWarps - 1);
+    int lead = F >= 0 ? F : len, last = Lu;
+#pragma unroll
+    for (int d = kWarps / 2; d > 0; d >>= 1) {
+      lead = min(lead, __shfl_xor_sync(kAll, lead, d));
+      last = max(last, __shfl_xor_sync(kAll, last, d));
+    }
+    lead = __shfl_sync(kAll, lead, 0);
+    last = __shfl_sync(kAll, last, 0);
+
+    // ---- copy-out: warp w's tokens (its first run, then the staged ones)
+    // to their place in the chunk's slot, which holds the chunk's tokens from
+    // the first value's position on (the lead zero run's tokens, written
+    // later by runs_kernel, fit before it, since each token starts at its
+    // own element)
+    {
+      const int o = __shfl_sync(kAll, incT - tok, w);
+      const int fr = __shfl_sync(kAll, sg0 + dp0, w);
+      const int gw = __shfl_sync(kAll, g0, w);
+      const int nw = fr + __shfl_sync(kAll, I, w);
+      uint16_t *g = b.tok + cd.coefOff + start + lead + o;
+      for (int j = lane; j < nw; j += 32)
+        g[j] = j < fr ? run_token_at(gw, j, B, dupV) : stage[j - fr];
+    }
+    __syncwarp();  // the staged tokens are read before the next prefill
     if (threadIdx.x == 0) {
-      b.chunkTok[chunk] = (int)nTok;
-      b.chunkSpan[chunk] = make_int2(lead, (int)nTok);  // runs_kernel adds the edge runs
+      b.chunkTok[chunk] = nTok;
+      b.chunkSpan[chunk] = make_int2(lead, nTok);  // runs_kernel adds the edge runs
       if (dupV >= 0) {
-        int first = -1, last = -1;
-        for (int v = 0; v < kWarps; v++) {
-          if (first < 0) first = wFirst[par][v];
-          last = max(last, wLast[par][v]);
-        }
         const bool any = last >= 0;
-        b.chunkRun[chunk] = make_int4(any ? first : len, any ? len - 1 - last : len, any ? 0 : 1, len);
+        b.chunkRun[chunk] = make_int4(lead, any ? len - 1 - last : len, any ? 0 : 1, len);
       }
     }
-    // no barrier: the next chunk writes the other summary set, and a warp
-    // reaches this chunk's set again only after every warp has passed the
-    // next chunk's barriers
+    // one barrier per chunk: the next chunk writes the other summary set,
+    // and a warp reaches this chunk's set again only after every warp has
+    // passed the next chunk's barrier, i.e. has finished this chunk
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    singles += __shfl_xor_sync(kAll, singles, d);
+    dups += __shfl_xor_sync(kAll, dups, d);
+  }
+  if (lane == 0 && dupV >= 0) {
+    if (singles) atomicAdd(&hist[dupV], (unsigned)singles);
+    if (dups) atomicAdd(&hist[B], (unsigned)dups);
   }
   __syncthreads();
   unsigned long long *gh = b.hist + (size_t)ci * kMaxSymbols;
