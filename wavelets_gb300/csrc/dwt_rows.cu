@@ -1,0 +1,191 @@
+// Row-register wavelet pass: rows contiguous in memory on both sides, of a
+// power-of-two length L = 8 G (16 .. 256), each held by G lanes of a warp in
+// registers -- eight consecutive elements per lane, loaded and stored as
+// 16-byte words.  This is the forward z pass (the last forward pass, which
+// works in place on rows of the z-x-y layout), where the column-tile kernel
+// would stage every row through shared memory and split its levels into
+// segments with halos.
+//
+// A level with m pairs per lane (m = 4, 2, 1 for levels 0, 1, 2) lifts the
+// lane's pairs in registers and takes the neighbouring pair values from the
+// next and previous lane (four shuffles per level).  After level 2 a lane holds
+// one low-pass value; each later level gathers pair j into lane j (two
+// shuffles) and runs with fewer lanes.  Detail bands leave as soon as they
+// are final, at their band positions (low band, then detail bands of the
+// last level down to the first, dwt_cpu.cc:703-728) with the deferred
+// lifting scale, so the band order costs nothing.  Every lifting step does the
+// same arithmetic as dwt.cu and dwt_cols.cu (the same operands in the same
+// order), so the coefficients are identical.
+#include <cuda_runtime.h>
+
+#include "dwt_common.cuh"
+#include "wl_internal.h"
+
+namespace wl {
+namespace {
+using namespace dwtc;
+
+constexpr int kRegThreads = 256;
+constexpr unsigned kAll = 0xffffffffu;
+
+// One forward level, M pairs per lane (pair k of group lane `sub` is pair
+// M sub + k of the level), lanes [0, na) of the G-lane group active; the
+// mirrored ends of the lifting (dwt.cu fwd_lifting_level):
+//   d1_j = o_j + a (e_j + e_j+1)     e_h   = e_h-1
+//   s1_j = e_j + b (d1_j-1 + d1_j)   d1_-1 = d1_0
+//   d2_j = d1_j + g (s1_j + s1_j+1)  s1_h  = s1_h-1
+//   s2_j = s1_j + d (d2_j-1 + d2_j)  d2_-1 = d2_0
+// Returns the low-pass values in e[] and the details in o[].
+template <int M, int G, bool HAAR>
+__device__ __forceinline__ void fwd_level(float (&e)[M], float (&o)[M], int sub, int na) {
+  if (HAAR) {  // dwt_cpu.cc:159-162
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      const float a = e[k], b = o[k];
+      o[k] = __fmul_rn(__fsub_rn(a, b), kInvSqrt2);
+      e[k] = __fmul_rn(__fadd_rn(a, b), kInvSqrt2);
+    }
+    return;
+  }
+  const bool first = sub == 0, last = sub == na - 1;
+  float eN = __shfl_down_sync(kAll, e[0], 1, G);
+  if (last) eN = e[M - 1];
+  float d1[M], s1[M];
+#pragma unroll
+  for (int k = 0; k < M; k++) d1[k] = fmaf(kAlpha, e[k] + (k + 1 < M ? e[k + 1] : eN), o[k]);
+  float d1P = __shfl_up_sync(kAll, d1[M - 1], 1, G);
+  if (first) d1P = d1[0];
+#pragma unroll
+  for (int k = 0; k < M; k++) s1[k] = fmaf(kBeta, (k ? d1[k - 1] : d1P) + d1[k], e[k]);
+  float s1N = __shfl_down_sync(kAll, s1[0], 1, G);
+  if (last) s1N = s1[M - 1];
+#pragma unroll
+  for (int k = 0; k < M; k++) o[k] = fmaf(kGamma, s1[k] + (k + 1 < M ? s1[k + 1] : s1N), d1[k]);
+  float d2P = __shfl_up_sync(kAll, o[M - 1], 1, G);
+  if (first) d2P = o[0];
+#pragma unroll
+  for (int k = 0; k < M; k++) e[k] = fmaf(kDelta, (k ? o[k - 1] : d2P) + o[k], s1[k]);
+}
+
+// The rows [row0, row0 + kRegThreads / G) of one pass.
+template <int G, bool HAAR>
+__device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *scaleTab) {
+  constexpr int L = 8 * G;
+  const int S = d.steps;
+  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
+  const int row = row0 + (int)threadIdx.x / G;
+  const int sub = threadIdx.x & (G - 1);
+  const bool ok = row < d.rows;
+  long long bi = 0, bo = 0;
+  if (ok) {
+    const int a = row / d.B, b = row - a * d.B;
+    bi = (long long)a * d.inSA + (long long)b * d.inSB;
+    bo = (long long)a * d.outSA + (long long)b * d.outSB;
+  }
+  const float *src = static_cast<const float *>(d.in) + bi;
+  float *dst = static_cast<float *>(d.out) + bo;
+  float e[4], o[4];
+  if (ok) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(src) + 2 * sub;
+    const float4 p = s4[0], q = s4[1];
+    e[0] = p.x; o[0] = p.y; e[1] = p.z; o[1] = p.w;
+    e[2] = q.x; o[2] = q.y; e[3] = q.z; o[3] = q.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++) e[k] = o[k] = 0.f;
+  }
+  // the row is read by all its lanes before any of them stores (in place);
+  // the scale table is written
+  __syncthreads();
+
+  // level 0: four pairs per lane
+  if (S >= 1) {
+    fwd_level<4, G, HAAR>(e, o, sub, G);
+    if (ok) {
+      const float sc = scaleTab[0];
+      reinterpret_cast<float4 *>(dst + L / 2)[sub] =
+          make_float4(o[0] * sc, o[1] * sc, o[2] * sc, o[3] * sc);
+    }
+  }
+  if (S == 1) {
+    if (ok) {
+      const float sc = scaleTab[1];
+      reinterpret_cast<float4 *>(dst)[sub] = make_float4(e[0] * sc, e[1] * sc, e[2] * sc, e[3] * sc);
+    }
+    return;
+  }
+  // level 1: the four low-pass values of a lane are two pairs
+  float e1[2] = {e[0], e[2]}, o1[2] = {e[1], e[3]};
+  fwd_level<2, G, HAAR>(e1, o1, sub, G);
+  if (ok) {
+    const float sc = scaleTab[1];
+    reinterpret_cast<float2 *>(dst + L / 4)[sub] = make_float2(o1[0] * sc, o1[1] * sc);
+  }
+  if (S == 2) {
+    if (ok) {
+      const float sc = scaleTab[2];
+      reinterpret_cast<float2 *>(dst)[sub] = make_float2(e1[0] * sc, e1[1] * sc);
+    }
+    return;
+  }
+  // level 2: one pair per lane
+  float e2[1] = {e1[0]}, o2[1] = {e1[1]};
+  fwd_level<1, G, HAAR>(e2, o2, sub, G);
+  if (ok) dst[L / 8 + sub] = o2[0] * scaleTab[2];
+  // levels 3 ..: pair j gathered into lane j of the group
+  float s = e2[0];
+  int na = G;  // lanes holding a low-pass value
+  for (int lev = 3; lev < S; lev++) {
+    float ge[1] = {__shfl_sync(kAll, s, 2 * sub, G)};
+    float go[1] = {__shfl_sync(kAll, s, 2 * sub + 1, G)};
+    na >>= 1;  // pairs of this level = L >> (lev + 1)
+    fwd_level<1, G, HAAR>(ge, go, sub, na);
+    if (ok && sub < na) dst[(L >> (lev + 1)) + sub] = go[0] * scaleTab[lev];
+    s = ge[0];
+  }
+  if (ok && sub < (L >> S)) dst[sub] = s * scaleTab[S];
+}
+
+// One block: kRegThreads / G rows of the pass found by the tile prefix.
+template <int G>
+__global__ void __launch_bounds__(kRegThreads)
+dwt_rowreg_fwd_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
+                      int nPasses) {
+  __shared__ float scaleTab[16];
+  const int bid = blockIdx.x;
+  int lo = 0, hi = nPasses - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
+  }
+  const PassDesc &d = passes[lo];
+  const int row0 = (bid - tilePrefix[lo]) * (kRegThreads / G);
+  if (d.wavelet == WL_HAAR) rowreg_fwd<G, true>(d, row0, scaleTab);
+  else rowreg_fwd<G, false>(d, row0, scaleTab);
+}
+
+template <int G>
+void launch_g(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
+  dwt_rowreg_fwd_kernel<G><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
+}
+
+}  // namespace
+
+int dwt_rowreg_rows_per_block(int L) { return kRegThreads / (L / 8); }
+
+bool dwt_rowreg_fits(int L, int steps) {
+  return L >= 16 && L <= 256 && (L & (L - 1)) == 0 && steps >= 1 && (1 << steps) <= L;
+}
+
+void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int L,
+                       cudaStream_t s) {
+  switch (L) {
+    case 16: launch_g<2>(p, tp, n, blocks, s); break;
+    case 32: launch_g<4>(p, tp, n, blocks, s); break;
+    case 64: launch_g<8>(p, tp, n, blocks, s); break;
+    case 128: launch_g<16>(p, tp, n, blocks, s); break;
+    default: launch_g<32>(p, tp, n, blocks, s); break;
+  }
+}
+
+}  // namespace wl

@@ -84,6 +84,8 @@ int group_key(bool cols, int dtype, int L, bool vec = false) {
   return ((vec ? 1 : 0) << 13) | ((cols ? 1 : 0) << 12) | (dtype << 8) |
          (cols ? ceil_log2_int(L) : 0);
 }
+// row-register passes: one group per row length
+int rowreg_key(int L) { return (1 << 14) | (WL_F32 << 8) | ceil_log2_int(L); }
 
 // ---- result storage ------------------------------------------------------------
 // The arrays of all results of one compression call live in one page-locked
@@ -454,6 +456,11 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   f.out = o;
   f.outSA = Zp * Xp; f.outSB = Zp; f.outSC = 1;
   f.steps = pl.sz;
+  if (dwt_rowreg_fits(f.L, f.steps)) {
+    f.T = dwt_rowreg_rows_per_block(f.L); f.tiles = (f.rows + f.T - 1) / f.T;
+    zs[rowreg_key(f.L)].push_back(f);
+    return;
+  }
   f.T = dwt_cols_tile_rows(f.L); f.tiles = (f.rows + f.T - 1) / f.T;
   zs[group_key(true, WL_F32, f.L)].push_back(f);
 }
@@ -583,6 +590,9 @@ struct GroupLaunch {
   size_t off;
   int n, tiles, smem, rows, warps, inType, outType;
   bool inverse, cols, vec;
+  int regL;  // row-register pass of rows of regL elements (0: another kernel)
+  // bytes a launch moves, for ordering concurrent groups
+  double weight() const { return (double)tiles * (regL ? 4.0 * regL * rows : (double)smem); }
 };
 
 // Stage a group of passes (descriptors + tile prefix) at hoff of the host
@@ -591,14 +601,21 @@ struct GroupLaunch {
 // forced.
 wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int kind, int inType,
                       int outType, bool inverse, bool cols, bool vec,
-                      std::vector<GroupLaunch> &out, const TileShape *force = nullptr) {
+                      std::vector<GroupLaunch> &out, const TileShape *force = nullptr,
+                      int regL = 0) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int);
   if (hoff + bytes > ctx->hPasses.cap || hoff + bytes > ctx->passes.cap)
     return fail(ctx, WL_ENOMEM, "pass staging too small");
   int rows = 0, warps = 4;
-  if (cols) {
+  if (regL) {
+    rows = dwt_rowreg_rows_per_block(regL);
+    for (PassDesc &d : g) {
+      d.T = rows;
+      d.tiles = (d.rows + rows - 1) / rows;
+    }
+  } else if (cols) {
     int Lmax = 0;
     for (const PassDesc &d : g) Lmax = std::max(Lmax, d.L);
     const int gtype = kind == kTuneFwdX ? inType : kind == kTuneInvX ? outType : WL_F32;
@@ -617,11 +634,14 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
   for (size_t i = 0; i < n; i++) {
     tp[i] = tiles;
     tiles += g[i].tiles;
-    smem = std::max(smem, cols ? dwt_cols_smem_bytes(g[i].L, rows)
-                               : dwt_smem_bytes(g[i].L, g[i].T, g[i].exact && g[i].wavelet == WL_CDF97));
+    if (!regL)
+      smem = std::max(smem, cols ? dwt_cols_smem_bytes(g[i].L, rows)
+                                 : dwt_smem_bytes(g[i].L, g[i].T,
+                                                  g[i].exact && g[i].wavelet == WL_CDF97));
   }
   tp[n] = tiles;
-  out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec});
+  out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec,
+                 regL});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
@@ -632,8 +652,9 @@ wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind
   for (const auto &kv : gs) {
     const bool cols = (kv.first >> 12) & 1, vec = (kv.first >> 13) & 1;
     const int dt = (kv.first >> 8) & 15;
+    const int regL = (kv.first >> 14) & 1 ? kv.second[0].L : 0;
     TRY(stage_group(ctx, kv.second, hoff, kind, inverse ? WL_F32 : dt, outType, inverse, cols, vec,
-                    out));
+                    out, nullptr, regL));
   }
   return WL_OK;
 }
@@ -642,7 +663,9 @@ wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
   const char *base = P<char>(ctx->passes);
   const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
   const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
-  if (l.cols)
+  if (l.regL)
+    launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, s);
+  else if (l.cols)
     launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.warps, l.inType, l.outType, l.inverse,
                     l.vec, s);
   else
@@ -670,7 +693,7 @@ wl_status launch_phase(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a
   std::vector<size_t> order;
   for (size_t i = a; i < b; i++) order.push_back(i);
   std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
-    return (double)ls[x].tiles * ls[x].smem > (double)ls[y].tiles * ls[y].smem;
+    return ls[x].weight() > ls[y].weight();
   });
   const int nStreams = (int)std::min<size_t>(order.size(), wl_ctx::kSide + 1);
   CU(cudaEventRecord(ctx->fork, ctx->stream));

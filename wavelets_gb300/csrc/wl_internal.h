@@ -216,6 +216,12 @@ void launch_dwt_cols(const PassDesc *d_passes, const int *d_tilePrefix, int nPas
 int dwt_cols_tile_rows(int L);               // default tile height for rows of L
 int dwt_cols_smem_bytes(int L, int rows);
 bool dwt_cols_rows_fit(int L, int rows);      // rows in {32, 64, 128} and smem fits
+// row-register forward passes (dwt_rows.cu): float rows contiguous on both
+// sides, L a power of two in 16 .. 256, 1 <= steps <= log2 L
+bool dwt_rowreg_fits(int L, int steps);
+int dwt_rowreg_rows_per_block(int L);
+void launch_dwt_rowreg(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int blocks,
+                       int L, cudaStream_t s);
 
 // ---- column-tile heights per size class (tune.cpp) ----
 enum TuneKind { kTuneFwdX, kTuneFwdY, kTuneFwdZ, kTuneInvZ, kTuneInvY, kTuneInvX, kTuneKinds };
