@@ -48,6 +48,7 @@ namespace {
 using namespace dwtc;
 
 constexpr int kRows = 32;         // rows per warp (one per lane)
+constexpr int kMinSegPairs = 8;   // pairs per segment below which a level is not split
 
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -484,8 +485,11 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
   for (int it = 0; it < S; it++) {
     const int lev = INV ? S - 1 - it : it;
     const int h = (L >> lev) >> 1, P = (1 << lev) * kP;
-    const int i0 = kSegs == 1 ? 0 : (seg * h) / kSegs;
-    const int i1 = kSegs == 1 ? h : ((seg + 1) * h) / kSegs;
+    // a level of few pairs is not split: segment 0 sweeps it whole (every
+    // segment pays halo reads and a generic start and end)
+    const bool split = kSegs > 1 && h >= kMinSegPairs * kSegs;
+    const int i0 = split ? (seg * h) / kSegs : (seg == 0 ? 0 : h);
+    const int i1 = split ? ((seg + 1) * h) / kSegs : h;
     if (!lifting) {
       if (rowOk) haar_seg(x, P, i0, i1, INV);
     } else if (h == 1) {
