@@ -18,6 +18,7 @@
 // alone.  The compaction pass also builds the Lloyd histogram of every
 // |c| above the bucket, so the Lloyd quantizer needs no pass of its own.
 #include <cfloat>
+#include <type_traits>
 
 #include "wl_internal.h"
 
@@ -90,21 +91,32 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
   for (int i = threadIdx.x; i < kSelectBins; i += kThreads) hist[i] = 0;
   __syncthreads();
 
-  unsigned mn = 0xffffffffu, mx = 0u, a1 = 0u, a2 = 0u;
+  // min and max as floats, like the reference's x < min / x > max from FLT_MAX
+  // and FLT_MIN (a NaN never replaces either); ordered keys for the merge
+  float fmn = FLT_MAX, fmx = FLT_MIN;
+  unsigned a1 = 0u, a2 = 0u;
+  auto visit = [&](float x) {
+    const unsigned a = __float_as_uint(x) & 0x7fffffffu;
+    atomicAdd(&hist[a >> 20], 1u);
+    fmn = fminf(fmn, x);
+    fmx = fmaxf(fmx, x);
+    a2 = max(a2, min(a1, a));  // top2_merge(a1, a2, a, 0)
+    a1 = max(a1, a);
+  };
   for (int k = 0; k < nc; k++) {
     const int len = chunk_len(k);
     float v[kPerThread];
     load_chunk(chunk_src(k), len, v);
+    if (len == kChunk) {
 #pragma unroll
-    for (int j = 0; j < kPerThread; j++) {
-      if (chunk_index(j) >= len) continue;
-      const unsigned a = __float_as_uint(v[j]) & 0x7fffffffu;
-      atomicAdd(&hist[a >> 20], 1u);
-      mn = min(mn, ord_enc(v[j]));
-      mx = max(mx, ord_enc(v[j]));
-      top2_merge(a1, a2, a, 0u);
+      for (int j = 0; j < kPerThread; j++) visit(v[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kPerThread; j++)
+        if (chunk_index(j) < len) visit(v[j]);
     }
   }
+  unsigned mn = ord_enc(fmn), mx = ord_enc(fmx);
   for (int off = 16; off > 0; off >>= 1) {
     mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
     mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
@@ -174,13 +186,18 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
     float v[kPerThread];
     load_chunk(chunk_src(k), len, v);
     unsigned m = 0;  // candidates among this thread's values
+    auto scan = [&](auto full) {
 #pragma unroll
-    for (int j = 0; j < kPerThread; j++) {
-      const unsigned a = __float_as_uint(v[j]) & 0x7fffffffu;
-      const bool in = chunk_index(j) < len;
-      if (in && (a >> 20) == prefix) m |= 1u << j;
-      if (lloyd && in && (a >> 20) > prefix && a <= lhi) atomicAdd(&lh[(a - lbase) >> lshift], 1u);
-    }
+      for (int j = 0; j < kPerThread; j++) {
+        const unsigned a = __float_as_uint(v[j]) & 0x7fffffffu;
+        const bool in = decltype(full)::value || chunk_index(j) < len;
+        if (in && (a >> 20) == prefix) m |= 1u << j;
+        if (lloyd && in && (a >> 20) > prefix && a <= lhi)
+          atomicAdd(&lh[(a - lbase) >> lshift], 1u);
+      }
+    };
+    if (len == kChunk) scan(std::true_type());
+    else scan(std::false_type());
     // block-wide exclusive count of candidates, one reservation per chunk
     const unsigned cnt = __popc(m);
     unsigned inc = cnt;
