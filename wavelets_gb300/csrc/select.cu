@@ -160,8 +160,6 @@ select_pass0(DevBatch b, const float *__restrict__ coef) {
 __global__ void __launch_bounds__(kThreads, 6)
 select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict__ cand) {
   __shared__ unsigned lh[kLloydBins];
-  __shared__ unsigned wCnt[kThreads / 32];
-  __shared__ unsigned sBase;
   const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
@@ -179,7 +177,7 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
     for (int i = threadIdx.x; i < kLloydBins; i += kThreads) lh[i] = 0;
   __syncthreads();
 
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   unsigned *dst = cand + cd.coefOff;
   for (int k = 0; k < nc; k++) {
     const int len = chunk_len(k);
@@ -198,27 +196,20 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
     };
     if (len == kChunk) scan(std::true_type());
     else scan(std::false_type());
-    // block-wide exclusive count of candidates, one reservation per chunk
+    // warp-wide exclusive count of candidates, one reservation per warp and
+    // chunk (the candidates' order does not matter: they are only counted)
     const unsigned cnt = __popc(m);
     unsigned inc = cnt;
     for (int off = 1; off < 32; off <<= 1) {
       const unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
       if (lane >= off) inc += t;
     }
-    if (lane == 31) wCnt[w] = inc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned tot = 0;
-      for (int i = 0; i < kThreads / 32; i++) tot += wCnt[i];
-      sBase = tot ? atomicAdd(&st->candCount, tot) : 0u;
-    }
-    __syncthreads();
-    unsigned o = sBase + inc - cnt;
-    for (int i = 0; i < w; i++) o += wCnt[i];
+    unsigned base = 0;
+    if (lane == 31 && inc) base = atomicAdd(&st->candCount, inc);
+    unsigned o = __shfl_sync(0xffffffffu, base, 31) + inc - cnt;
 #pragma unroll
     for (int j = 0; j < kPerThread; j++)
       if ((m >> j) & 1u) dst[o++] = __float_as_uint(v[j]) & 0x7fffffffu;
-    __syncthreads();  // wCnt and sBase are reused by the next chunk
   }
   if (lloyd) {
     unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
@@ -383,7 +374,6 @@ __global__ void select_init(DevBatch b) {
 void launch_select(DevBatch &b, const float *coef, cudaStream_t s) {
   chunk_map_kernel<<<b.n, 256, 0, s>>>(b);
   select_init<<<(b.n + 127) / 128, 128, 0, s>>>(b);
-  const unsigned chunks = (unsigned)b.totalChunks;
   unsigned *cand = reinterpret_cast<unsigned *>(b.coef2);
   const unsigned groups = (unsigned)b.totalGroups;
   select_pass0<<<groups, kThreads, 0, s>>>(b, coef);
