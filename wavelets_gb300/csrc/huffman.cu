@@ -235,18 +235,6 @@ __device__ __forceinline__ int token_len(uint16_t t, const uint8_t *len, int dup
   return len[sym] + (sym == dupKey ? 3 : 0);
 }
 
-// block sum of unsigned long long (256 threads)
-__device__ __forceinline__ unsigned long long block_sum(unsigned long long v, unsigned long long *sh) {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) sh[w] = v;
-  __syncthreads();
-  unsigned long long t = 0;
-  for (int i = 0; i < kThreads / 32; i++) t += sh[i];
-  __syncthreads();
-  return t;
-}
-
 // exclusive block scan (256 threads)
 __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, unsigned &total) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -269,22 +257,34 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, un
 
 // Bits of a chunk: the code lengths of its tokens, read straight from its slot.
 __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
+  // one CTA per group of kQuantGroup chunks of a cubelet: the code lengths
+  // are loaded once, and each chunk's tokens are summed by kWpc warps
+  constexpr int kWpc = (kThreads / 32) / kQuantGroup;
+  static_assert(kWpc >= 1 && kWpc * kQuantGroup * 32 == kThreads, "warps per chunk");
   __shared__ uint8_t sLen[kMaxSymbols + 3];
-  __shared__ unsigned long long sh[kThreads / 32];
-  const long long chunk = blockIdx.x;
-  const int ci = b.chunkCub[chunk];
+  __shared__ unsigned sBits[kQuantGroup];
+  const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
+  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
+  const int nc = min(kQuantGroup, cd.nChunks - c0);
   const int dupKey = cd.binCount;
   const int S = cd.binCount + 1;
   for (int i = threadIdx.x; i < S; i += kThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
-  const long long cstart = (chunk - cd.chunkBase) * (long long)kChunk;
-  const int2 span = b.chunkSpan[chunk];
-  const uint16_t *src = b.tok + cd.coefOff + cstart + span.x;
+  if ((int)threadIdx.x < kQuantGroup) sBits[threadIdx.x] = 0;
   __syncthreads();
-  unsigned long long s = 0;
-  for (int i = threadIdx.x; i < span.y; i += kThreads) s += token_len(src[i], sLen, dupKey);
-  s = block_sum(s, sh);
-  if (threadIdx.x == 0) b.chunkBits[chunk] = s;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = w / kWpc, part = w % kWpc;
+  if (k < nc) {
+    const long long chunk = cd.chunkBase + c0 + k;
+    const int2 span = b.chunkSpan[chunk];
+    const uint16_t *src = b.tok + cd.coefOff + (long long)(c0 + k) * kChunk + span.x;
+    unsigned s = 0;  // at most kChunk tokens of at most 64 bits
+    for (int i = part * 32 + lane; i < span.y; i += kWpc * 32) s += token_len(src[i], sLen, dupKey);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0 && s) atomicAdd(&sBits[k], s);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nc) b.chunkBits[cd.chunkBase + c0 + threadIdx.x] = sBits[threadIdx.x];
 }
 
 // per cubelet: exclusive scan of the chunk bit counts
@@ -514,7 +514,7 @@ void launch_pack_meta(DevBatch &b, cudaStream_t s) { pack_meta_kernel<<<b.n, 256
 
 void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const unsigned chunks = (unsigned)b.totalChunks;
-  encode_count_kernel<<<chunks, kThreads, 0, s>>>(b);
+  encode_count_kernel<<<(unsigned)b.totalGroups, kThreads, 0, s>>>(b);
   encode_scan_kernel<<<b.n, 1024, 0, s>>>(b);
   cubelet_offsets_kernel<<<1, 1024, 0, s>>>(b);
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);

@@ -167,10 +167,10 @@ lloyd_deferred_kernel(DevBatch b, const float *__restrict__ coef) {
 // four CTAs per SM, so a batch of up to 4 x 152 cubelets solves in one wave.
 constexpr int kSolveThreads = 512;
 // prefix sums: counts (exact in 32 bits) and count * centre (double), block
-// scan scratch, then the codebook, midpoints and next codebook (cbCap each)
+// scan scratch, then two codebook buffers (cbCap each)
 __host__ __device__ inline size_t lloyd_smem_bytes(int cbCap) {
   return (size_t)(kLloydBins + 1) * 8 + (size_t)(kLloydBins + 2) * 4 + 64 * 8 +
-         (size_t)3 * cbCap * 4;
+         (size_t)2 * cbCap * 4;
 }
 
 __global__ void __launch_bounds__(kSolveThreads, 4) lloyd_solve_kernel(DevBatch b, int cbCap) {
@@ -179,8 +179,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) lloyd_solve_kernel(DevBatch 
   unsigned *pw = reinterpret_cast<unsigned *>(pwx + (kLloydBins + 1));
   double *scratch = reinterpret_cast<double *>(pw + (kLloydBins + 2));
   float *cb = reinterpret_cast<float *>(scratch + 64);
-  float *mid = cb + cbCap;
-  float *nxt = mid + cbCap;
+  float *nxt = cb + cbCap;
   const int ci = blockIdx.x;
   const CubeletDev cd = b.cub[ci];
   if (cd.quantAlg != WL_LLOYD) return;
@@ -253,20 +252,27 @@ __global__ void __launch_bounds__(kSolveThreads, 4) lloyd_solve_kernel(DevBatch 
     for (int i = threadIdx.x; i < cbs; i += kSolveThreads) cb[i] = lo * expf(i * logScale);
   }
   __syncthreads();
+  // one barrier per iteration: a thread forms the midpoints around its cell
+  // itself, and the codebook alternates between two buffers
+  float *cur = cb, *nx = nxt;
   for (int it = 0; it < cd.lloydIters && !degenerate; it++) {
-    for (int i = threadIdx.x; i + 1 < cbs; i += kSolveThreads) mid[i] = 0.5f * (cb[i] + cb[i + 1]);
-    __syncthreads();
     // cell i covers histogram bins [first(i), first(i+1)): first bin whose
-    // centre is >= mid[i-1]
+    // centre is >= the midpoint (cb[i-1] + cb[i]) / 2
     for (int i = threadIdx.x; i < cbs; i += kSolveThreads) {
-      const int a = i > 0 ? first_bin(mid[i - 1]) : 0;
-      int z = i + 1 < cbs ? first_bin(mid[i]) : kLloydBins;
+      const float c = cur[i];
+      const int a = i > 0 ? first_bin(0.5f * (cur[i - 1] + c)) : 0;
+      int z = i + 1 < cbs ? first_bin(0.5f * (c + cur[i + 1])) : kLloydBins;
       if (z < a) z = a;
       const double cw = (double)(pw[z] - pw[a]);
-      nxt[i] = cw > 0 ? (float)((pwx[z] - pwx[a]) / cw) : cb[i];
+      nx[i] = cw > 0 ? (float)((pwx[z] - pwx[a]) / cw) : c;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < cbs; i += kSolveThreads) cb[i] = nxt[i];
+    float *t = cur;
+    cur = nx;
+    nx = t;
+  }
+  if (cur != cb) {
+    for (int i = threadIdx.x; i < cbs; i += kSolveThreads) cb[i] = cur[i];
     __syncthreads();
   }
   // setBinsFromCodebook (test_compress_common.cc:784-846), one thread, the

@@ -211,6 +211,7 @@ select_compact(DevBatch b, const float *__restrict__ coef, unsigned *__restrict_
     for (int j = 0; j < kPerThread; j++)
       if ((m >> j) & 1u) dst[o++] = __float_as_uint(v[j]) & 0x7fffffffu;
   }
+  __syncthreads();  // every thread's Lloyd histogram counts are in
   if (lloyd) {
     unsigned *g = reinterpret_cast<unsigned *>(b.lloydHist) + (size_t)ci * kLloydBins;
     for (int i = threadIdx.x; i < kLloydBins; i += kThreads)
