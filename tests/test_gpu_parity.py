@@ -368,6 +368,24 @@ def test_full_size_transform_error_against_float64_lifting(ctx, shape, steps, wa
 
 
 
+@pytest.mark.parametrize("z,zsteps", [(16, 4), (16, 1), (32, 2), (48, 4), (48, 1), (48, 3),
+                                      (64, 6), (96, 5), (96, 2), (128, 3), (192, 6),
+                                      (192, 1), (256, 8), (256, 4)])
+@pytest.mark.parametrize("wavelet", [P.CDF97, P.HAAR])
+def test_row_register_z_lengths_against_float64_lifting(ctx, z, zsteps, wavelet):
+    """z rows of every length the row-register pass takes (8 or 6 elements
+    per lane, every level count), 240 rows so that the last block is ragged."""
+    from oracle import lifting64
+    a = synth.scaled_blob_cubelet(np.random.default_rng(z * 31 + zsteps), (z, 12, 20),
+                                  np.float32)
+    steps = (2, 2, zsteps)
+    p = P.Params(steps=steps, wavelet=wavelet)
+    coeffs, _ = ctx.forward_transform(a, p)
+    ref, _ = lifting64.forward(a, steps, wavelet)
+    err = float(np.abs(coeffs - ref).max()) / float(np.abs(ref).max())
+    assert err <= FP64_RTOL
+
+
 @pytest.mark.parametrize("two_d_steps", [(-1, -1, -1), (3, 2, 0), (0, 2, 3), (4, 4, 1)])
 def test_2d_mode_batched_equals_single_and_round_trips(ctx, two_d_steps, tmp_path):
     """-2d on the column-tile kernel (lifting): a batch of mixed sizes equals

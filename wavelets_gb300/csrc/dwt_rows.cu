@@ -67,10 +67,13 @@ __device__ __forceinline__ void fwd_level(float (&e)[M], float (&o)[M], int sub,
   for (int k = 0; k < M; k++) e[k] = fmaf(kDelta, (k ? o[k - 1] : d2P) + o[k], s1[k]);
 }
 
-// The rows [row0, row0 + kRegThreads / G) of one pass.
-template <int G, bool HAAR>
+// The rows [row0, row0 + kRegThreads / G) of one pass; E = 8 or 6 elements
+// per lane (L = E G).
+template <int G, int E, bool HAAR>
 __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *scaleTab) {
-  constexpr int L = 8 * G;
+  constexpr int L = E * G;
+  constexpr int M = E / 2;                // level-0 pairs per lane
+  constexpr int NA1 = M == 4 ? G : 3 * G / 4;  // lanes of levels 1 and 2 (two pairs, one pair)
   const int S = d.steps;
   if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
   const int row = row0 + (int)threadIdx.x / G;
@@ -84,45 +87,77 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
   }
   const float *src = static_cast<const float *>(d.in) + bi;
   float *dst = static_cast<float *>(d.out) + bo;
-  float e[4], o[4];
+  float e[M], o[M];
   if (ok) {
-    const float4 *s4 = reinterpret_cast<const float4 *>(src) + 2 * sub;
-    const float4 p = s4[0], q = s4[1];
-    e[0] = p.x; o[0] = p.y; e[1] = p.z; o[1] = p.w;
-    e[2] = q.x; o[2] = q.y; e[3] = q.z; o[3] = q.w;
+    if (M == 4) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(src) + 2 * sub;
+      const float4 p = s4[0], q = s4[1];
+      e[0] = p.x; o[0] = p.y; e[1] = p.z; o[1] = p.w;
+      e[2 % M] = q.x; o[2 % M] = q.y; e[3 % M] = q.z; o[3 % M] = q.w;
+    } else {
+      const float2 *s2 = reinterpret_cast<const float2 *>(src) + 3 * sub;
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float2 p = s2[k];
+        e[k] = p.x;
+        o[k] = p.y;
+      }
+    }
   } else {
 #pragma unroll
-    for (int k = 0; k < 4; k++) e[k] = o[k] = 0.f;
+    for (int k = 0; k < M; k++) e[k] = o[k] = 0.f;
   }
   // the row is read by all its lanes before any of them stores (in place);
   // the scale table is written
   __syncthreads();
 
-  // level 0: four pairs per lane
-  if (S >= 1) {
-    fwd_level<4, G, HAAR>(e, o, sub, G);
-    if (ok) {
-      const float sc = scaleTab[0];
+  // level 0: M pairs per lane
+  fwd_level<M, G, HAAR>(e, o, sub, G);
+  if (ok) {
+    const float sc = scaleTab[0];
+    if (M == 4) {
       reinterpret_cast<float4 *>(dst + L / 2)[sub] =
-          make_float4(o[0] * sc, o[1] * sc, o[2] * sc, o[3] * sc);
+          make_float4(o[0] * sc, o[1 % M] * sc, o[2 % M] * sc, o[3 % M] * sc);
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; k++) dst[L / 2 + M * sub + k] = o[k] * sc;
     }
   }
   if (S == 1) {
     if (ok) {
       const float sc = scaleTab[1];
-      reinterpret_cast<float4 *>(dst)[sub] = make_float4(e[0] * sc, e[1] * sc, e[2] * sc, e[3] * sc);
+#pragma unroll
+      for (int k = 0; k < M; k++) dst[M * sub + k] = e[k] * sc;
     }
     return;
   }
-  // level 1: the four low-pass values of a lane are two pairs
-  float e1[2] = {e[0], e[2]}, o1[2] = {e[1], e[3]};
-  fwd_level<2, G, HAAR>(e1, o1, sub, G);
-  if (ok) {
+  // level 1: lane j of the first NA1 holds the low-pass values 4j .. 4j+3,
+  // two pairs (with three per lane they are gathered from the lanes that
+  // hold them)
+  float q4[4];
+  if (M == 4) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) q4[r] = e[r % M];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int v = min(4 * sub + r, L / 2 - 1);
+      const int from = v / 3, reg = v - 3 * from;
+      const float a = __shfl_sync(kAll, e[0], from, G);
+      const float b = __shfl_sync(kAll, e[1 % M], from, G);
+      const float c = __shfl_sync(kAll, e[2 % M], from, G);
+      q4[r] = reg == 0 ? a : (reg == 1 ? b : c);
+    }
+  }
+  const bool act1 = sub < NA1;
+  float e1[2] = {q4[0], q4[2]}, o1[2] = {q4[1], q4[3]};
+  fwd_level<2, G, HAAR>(e1, o1, sub, NA1);
+  if (ok && act1) {
     const float sc = scaleTab[1];
     reinterpret_cast<float2 *>(dst + L / 4)[sub] = make_float2(o1[0] * sc, o1[1] * sc);
   }
   if (S == 2) {
-    if (ok) {
+    if (ok && act1) {
       const float sc = scaleTab[2];
       reinterpret_cast<float2 *>(dst)[sub] = make_float2(e1[0] * sc, e1[1] * sc);
     }
@@ -130,14 +165,14 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
   }
   // level 2: one pair per lane
   float e2[1] = {e1[0]}, o2[1] = {e1[1]};
-  fwd_level<1, G, HAAR>(e2, o2, sub, G);
-  if (ok) dst[L / 8 + sub] = o2[0] * scaleTab[2];
+  fwd_level<1, G, HAAR>(e2, o2, sub, NA1);
+  if (ok && act1) dst[L / 8 + sub] = o2[0] * scaleTab[2];
   // levels 3 ..: pair j gathered into lane j of the group
   float s = e2[0];
-  int na = G;  // lanes holding a low-pass value
+  int na = NA1;  // lanes holding a low-pass value
   for (int lev = 3; lev < S; lev++) {
-    float ge[1] = {__shfl_sync(kAll, s, 2 * sub, G)};
-    float go[1] = {__shfl_sync(kAll, s, 2 * sub + 1, G)};
+    float ge[1] = {__shfl_sync(kAll, s, (2 * sub) & (G - 1), G)};
+    float go[1] = {__shfl_sync(kAll, s, (2 * sub + 1) & (G - 1), G)};
     na >>= 1;  // pairs of this level = L >> (lev + 1)
     fwd_level<1, G, HAAR>(ge, go, sub, na);
     if (ok && sub < na) dst[(L >> (lev + 1)) + sub] = go[0] * scaleTab[lev];
@@ -147,7 +182,7 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
 }
 
 // One block: kRegThreads / G rows of the pass found by the tile prefix.
-template <int G>
+template <int G, int E>
 __global__ void __launch_bounds__(kRegThreads)
 dwt_rowreg_fwd_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                       int nPasses) {
@@ -160,21 +195,29 @@ dwt_rowreg_fwd_kernel(const PassDesc *__restrict__ passes, const int *__restrict
   }
   const PassDesc &d = passes[lo];
   const int row0 = (bid - tilePrefix[lo]) * (kRegThreads / G);
-  if (d.wavelet == WL_HAAR) rowreg_fwd<G, true>(d, row0, scaleTab);
-  else rowreg_fwd<G, false>(d, row0, scaleTab);
+  if (d.wavelet == WL_HAAR) rowreg_fwd<G, E, true>(d, row0, scaleTab);
+  else rowreg_fwd<G, E, false>(d, row0, scaleTab);
 }
 
-template <int G>
+template <int G, int E = 8>
 void launch_g(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
-  dwt_rowreg_fwd_kernel<G><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
+  dwt_rowreg_fwd_kernel<G, E><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
 }
 
 }  // namespace
 
-int dwt_rowreg_rows_per_block(int L) { return kRegThreads / (L / 8); }
+// rows of 8 G elements (G = 2 .. 32) or 6 G (G = 8, 16, 32)
+static int rowreg_lanes(int L) {
+  if (L >= 16 && L <= 256 && (L & (L - 1)) == 0) return L / 8;
+  if (L == 48 || L == 96 || L == 192) return L / 6;
+  return 0;
+}
+
+int dwt_rowreg_rows_per_block(int L) { return kRegThreads / rowreg_lanes(L); }
 
 bool dwt_rowreg_fits(int L, int steps) {
-  return L >= 16 && L <= 256 && (L & (L - 1)) == 0 && steps >= 1 && (1 << steps) <= L;
+  return rowreg_lanes(L) > 0 && steps >= 1 && L % (1 << steps) == 0 &&
+         (L & (L - 1) ? (L >> steps) >= 3 : true);
 }
 
 void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int L,
@@ -182,8 +225,11 @@ void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int 
   switch (L) {
     case 16: launch_g<2>(p, tp, n, blocks, s); break;
     case 32: launch_g<4>(p, tp, n, blocks, s); break;
+    case 48: launch_g<8, 6>(p, tp, n, blocks, s); break;
     case 64: launch_g<8>(p, tp, n, blocks, s); break;
+    case 96: launch_g<16, 6>(p, tp, n, blocks, s); break;
     case 128: launch_g<16>(p, tp, n, blocks, s); break;
+    case 192: launch_g<32, 6>(p, tp, n, blocks, s); break;
     default: launch_g<32>(p, tp, n, blocks, s); break;
   }
 }

@@ -85,7 +85,7 @@ int group_key(bool cols, int dtype, int L, bool vec = false) {
          (cols ? ceil_log2_int(L) : 0);
 }
 // row-register passes: one group per row length
-int rowreg_key(int L) { return (1 << 14) | (WL_F32 << 8) | ceil_log2_int(L); }
+int rowreg_key(int L) { return (1 << 20) | L; }
 
 // ---- result storage ------------------------------------------------------------
 // The arrays of all results of one compression call live in one page-locked
@@ -650,9 +650,9 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
 wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind, int outType,
                        bool inverse, std::vector<GroupLaunch> &out) {
   for (const auto &kv : gs) {
-    const bool cols = (kv.first >> 12) & 1, vec = (kv.first >> 13) & 1;
-    const int dt = (kv.first >> 8) & 15;
-    const int regL = (kv.first >> 14) & 1 ? kv.second[0].L : 0;
+    const int regL = (kv.first >> 20) & 1 ? kv.second[0].L : 0;
+    const bool cols = !regL && ((kv.first >> 12) & 1), vec = !regL && ((kv.first >> 13) & 1);
+    const int dt = regL ? WL_F32 : (kv.first >> 8) & 15;
     TRY(stage_group(ctx, kv.second, hoff, kind, inverse ? WL_F32 : dt, outType, inverse, cols, vec,
                     out, nullptr, regL));
   }
