@@ -18,6 +18,8 @@
 // order), so the coefficients are identical.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "dwt_common.cuh"
 #include "wl_internal.h"
 
@@ -67,67 +69,54 @@ __device__ __forceinline__ void fwd_level(float (&e)[M], float (&o)[M], int sub,
   for (int k = 0; k < M; k++) e[k] = fmaf(kDelta, (k ? o[k - 1] : d2P) + o[k], s1[k]);
 }
 
-// The rows [row0, row0 + kRegThreads / G) of one pass; E = 8 or 6 elements
-// per lane (L = E G).
-template <int G, int E, bool HAAR>
-__device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *scaleTab) {
-  constexpr int L = E * G;
-  constexpr int M = E / 2;                // level-0 pairs per lane
-  constexpr int NA1 = M == 4 ? G : 3 * G / 4;  // lanes of levels 1 and 2 (two pairs, one pair)
-  const int S = d.steps;
-  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
-  const int row = row0 + (int)threadIdx.x / G;
-  const int sub = threadIdx.x & (G - 1);
-  const bool ok = row < d.rows;
-  long long bi = 0, bo = 0;
-  if (ok) {
-    const int a = row / d.B, b = row - a * d.B;
-    bi = (long long)a * d.inSA + (long long)b * d.inSB;
-    bo = (long long)a * d.outSA + (long long)b * d.outSB;
+// Where the finished values of a row go: band position q of the row.
+// put4 / put2 take 4 / 2 consecutive positions starting at a multiple of 4 / 2.
+struct GlobalRow {  // the row itself, in place (float row, 16-byte aligned)
+  float *dst;
+  __device__ void put(int q, float v) const { dst[q] = v; }
+  __device__ void put2(int q, float a, float b) const {
+    *reinterpret_cast<float2 *>(dst + q) = make_float2(a, b);
   }
-  const float *src = static_cast<const float *>(d.in) + bi;
-  float *dst = static_cast<float *>(d.out) + bo;
-  float e[M], o[M];
-  if (ok) {
-    if (M == 4) {
-      const float4 *s4 = reinterpret_cast<const float4 *>(src) + 2 * sub;
-      const float4 p = s4[0], q = s4[1];
-      e[0] = p.x; o[0] = p.y; e[1] = p.z; o[1] = p.w;
-      e[2 % M] = q.x; o[2 % M] = q.y; e[3 % M] = q.z; o[3 % M] = q.w;
-    } else {
-      const float2 *s2 = reinterpret_cast<const float2 *>(src) + 3 * sub;
-#pragma unroll
-      for (int k = 0; k < M; k++) {
-        const float2 p = s2[k];
-        e[k] = p.x;
-        o[k] = p.y;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < M; k++) e[k] = o[k] = 0.f;
+  __device__ void put4(int q, float a, float b, float c, float d) const {
+    *reinterpret_cast<float4 *>(dst + q) = make_float4(a, b, c, d);
   }
-  // the row is read by all its lanes before any of them stores (in place);
-  // the scale table is written
-  __syncthreads();
+};
+struct TileRow {  // column r of a shared-memory tile, position q at q * P + r
+  float *col;
+  int P;
+  __device__ void put(int q, float v) const { col[q * P] = v; }
+  __device__ void put2(int q, float a, float b) const { put(q, a); put(q + 1, b); }
+  __device__ void put4(int q, float a, float b, float c, float d) const {
+    put(q, a); put(q + 1, b); put(q + 2, c); put(q + 3, d);
+  }
+};
 
+// All levels of rows of L = E G elements held E per lane (e: even, o: odd
+// elements of the lane's M = E / 2 pairs), each value handed to out.put*
+// (when ok) at its band position with the deferred lifting scale.
+template <int G, int E, bool HAAR, class Out>
+__device__ __forceinline__ void rowreg_levels(float (&e)[E / 2], float (&o)[E / 2], int sub,
+                                              int S, const float *scaleTab, bool ok,
+                                              const Out &out) {
+  constexpr int L = E * G;
+  constexpr int M = E / 2;                     // level-0 pairs per lane
+  constexpr int NA1 = M == 4 ? G : 3 * G / 4;  // lanes of levels 1 and 2
   // level 0: M pairs per lane
   fwd_level<M, G, HAAR>(e, o, sub, G);
   if (ok) {
     const float sc = scaleTab[0];
-    if (M == 4) {
-      reinterpret_cast<float4 *>(dst + L / 2)[sub] =
-          make_float4(o[0] * sc, o[1 % M] * sc, o[2 % M] * sc, o[3 % M] * sc);
-    } else {
+    if (M == 4) out.put4(L / 2 + 4 * sub, o[0] * sc, o[1 % M] * sc, o[2 % M] * sc, o[3 % M] * sc);
+    else
 #pragma unroll
-      for (int k = 0; k < M; k++) dst[L / 2 + M * sub + k] = o[k] * sc;
-    }
+      for (int k = 0; k < M; k++) out.put(L / 2 + M * sub + k, o[k] * sc);
   }
   if (S == 1) {
     if (ok) {
       const float sc = scaleTab[1];
+      if (M == 4) out.put4(4 * sub, e[0] * sc, e[1 % M] * sc, e[2 % M] * sc, e[3 % M] * sc);
+      else
 #pragma unroll
-      for (int k = 0; k < M; k++) dst[M * sub + k] = e[k] * sc;
+        for (int k = 0; k < M; k++) out.put(M * sub + k, e[k] * sc);
     }
     return;
   }
@@ -154,19 +143,19 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
   fwd_level<2, G, HAAR>(e1, o1, sub, NA1);
   if (ok && act1) {
     const float sc = scaleTab[1];
-    reinterpret_cast<float2 *>(dst + L / 4)[sub] = make_float2(o1[0] * sc, o1[1] * sc);
+    out.put2(L / 4 + 2 * sub, o1[0] * sc, o1[1] * sc);
   }
   if (S == 2) {
     if (ok && act1) {
       const float sc = scaleTab[2];
-      reinterpret_cast<float2 *>(dst)[sub] = make_float2(e1[0] * sc, e1[1] * sc);
+      out.put2(2 * sub, e1[0] * sc, e1[1] * sc);
     }
     return;
   }
   // level 2: one pair per lane
   float e2[1] = {e1[0]}, o2[1] = {e1[1]};
   fwd_level<1, G, HAAR>(e2, o2, sub, NA1);
-  if (ok && act1) dst[L / 8 + sub] = o2[0] * scaleTab[2];
+  if (ok && act1) out.put(L / 8 + sub, o2[0] * scaleTab[2]);
   // levels 3 ..: pair j gathered into lane j of the group
   float s = e2[0];
   int na = NA1;  // lanes holding a low-pass value
@@ -175,10 +164,219 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
     float go[1] = {__shfl_sync(kAll, s, (2 * sub + 1) & (G - 1), G)};
     na >>= 1;  // pairs of this level = L >> (lev + 1)
     fwd_level<1, G, HAAR>(ge, go, sub, na);
-    if (ok && sub < na) dst[(L >> (lev + 1)) + sub] = go[0] * scaleTab[lev];
+    if (ok && sub < na) out.put((L >> (lev + 1)) + sub, go[0] * scaleTab[lev]);
     s = ge[0];
   }
-  if (ok && sub < (L >> S)) dst[sub] = s * scaleTab[S];
+  if (ok && sub < (L >> S)) out.put(sub, s * scaleTab[S]);
+}
+
+// The rows [row0, row0 + kRegThreads / G) of one in-place pass of float rows;
+// E = 8 or 6 elements per lane (L = E G).
+template <int G, int E, bool HAAR>
+__device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *scaleTab) {
+  constexpr int M = E / 2;
+  const int S = d.steps;
+  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
+  const int row = row0 + (int)threadIdx.x / G;
+  const int sub = threadIdx.x & (G - 1);
+  const bool ok = row < d.rows;
+  long long bi = 0, bo = 0;
+  if (ok) {
+    const int a = row / d.B, b = row - a * d.B;
+    bi = (long long)a * d.inSA + (long long)b * d.inSB;
+    bo = (long long)a * d.outSA + (long long)b * d.outSB;
+  }
+  const float *src = static_cast<const float *>(d.in) + bi;
+  float e[M], o[M];
+  if (ok) {
+    if (M == 4) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(src) + 2 * sub;
+      const float4 p = s4[0], q = s4[1];
+      e[0] = p.x; o[0] = p.y; e[1] = p.z; o[1] = p.w;
+      e[2 % M] = q.x; o[2 % M] = q.y; e[3 % M] = q.z; o[3 % M] = q.w;
+    } else {
+      const float2 *s2 = reinterpret_cast<const float2 *>(src) + 3 * sub;
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float2 p = s2[k];
+        e[k] = p.x;
+        o[k] = p.y;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; k++) e[k] = o[k] = 0.f;
+  }
+  // the row is read by all its lanes before any of them stores (in place);
+  // the scale table is written
+  __syncthreads();
+  rowreg_levels<G, E, HAAR>(e, o, sub, S, scaleTab, ok,
+                            GlobalRow{static_cast<float *>(d.out) + bo});
+}
+
+// E elements [first, first + E) of a row of n real elements as floats: one
+// to three vector loads when the run is whole and aligned, else element by
+// element with the REPEAT clamp to the last real element.
+template <typename InT, int E>
+__device__ __forceinline__ void load_run(const InT *row, int first, int n, float (&v)[E]) {
+  const InT *p = row + first;
+  const size_t addr = reinterpret_cast<size_t>(p);
+  if (first + E <= n) {
+    if (sizeof(InT) == 4 && E == 8 && (addr & 15) == 0) {
+      const uint4 a = reinterpret_cast<const uint4 *>(p)[0], b = reinterpret_cast<const uint4 *>(p)[1];
+      const unsigned w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int k = 0; k < E; k++)
+        v[k] = sizeof(InT) == 4 && std::is_same<InT, float>::value ? __uint_as_float(w[k % 8])
+                                                                     : (float)(int)w[k % 8];
+      return;
+    }
+    if (sizeof(InT) == 4 && E == 6 && (addr & 7) == 0) {
+      const uint2 *q = reinterpret_cast<const uint2 *>(p);
+      const uint2 a = q[0], b = q[1], c = q[2];
+      const unsigned w[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
+#pragma unroll
+      for (int k = 0; k < E; k++)
+        v[k] = std::is_same<InT, float>::value ? __uint_as_float(w[k % 6]) : (float)(int)w[k % 6];
+      return;
+    }
+    if (sizeof(InT) == 2 && E == 8 && (addr & 15) == 0) {
+      const uint4 a = reinterpret_cast<const uint4 *>(p)[0];
+      const unsigned w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = (float)((w[(k / 2) % 4] >> (16 * (k & 1))) & 0xffffu);
+      return;
+    }
+    if (sizeof(InT) == 2 && E == 6 && (addr & 3) == 0) {
+      const unsigned *q = reinterpret_cast<const unsigned *>(p);
+      const unsigned w[3] = {q[0], q[1], q[2]};
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = (float)((w[(k / 2) % 3] >> (16 * (k & 1))) & 0xffffu);
+      return;
+    }
+    if (sizeof(InT) == 1 && E == 8 && (addr & 7) == 0) {
+      const uint2 a = reinterpret_cast<const uint2 *>(p)[0];
+      const unsigned w[2] = {a.x, a.y};
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = (float)((w[(k / 4) % 2] >> (8 * (k & 3))) & 0xffu);
+      return;
+    }
+    if (sizeof(InT) == 1 && E == 6 && (addr & 1) == 0) {
+      const unsigned short *q = reinterpret_cast<const unsigned short *>(p);
+      const unsigned w[3] = {q[0], q[1], q[2]};
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = (float)((w[(k / 2) % 3] >> (8 * (k & 1))) & 0xffu);
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < E; k++) v[k] = load_as_float(row + min(first + k, n - 1));
+}
+
+// Rows contiguous in memory read into registers (any element type, REPEAT
+// clamp to the real row length and row range), finished values written as
+// columns of a shared-memory tile of R rows, then stored position by
+// position: a warp writes one position of 32 consecutive rows, which are
+// neighbours in the output (the forward x and y passes).
+template <int G> struct TileRows {
+  static constexpr int kPerRound = kRegThreads / G;  // rows one round of the block holds
+  static constexpr int R = kPerRound > 32 ? kPerRound : 32;
+  static constexpr int P = R + 1;  // odd stride: a position of 32 rows is conflict-free
+};
+
+template <typename InT, int G, int E, bool HAAR>
+__device__ __forceinline__ void rowreg_t(const PassDesc &d, int tile, float *tileSm,
+                                         float *scaleTab, long long *rowOut) {
+  constexpr int L = E * G;
+  constexpr int M = E / 2;
+  constexpr int R = TileRows<G>::R, P = TileRows<G>::P, kPerRound = TileRows<G>::kPerRound;
+  const int S = d.steps;
+  const int r0 = tile * R;
+  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
+  for (int t = threadIdx.x; t < R; t += kRegThreads) {
+    const int row = r0 + t;
+    long long bo = -1;
+    if (row < d.rows) {
+      const int a = row / d.B, b = row - a * d.B;
+      bo = (long long)a * d.outSA + (long long)b * d.outSB;
+    }
+    rowOut[t] = bo;
+  }
+  __syncthreads();
+  const int sub = threadIdx.x & (G - 1);
+  const int n = min(L, d.clampL);  // real elements of a row
+  const InT *in = static_cast<const InT *>(d.in);
+  for (int rr = (int)threadIdx.x / G; rr < R; rr += kPerRound) {
+    const int row = r0 + rr;
+    const bool ok = row < d.rows;
+    float v[E];
+    if (ok) {
+      const int a = row / d.B, b = row - a * d.B;
+      const long long bi = (long long)min(a, d.clampA - 1) * d.inSA +
+                           (long long)min(b, d.clampB - 1) * d.inSB;
+      load_run<InT, E>(in + bi, E * sub, n, v);
+    } else {
+#pragma unroll
+      for (int k = 0; k < E; k++) v[k] = 0.f;
+    }
+    float e[M], o[M];
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      e[k] = v[2 * k];
+      o[k] = v[2 * k + 1];
+    }
+    rowreg_levels<G, E, HAAR>(e, o, sub, S, scaleTab, ok, TileRow{tileSm + rr, P});
+  }
+  __syncthreads();
+  float *out = static_cast<float *>(d.out);
+  const long long outSC = d.outSC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = warp; q < L; q += kRegThreads / 32)
+    for (int rr = lane; rr < R; rr += 32) {
+      const long long bo = rowOut[rr];
+      if (bo >= 0) out[bo + q * outSC] = tileSm[q * P + rr];
+    }
+}
+
+template <typename InT, int G, int E>
+__global__ void __launch_bounds__(kRegThreads)
+dwt_rowreg_t_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
+                    int nPasses) {
+  extern __shared__ float tileSm[];
+  __shared__ float scaleTab[16];
+  __shared__ long long rowOut[TileRows<G>::R];
+  const int bid = blockIdx.x;
+  int lo = 0, hi = nPasses - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
+  }
+  const PassDesc &d = passes[lo];
+  const int tile = bid - tilePrefix[lo];
+  if (d.wavelet == WL_HAAR) rowreg_t<InT, G, E, true>(d, tile, tileSm, scaleTab, rowOut);
+  else rowreg_t<InT, G, E, false>(d, tile, tileSm, scaleTab, rowOut);
+}
+
+template <typename InT, int G, int E = 8>
+void launch_tg(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
+  const int smem = E * G * TileRows<G>::P * (int)sizeof(float);
+  auto k = dwt_rowreg_t_kernel<InT, G, E>;
+  if (smem > 48 * 1024) raise_smem_limit(k, smem);
+  k<<<blocks, kRegThreads, smem, s>>>(p, tp, n);
+}
+
+template <typename InT>
+void launch_t_len(const PassDesc *p, const int *tp, int n, int blocks, int L, cudaStream_t s) {
+  switch (L) {
+    case 16: launch_tg<InT, 2>(p, tp, n, blocks, s); break;
+    case 32: launch_tg<InT, 4>(p, tp, n, blocks, s); break;
+    case 48: launch_tg<InT, 8, 6>(p, tp, n, blocks, s); break;
+    case 64: launch_tg<InT, 8>(p, tp, n, blocks, s); break;
+    case 96: launch_tg<InT, 16, 6>(p, tp, n, blocks, s); break;
+    case 128: launch_tg<InT, 16>(p, tp, n, blocks, s); break;
+    case 192: launch_tg<InT, 32, 6>(p, tp, n, blocks, s); break;
+    default: launch_tg<InT, 32>(p, tp, n, blocks, s); break;
+  }
 }
 
 // One block: kRegThreads / G rows of the pass found by the tile prefix.
@@ -218,6 +416,26 @@ int dwt_rowreg_rows_per_block(int L) { return kRegThreads / rowreg_lanes(L); }
 bool dwt_rowreg_fits(int L, int steps) {
   return rowreg_lanes(L) > 0 && steps >= 1 && L % (1 << steps) == 0 &&
          (L & (L - 1) ? (L >> steps) >= 3 : true);
+}
+
+int dwt_rowreg_t_rows_per_block(int L) {
+  switch (rowreg_lanes(L)) {
+    case 2: return TileRows<2>::R;
+    case 4: return TileRows<4>::R;
+    case 8: return TileRows<8>::R;
+    case 16: return TileRows<16>::R;
+    default: return TileRows<32>::R;
+  }
+}
+
+void launch_dwt_rowreg_t(const PassDesc *p, const int *tp, int n, int blocks, int L, int inType,
+                         cudaStream_t s) {
+  switch (inType) {
+    case WL_U8: launch_t_len<uint8_t>(p, tp, n, blocks, L, s); break;
+    case WL_U16: launch_t_len<uint16_t>(p, tp, n, blocks, L, s); break;
+    case WL_I32: launch_t_len<int32_t>(p, tp, n, blocks, L, s); break;
+    default: launch_t_len<float>(p, tp, n, blocks, L, s); break;
+  }
 }
 
 void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int L,

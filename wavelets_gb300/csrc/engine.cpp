@@ -84,8 +84,10 @@ int group_key(bool cols, int dtype, int L, bool vec = false) {
   return ((vec ? 1 : 0) << 13) | ((cols ? 1 : 0) << 12) | (dtype << 8) |
          (cols ? ceil_log2_int(L) : 0);
 }
-// row-register passes: one group per row length
+// row-register passes: one group per row length (and source type for the
+// passes stored through a tile)
 int rowreg_key(int L) { return (1 << 20) | L; }
+int rowreg_t_key(int dtype, int L) { return (1 << 21) | (dtype << 16) | L; }
 
 // ---- result storage ------------------------------------------------------------
 // The arrays of all results of one compression call live in one page-locked
@@ -424,7 +426,8 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   memset(&d, 0, sizeof d);
   d.cropL = d.cropB = d.cropA = big;
   d.wavelet = pl.p.wavelet;
-  // x pass: rows (a = y, b = z), REPEAT padding by clamping
+  // x pass: rows (a = y, b = z) of the source, REPEAT padding by clamping,
+  // to z-y-x (z fastest): consecutive rows are neighbours in the output
   d.in = in;
   d.vecLoad = hostIn ? 1 : 0;
   d.inSA = pl.pitchY; d.inSB = pl.pitchZ; d.inSC = 1;
@@ -433,9 +436,15 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   d.out = o2;
   d.outSA = Zp; d.outSB = 1; d.outSC = Zp * Yp;
   d.steps = pl.sx;
-  d.T = dwt_cols_tile_rows(d.L); d.tiles = (d.rows + d.T - 1) / d.T;
-  xs[group_key(true, pl.dtype, d.L, hostIn && dtype_size(pl.dtype) < 4)].push_back(d);
-  // y pass: rows (a = x, b = z) of z-y-x -> z-x-y
+  if (dwt_rowreg_fits(d.L, d.steps)) {
+    d.T = dwt_rowreg_t_rows_per_block(d.L); d.tiles = (d.rows + d.T - 1) / d.T;
+    xs[rowreg_t_key(pl.dtype, d.L)].push_back(d);
+  } else {
+    d.T = dwt_cols_tile_rows(d.L); d.tiles = (d.rows + d.T - 1) / d.T;
+    xs[group_key(true, pl.dtype, d.L, hostIn && dtype_size(pl.dtype) < 4)].push_back(d);
+  }
+  // y pass: rows (a = x, b = z) of z-y-x -> z-x-y (column tiles: rows that
+  // are neighbours in memory on both sides)
   PassDesc e = d;
   e.clampL = e.clampB = e.clampA = big;
   e.vecLoad = 0;
@@ -591,6 +600,7 @@ struct GroupLaunch {
   int n, tiles, smem, rows, warps, inType, outType;
   bool inverse, cols, vec;
   int regL;  // row-register pass of rows of regL elements (0: another kernel)
+  bool regT;  // ... stored through a tile (the forward x and y passes)
   // bytes a launch moves, for ordering concurrent groups
   double weight() const { return (double)tiles * (regL ? 4.0 * regL * rows : (double)smem); }
 };
@@ -602,7 +612,7 @@ struct GroupLaunch {
 wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int kind, int inType,
                       int outType, bool inverse, bool cols, bool vec,
                       std::vector<GroupLaunch> &out, const TileShape *force = nullptr,
-                      int regL = 0) {
+                      int regL = 0, bool regT = false) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int);
@@ -610,7 +620,7 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
     return fail(ctx, WL_ENOMEM, "pass staging too small");
   int rows = 0, warps = 4;
   if (regL) {
-    rows = dwt_rowreg_rows_per_block(regL);
+    rows = regT ? dwt_rowreg_t_rows_per_block(regL) : dwt_rowreg_rows_per_block(regL);
     for (PassDesc &d : g) {
       d.T = rows;
       d.tiles = (d.rows + rows - 1) / rows;
@@ -641,7 +651,7 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
   }
   tp[n] = tiles;
   out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec,
-                 regL});
+                 regL, regT});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
@@ -650,11 +660,12 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
 wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind, int outType,
                        bool inverse, std::vector<GroupLaunch> &out) {
   for (const auto &kv : gs) {
-    const int regL = (kv.first >> 20) & 1 ? kv.second[0].L : 0;
+    const bool regT = (kv.first >> 21) & 1;
+    const int regL = regT || ((kv.first >> 20) & 1) ? kv.second[0].L : 0;
     const bool cols = !regL && ((kv.first >> 12) & 1), vec = !regL && ((kv.first >> 13) & 1);
-    const int dt = regL ? WL_F32 : (kv.first >> 8) & 15;
+    const int dt = regT ? (kv.first >> 16) & 15 : regL ? WL_F32 : (kv.first >> 8) & 15;
     TRY(stage_group(ctx, kv.second, hoff, kind, inverse ? WL_F32 : dt, outType, inverse, cols, vec,
-                    out, nullptr, regL));
+                    out, nullptr, regL, regT));
   }
   return WL_OK;
 }
@@ -663,7 +674,9 @@ wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
   const char *base = P<char>(ctx->passes);
   const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
   const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
-  if (l.regL)
+  if (l.regL && l.regT)
+    launch_dwt_rowreg_t(dp, dtp, l.n, l.tiles, l.regL, l.inType, s);
+  else if (l.regL)
     launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, s);
   else if (l.cols)
     launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.warps, l.inType, l.outType, l.inverse,

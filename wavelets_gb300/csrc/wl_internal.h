@@ -222,6 +222,12 @@ bool dwt_rowreg_fits(int L, int steps);
 int dwt_rowreg_rows_per_block(int L);
 void launch_dwt_rowreg(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int blocks,
                        int L, cudaStream_t s);
+// the same with the rows read from any element type (REPEAT clamp) and
+// stored through a shared-memory tile to an output where consecutive rows
+// are neighbours (forward x and y passes)
+int dwt_rowreg_t_rows_per_block(int L);
+void launch_dwt_rowreg_t(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
+                         int blocks, int L, int inType, cudaStream_t s);
 
 // ---- column-tile heights per size class (tune.cpp) ----
 enum TuneKind { kTuneFwdX, kTuneFwdY, kTuneFwdZ, kTuneInvZ, kTuneInvY, kTuneInvX, kTuneKinds };
