@@ -331,11 +331,18 @@ __device__ __forceinline__ void rowreg_t(const PassDesc &d, int tile, float *til
   float *out = static_cast<float *>(d.out);
   const long long outSC = d.outSC;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = warp; q < L; q += kRegThreads / 32)
-    for (int rr = lane; rr < R; rr += 32) {
-      const long long bo = rowOut[rr];
-      if (bo >= 0) out[bo + q * outSC] = tileSm[q * P + rr];
+  for (int rr = lane; rr < R; rr += 32) {
+    const long long bo = rowOut[rr];
+    if (bo < 0) continue;
+    float *dst = out + bo + warp * outSC;
+    const float *t = tileSm + warp * P + rr;
+#pragma unroll 4
+    for (int q = warp; q < L; q += kRegThreads / 32) {
+      *dst = *t;
+      dst += (kRegThreads / 32) * outSC;
+      t += (kRegThreads / 32) * P;
     }
+  }
 }
 
 template <typename InT, int G, int E>
