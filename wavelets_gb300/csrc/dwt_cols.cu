@@ -429,9 +429,20 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
       const InT *src = in + rowIn[me];
       float *col = tile + me;
       if (!INV) {
+        // pointer steps over the real elements, then the REPEAT padding
         const int cl = min(L, d.clampL) - 1;
-        for (int c = cFirst; c < L; c += cStep)
-          stage(col + c * kP, src + (long long)min(c, cl) * inSC);
+        const int cEnd = min(L, cl + 1);
+        const InT *sp = src + (long long)cFirst * inSC;
+        float *tp = col + cFirst * kP;
+        const long long sStep = (long long)cStep * inSC;
+        int c = cFirst;
+#pragma unroll 4
+        for (; c < cEnd; c += cStep) {
+          stage(tp, sp);
+          sp += sStep;
+          tp += cStep * kP;
+        }
+        for (; c < L; c += cStep) stage(col + c * kP, src + (long long)cl * inSC);
       } else {
         // band order -> in-place positions, undoing the deferred scale
         const int nLow = L >> S;
@@ -531,11 +542,16 @@ dwt_cols_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ til
         for (int t = 0; t < S; t++) {
           const int qs = L >> (t + 1);
           const float st = scaleTab[t];
-          OutT *db = dst + (long long)qs * outSC;
-          const float *cb = col + (1 << t) * kP;
-          const int step = (2 << t) * kP;
-          for (int k = cFirst; k < qs; k += cStep)
-            store_from_float(db + k * outSC, cb[k * step] * st);
+          OutT *db = dst + (long long)(qs + cFirst) * outSC;
+          const float *cb = col + (1 << t) * kP + cFirst * ((2 << t) * kP);
+          const long long dStep = (long long)cStep * outSC;
+          const int cStepT = cStep * ((2 << t) * kP);
+#pragma unroll 4
+          for (int k = cFirst; k < qs; k += cStep) {
+            store_from_float(db, *cb * st);
+            db += dStep;
+            cb += cStepT;
+          }
         }
       } else {
         const int Lc = min(L, d.cropL);
