@@ -544,6 +544,30 @@ def main():
     same = all(np.array_equal(a.words, b) for a, b in zip(out, ref_words))
     value = world * in_bytes / (step_ms / 1e3) / 1e9
 
+    # ---- batched decompression of the step's results into device memory ----
+    decomp = None
+    if rank == 0 and split_vol is None:
+        outs_b = [(a.nbytes + 255) // 256 * 256 for a, _ in items]
+        dbuf = lib.DeviceBuffer(sum(outs_b))
+        dptr, acc = [], 0
+        for nb in outs_b:
+            dptr.append(dbuf.ptr + acc)
+            acc += nb
+        for _ in range(2):
+            ctx.decompress_batch(out, device_outs=dptr)
+        nd = max(3, min(10, args.steps))
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(nd):
+            ctx.decompress_batch(out, device_outs=dptr)
+        ctx.sync()
+        dms = (time.perf_counter() - t0) * 1e3 / nd
+        decomp = {"value": in_bytes / (dms / 1e3) / 1e9, "unit": "GB/s",
+                  "ms_per_batch": dms, "bytes_out": in_bytes, "bytes_in": comp_bytes,
+                  "how": "wl_decompress_batch of the step's results (page-locked host "
+                         "memory) into device memory, original types; wall clock"}
+        dbuf.free()
+
     # ---- PSNR on a sample (equal for batched and plain: identical streams) ----
     psnrs = []
     if split_vol is not None:
@@ -759,6 +783,7 @@ def main():
                                   "bytes": "input + compressed output per step"},
             "serving": serving,
             "opt_sweep": opt,
+            "decompress": decomp,
             "autotune": {"ms": tune_ms, "classes": len(tune_rows),
                          "shapes": {f"{r}x{w}": sum(1 for v in tune_rows.values()
                                                     if v[0] == (r, w))

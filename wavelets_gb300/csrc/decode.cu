@@ -37,6 +37,8 @@ struct DecCub {
   int binCount;
   long long n;        // elements
   int *out;           // bins
+  float *fout = nullptr;  // or the dequantized values dq[bin]
+  const float *dq = nullptr;
   long long subBase;  // first subsequence
   long long nSub;
   int lutOff;
@@ -212,6 +214,23 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
   const long long limit = exitPos[2 * i + (lastRound & 1)];
   long long p = start[i], o = offs[i];
   const long long total = c.nWords * 32;
+  if (c.fout) {
+    // dequantized on the way: a token's copies are one value, written a
+    // 16-byte word at a time where the run allows
+    float *F = c.fout;
+    while (p < limit && p < total && o < c.n) {
+      int cnt, val;
+      const int used = decode_token(c, L, p, cnt, val);
+      if (used <= 0) break;
+      p += used;
+      const float fv = c.dq[min(max(val, 0), c.binCount - 1)];
+      const long long e = min(o + cnt, c.n);
+      for (; o < e && (o & 3); o++) F[o] = fv;
+      for (; o + 4 <= e; o += 4) *reinterpret_cast<float4 *>(F + o) = make_float4(fv, fv, fv, fv);
+      for (; o < e; o++) F[o] = fv;
+    }
+    return;
+  }
   while (p < limit && p < total && o < c.n) {
     int cnt, val;
     const int used = decode_token(c, L, p, cnt, val);
@@ -269,7 +288,8 @@ int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags,
                                ? (it.nWords * 32 + kSubBits - 1) / kSubBits : 1;
     c.words = it.words; c.nWords = it.nWords; c.table = it.table; c.nTable = it.nTable;
     c.dupKey = it.dupKey; c.dupValue = it.dupValue; c.binCount = it.binCount; c.n = it.n;
-    c.out = it.out; c.subBase = totalSub; c.nSub = nSub; c.lutOff = i * 4096;
+    c.out = it.out; c.fout = it.fout; c.dq = it.dq;
+    c.subBase = totalSub; c.nSub = nSub; c.lutOff = i * 4096;
     totalSub += nSub;
   }
   char *p = static_cast<char *>(ws);
@@ -338,7 +358,7 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
   long long *elems = reinterpret_cast<long long *>(p); p += nSub * 8;
   long long *total = reinterpret_cast<long long *>(p); p += 8;
   int *flags = reinterpret_cast<int *>(p);
-  DecCub c;
+  DecCub c{};  // bins out (fout stays null)
   c.words = words; c.nWords = nWords; c.table = table; c.nTable = nTable;
   c.dupKey = dupKey; c.dupValue = dupValue; c.binCount = binCount; c.n = n; c.out = out;
   c.subBase = 0; c.nSub = nSub; c.lutOff = 0;
@@ -372,6 +392,18 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
   if (got < n) return 1;  // the reference stops with fewer values than the cubelet holds
   write_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, round);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+__global__ void fill_float_kernel(float *out, long long n, float v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = v;
+}
+
+void fill_float(float *out, long long n, float v, cudaStream_t s) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  fill_float_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, s>>>(out, n, v);
 }
 
 void fill_value(int *out, long long n, int v, cudaStream_t s) {

@@ -1636,6 +1636,12 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
   std::vector<int> ot(n);
   long long coefTotal = 0, wordsTotal = 0, tableTotal = 0, outTotal = 0, totalSub = 0;
   int nStreams = 0;
+  // results whose words follow each other in memory (the results of one
+  // compression call) keep that layout on the device: one copy per run
+  auto follows = [&](int i) {
+    return i > 0 && rs[i].words && rs[i - 1].words &&
+           rs[i].words == rs[i - 1].words + rs[i - 1].n_words;
+  };
   for (int i = 0; i < n; i++) {
     const wl_result *r = rs + i;
     ot[i] = outTypes ? outTypes[i] : r->original_dtype;
@@ -1643,8 +1649,8 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
     TRY(check_result(ctx, r, ot[i], N[i]));
     coefOff[i] = coefTotal;
     coefTotal += (N[i] + 63) & ~63LL;
-    wordsOff[i] = wordsTotal;
-    wordsTotal += ((long long)r->n_words + 3) & ~3LL;
+    wordsOff[i] = follows(i) ? wordsOff[i - 1] + rs[i - 1].n_words : (wordsTotal + 3) & ~3LL;
+    wordsTotal = wordsOff[i] + r->n_words;
     tableOff[i] = tableTotal;
     tableTotal += ((long long)r->n_decode + 3) & ~3LL;
     outOff[i] = outTotal;
@@ -1656,52 +1662,53 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
     }
   }
   const size_t decWsBytes = decode_batch_workspace_bytes(nStreams, totalSub);
-  const size_t dqItemsOff = (decWsBytes + 255) & ~(size_t)255;
   TRY(ensure(ctx, ctx->coef, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->coef2, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->bins, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->decWords, (size_t)wordsTotal * 4 + 16));
   TRY(ensure(ctx, ctx->decTable, (size_t)tableTotal * 4 + 16));
   TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
-  TRY(ensure(ctx, ctx->decWs, dqItemsOff + (size_t)n * sizeof(DqItem)));
+  TRY(ensure(ctx, ctx->decWs, decWsBytes));
   if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, (size_t)outTotal + 16));
-  TRY(ensure_host(ctx, ctx->hWords, (size_t)wordsTotal * 4 + 16));
   TRY(ensure_host(ctx, ctx->hDecode, (size_t)tableTotal * 4 + 16));
-  TRY(ensure_host(ctx, ctx->hVals, (size_t)n * kMaxBins * 4 + (size_t)n * sizeof(DqItem)));
+  TRY(ensure_host(ctx, ctx->hVals, (size_t)n * kMaxBins * 4));
   TRY(ensure_host(ctx, ctx->hFlags, 64 + (size_t)n * 8));
   cudaStream_t s = ctx->stream;
-  // gather the host arrays into page-locked staging: three copies in all
-  uint32_t *hw = H<uint32_t>(ctx->hWords);
+  // decode tables and dequantization tables gathered into page-locked staging
   int *ht = H<int>(ctx->hDecode);
   float *hq = H<float>(ctx->hVals);
-  DqItem *hdq = reinterpret_cast<DqItem *>(hq + (size_t)n * kMaxBins);
-  long long blocks = 0;
   std::vector<DecodeItem> items;
   items.reserve(nStreams);
   for (int i = 0; i < n; i++) {
     const wl_result *r = rs + i;
-    if (r->n_words) memcpy(hw + wordsOff[i], r->words, (size_t)r->n_words * 4);
     memcpy(ht + tableOff[i], r->decode, (size_t)r->n_decode * 4);
     dequant_values(r->quant_alg, r->bin_count, r->threshold_value, r->max_value, r->values,
                    hq + (size_t)i * kMaxBins);
-    int *bins = P<int>(ctx->bins) + coefOff[i];
-    hdq[i] = DqItem{bins, P<float>(ctx->coef) + coefOff[i], N[i],
-                    P<float>(ctx->dqtable) + (size_t)i * kMaxBins, r->bin_count, blocks};
-    blocks += (N[i] + 2047) / 2048;
-    if (!single_symbol(r))
-      items.push_back(DecodeItem{P<uint32_t>(ctx->decWords) + wordsOff[i], r->n_words,
-                                 P<int>(ctx->decTable) + tableOff[i], r->n_decode, r->dup_key,
-                                 r->dup_value, r->bin_count, N[i], bins});
+    if (!single_symbol(r)) {
+      DecodeItem it{P<uint32_t>(ctx->decWords) + wordsOff[i], r->n_words,
+                    P<int>(ctx->decTable) + tableOff[i], r->n_decode, r->dup_key,
+                    r->dup_value, r->bin_count, N[i], P<int>(ctx->bins) + coefOff[i]};
+      it.fout = P<float>(ctx->coef) + coefOff[i];
+      it.dq = P<float>(ctx->dqtable) + (size_t)i * kMaxBins;
+      items.push_back(it);
+    }
   }
-  CU(cudaMemcpyAsync(ctx->decWords.p, hw, (size_t)wordsTotal * 4, cudaMemcpyHostToDevice, s));
+  for (int i = 0; i < n;) {  // the words, run by run
+    int j = i + 1;
+    long long nw = rs[i].n_words;
+    while (j < n && follows(j)) nw += rs[j++].n_words;
+    if (nw)
+      CU(cudaMemcpyAsync(P<uint32_t>(ctx->decWords) + wordsOff[i], rs[i].words, (size_t)nw * 4,
+                         cudaMemcpyHostToDevice, s));
+    i = j;
+  }
   CU(cudaMemcpyAsync(ctx->decTable.p, ht, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(ctx->dqtable.p, hq, (size_t)n * kMaxBins * 4, cudaMemcpyHostToDevice, s));
-  DqItem *ddq = reinterpret_cast<DqItem *>(P<char>(ctx->decWs) + dqItemsOff);
-  CU(cudaMemcpyAsync(ddq, hdq, (size_t)n * sizeof(DqItem), cudaMemcpyHostToDevice, s));
   ctx->launches = 0;
   for (int i = 0; i < n; i++)
-    if (single_symbol(rs + i)) {
-      fill_value(P<int>(ctx->bins) + coefOff[i], N[i], rs[i].decode[1], s);
+    if (single_symbol(rs + i)) {  // every element the one symbol's value
+      const int v = std::min(std::max(rs[i].decode[1], 0), rs[i].bin_count - 1);
+      fill_float(P<float>(ctx->coef) + coefOff[i], N[i], hq[(size_t)i * kMaxBins + v], s);
       ctx->launches++;
     }
   if (!items.empty()) {
@@ -1712,7 +1719,6 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
     if (rc > 0) return fail(ctx, WL_EFORMAT, "corrupt Huffman stream in the batch");
     ctx->launches += 5;
   }
-  launch_dequant_batch(ddq, n, blocks, s);
   CU(cudaGetLastError());
   PassGroups ph[3];
   for (int i = 0; i < n; i++) {

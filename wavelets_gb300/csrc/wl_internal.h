@@ -274,6 +274,9 @@ struct DecodeItem {
   int dupKey, dupValue, binCount;
   long long n;            // elements
   int *out;               // device bins
+  // instead of bins: the dequantized values dq[bin] (binCount entries)
+  float *fout = nullptr;
+  const float *dq = nullptr;
 };
 inline long long decode_subsequences(long long nWords) {
   const long long k = (nWords * 32 + 1023) / 1024;
@@ -297,6 +300,7 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
                   int dupKey, int dupValue, int binCount, long long n, int *out, void *ws,
                   int *hostFlags, cudaStream_t s);
 void fill_value(int *out, long long n, int v, cudaStream_t s);
+void fill_float(float *out, long long n, float v, cudaStream_t s);
 
 // host-side exact log-quantizer tables (quant_host.cpp)
 struct LogTable {

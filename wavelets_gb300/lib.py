@@ -563,9 +563,11 @@ class Context:
         self._check(st)
         return out
 
-    def decompress_batch(self, cs: Sequence[Compressed], dtypes=None) -> List[np.ndarray]:
+    def decompress_batch(self, cs: Sequence[Compressed], dtypes=None, device_outs=None):
         """Restore many cubelets in one batched call (dtypes default to each
-        one's original)."""
+        one's original).  With device_outs (one device address per cubelet,
+        original_size elements of its type each) the cubelets are restored
+        into device memory and nothing is returned; else into new arrays."""
         n = len(cs)
         rs = (WlResult * n)()
         keep = []
@@ -578,13 +580,17 @@ class Context:
                            ctypes.sizeof(WlResult))
             wl_dt = (NP_TO_WL[np.dtype(dtypes[i])] if dtypes is not None and dtypes[i] is not None
                      else c.original_dtype)
-            X, Y, Z = c.original_size
-            o = np.empty((Z, Y, X), WL_TO_NP[wl_dt])
-            outs.append(o)
-            ptrs[i] = o.ctypes.data
+            if device_outs is not None:
+                ptrs[i] = device_outs[i]
+            else:
+                X, Y, Z = c.original_size
+                o = np.empty((Z, Y, X), WL_TO_NP[wl_dt])
+                outs.append(o)
+                ptrs[i] = o.ctypes.data
             dts[i] = wl_dt
-        self._check(self.lib.wl_decompress_batch(self.h, rs, n, dts, ptrs, 0))
-        return outs
+        self._check(self.lib.wl_decompress_batch(self.h, rs, n, dts, ptrs,
+                                                 1 if device_outs is not None else 0))
+        return None if device_outs is not None else outs
 
     def forward_transform(self, arr, params: Optional[P.Params] = None):
         """Coefficients of the forward transform in the stored (rotated) order
