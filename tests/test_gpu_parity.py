@@ -386,6 +386,23 @@ def test_row_register_z_lengths_against_float64_lifting(ctx, z, zsteps, wavelet)
     assert err <= FP64_RTOL
 
 
+@pytest.mark.parametrize("z,zsteps", [(16, 4), (16, 1), (32, 2), (48, 4), (48, 1), (48, 3),
+                                      (64, 6), (96, 5), (96, 2), (128, 3), (192, 6),
+                                      (192, 1), (256, 8), (256, 4)])
+@pytest.mark.parametrize("wavelet", [P.CDF97, P.HAAR])
+def test_row_register_inverse_z_lengths_round_trip(ctx, z, zsteps, wavelet):
+    """The inverse transform (its z rows in registers for these lengths)
+    restores the forward transform's input; 240 rows, the last block ragged."""
+    a = synth.scaled_blob_cubelet(np.random.default_rng(z * 17 + zsteps), (z, 12, 20),
+                                  np.float32)
+    steps = (2, 2, zsteps)
+    p = P.Params(steps=steps, wavelet=wavelet)
+    coeffs, stored = ctx.forward_transform(a, p)
+    back = ctx.inverse_transform(coeffs, stored, steps, wavelet, (20, 12, z))
+    err = float(np.abs(back - a).max()) / float(np.abs(a).max())
+    assert err <= 2e-6
+
+
 @pytest.mark.parametrize("two_d_steps", [(-1, -1, -1), (3, 2, 0), (0, 2, 3), (4, 4, 1)])
 def test_2d_mode_batched_equals_single_and_round_trips(ctx, two_d_steps, tmp_path):
     """-2d on the column-tile kernel (lifting): a batch of mixed sizes equals

@@ -386,6 +386,193 @@ void launch_t_len(const PassDesc *p, const int *tp, int n, int blocks, int L, cu
   }
 }
 
+// One inverse level, M pairs per lane (pair k of group lane `sub` is pair
+// M sub + k), lanes [0, na) active; s: low-pass, d: detail values in, the
+// even (e) and odd (o) elements out, with the mirrored ends of dwt.cu
+// inv_lifting_level / dwt_cols.cu lift_inv_seg (same operands, same order):
+//   s1_j = s2_j - d (d2_j-1 + d2_j)   d2_-1 = d2_0
+//   d1_j = d2_j - g (s1_j + s1_j+1)   s1_h  = s1_h-1
+//   e_j  = s1_j - b (d1_j-1 + d1_j)   d1_-1 = d1_0
+//   o_j  = d1_j - a (e_j + e_j+1)     e_h   = e_h-1
+template <int M, int G, bool HAAR>
+__device__ __forceinline__ void inv_level(const float (&s2)[M], const float (&d2)[M], int sub,
+                                          int na, float (&e)[M], float (&o)[M]) {
+  if (HAAR) {  // dwt_cpu.cc:193-196
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      e[k] = __fmul_rn(kInvSqrt2, __fadd_rn(s2[k], d2[k]));
+      o[k] = __fmul_rn(kInvSqrt2, __fsub_rn(s2[k], d2[k]));
+    }
+    return;
+  }
+  const bool first = sub == 0, last = sub == na - 1;
+  float s1[M], d1[M];
+  float d2P = __shfl_up_sync(kAll, d2[M - 1], 1, G);
+  if (first) d2P = d2[0];
+#pragma unroll
+  for (int k = 0; k < M; k++) s1[k] = fmaf(-kDelta, (k ? d2[k - 1] : d2P) + d2[k], s2[k]);
+  float s1N = __shfl_down_sync(kAll, s1[0], 1, G);
+  if (last) s1N = s1[M - 1];
+#pragma unroll
+  for (int k = 0; k < M; k++) d1[k] = fmaf(-kGamma, s1[k] + (k + 1 < M ? s1[k + 1] : s1N), d2[k]);
+  float d1P = __shfl_up_sync(kAll, d1[M - 1], 1, G);
+  if (first) d1P = d1[0];
+#pragma unroll
+  for (int k = 0; k < M; k++) e[k] = fmaf(-kBeta, (k ? d1[k - 1] : d1P) + d1[k], s1[k]);
+  float eN = __shfl_down_sync(kAll, e[0], 1, G);
+  if (last) eN = e[M - 1];
+#pragma unroll
+  for (int k = 0; k < M; k++) o[k] = fmaf(-kAlpha, e[k] + (k + 1 < M ? e[k + 1] : eN), d1[k]);
+}
+
+// The inverse of rowreg_fwd, in place on rows of L = E G floats stored in
+// band order: every band value the row's lanes need is read first (with the
+// deferred scale undone by division), the levels run from the deepest up
+// in registers, and the lanes store their E elements of the restored row.
+template <int G, int E, bool HAAR>
+__device__ __forceinline__ void rowreg_inv(const PassDesc &d, int row0, float *scaleTab) {
+  constexpr int L = E * G;
+  constexpr int M = E / 2;
+  constexpr int NA1 = M == 4 ? G : 3 * G / 4;  // lanes of levels 1 and 2
+  const int S = d.steps;
+  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
+  __syncthreads();
+  const int row = row0 + (int)threadIdx.x / G;
+  const int sub = threadIdx.x & (G - 1);
+  const bool ok = row < d.rows;
+  long long bi = 0, bo = 0;
+  if (ok) {
+    const int a = row / d.B, b = row - a * d.B;
+    bi = (long long)a * d.inSA + (long long)b * d.inSB;
+    bo = (long long)a * d.outSA + (long long)b * d.outSB;
+  }
+  const float *src = static_cast<const float *>(d.in) + bi;
+  auto rd = [&](int q, int t) { return ok ? src[q] / scaleTab[t] : 0.f; };
+  const bool act1 = sub < NA1;
+  // ---- every input value, read before anything is stored
+  float d0[M], d1v[2] = {0.f, 0.f}, d2v = 0.f, lowv[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < M; k++) d0[k] = rd(L / 2 + M * sub + k, 0);
+  if (S == 1) {
+#pragma unroll
+    for (int k = 0; k < M; k++) lowv[k] = rd(M * sub + k, 1);
+  } else {
+    if (act1) { d1v[0] = rd(L / 4 + 2 * sub, 1); d1v[1] = rd(L / 4 + 2 * sub + 1, 1); }
+    if (S == 2) {
+      if (act1) { lowv[0] = rd(2 * sub, 2); lowv[1] = rd(2 * sub + 1, 2); }
+    } else {
+      if (act1) d2v = rd(L / 8 + sub, 2);
+      if (S == 3 && act1) lowv[0] = rd(sub, 3);
+    }
+  }
+  // deeper levels (S >= 4): lane j of the first L >> (t+1) holds pair j of level t
+  float dg[8];
+#pragma unroll
+  for (int t = 3; t < 11; t++) dg[t - 3] = 0.f;
+  float sg = 0.f;
+  if (S >= 4) {
+#pragma unroll
+    for (int t = 3; t < 11; t++)
+      if (t < S && sub < (L >> (t + 1))) dg[t - 3] = rd((L >> (t + 1)) + sub, t);
+    if (sub < (L >> S)) sg = rd(sub, S);
+  }
+  __syncwarp();  // the row is read by all its lanes before any of them stores
+
+  // ---- levels S-1 .. 3, gathered: pair j in lane j
+  float s2in = lowv[0];  // level 2's low-pass value of this lane
+  if (S >= 4) {
+    float s = sg;
+    int na = L >> S;  // pairs of level S-1
+#pragma unroll 1
+    for (int t = S - 1; t >= 3; t--) {
+      float sv[1] = {s}, dv[1] = {0.f}, ev[1], ov[1];
+#pragma unroll
+      for (int u = 3; u < 11; u++)
+        if (u == t) dv[0] = dg[u - 3];
+      inv_level<1, G, HAAR>(sv, dv, sub, na, ev, ov);
+      // level t-1's pair j is s^{t-1}[j]: element j of level t's output
+      const float a = __shfl_sync(kAll, ev[0], (sub >> 1) & (G - 1), G);
+      const float b = __shfl_sync(kAll, ov[0], (sub >> 1) & (G - 1), G);
+      s = (sub & 1) ? b : a;
+      na <<= 1;
+    }
+    s2in = s;
+  }
+  float e1in[2], o1in[2];  // level 1's two pairs per lane: low-pass in e1in
+  if (S >= 3) {
+    float sv[1] = {s2in}, dv[1] = {d2v}, ev[1], ov[1];
+    inv_level<1, G, HAAR>(sv, dv, sub, NA1, ev, ov);
+    e1in[0] = ev[0];
+    e1in[1] = ov[0];
+  } else {
+    e1in[0] = lowv[0];
+    e1in[1] = lowv[1];
+  }
+  float s0[M];  // level 0's low-pass values of this lane's pairs
+  if (S >= 2) {
+    o1in[0] = d1v[0];
+    o1in[1] = d1v[1];
+    float e1[2], o1[2];
+    inv_level<2, G, HAAR>(e1in, o1in, sub, NA1, e1, o1);
+    // lane j of the first NA1 now holds s^0[4j .. 4j+3]
+    const float q4[4] = {e1[0], o1[0], e1[1], o1[1]};
+    if (M == 4) {
+#pragma unroll
+      for (int k = 0; k < M; k++) s0[k] = q4[k % 4];
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const int v = min(M * sub + k, L / 2 - 1);
+        const int from = v >> 2, reg = v & 3;
+        const float a = __shfl_sync(kAll, q4[0], from, G);
+        const float b = __shfl_sync(kAll, q4[1], from, G);
+        const float c = __shfl_sync(kAll, q4[2], from, G);
+        const float dd = __shfl_sync(kAll, q4[3], from, G);
+        s0[k] = reg == 0 ? a : reg == 1 ? b : reg == 2 ? c : dd;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; k++) s0[k] = lowv[k % 4];
+  }
+  float e0[M], o0[M];
+  inv_level<M, G, HAAR>(s0, d0, sub, G, e0, o0);
+  if (ok) {
+    float *dst = static_cast<float *>(d.out) + bo;
+    if (M == 4) {
+      float4 *d4 = reinterpret_cast<float4 *>(dst) + 2 * sub;
+      d4[0] = make_float4(e0[0], o0[0], e0[1 % M], o0[1 % M]);
+      d4[1] = make_float4(e0[2 % M], o0[2 % M], e0[3 % M], o0[3 % M]);
+    } else {
+      float2 *d2p = reinterpret_cast<float2 *>(dst) + M * sub;
+#pragma unroll
+      for (int k = 0; k < M; k++) d2p[k] = make_float2(e0[k], o0[k]);
+    }
+  }
+}
+
+template <int G, int E>
+__global__ void __launch_bounds__(kRegThreads)
+dwt_rowreg_inv_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
+                      int nPasses) {
+  __shared__ float scaleTab[16];
+  const int bid = blockIdx.x;
+  int lo = 0, hi = nPasses - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
+  }
+  const PassDesc &d = passes[lo];
+  const int row0 = (bid - tilePrefix[lo]) * (kRegThreads / G);
+  if (d.wavelet == WL_HAAR) rowreg_inv<G, E, true>(d, row0, scaleTab);
+  else rowreg_inv<G, E, false>(d, row0, scaleTab);
+}
+
+template <int G, int E = 8>
+void launch_ig(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
+  dwt_rowreg_inv_kernel<G, E><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
+}
+
 // One block: kRegThreads / G rows of the pass found by the tile prefix.
 template <int G, int E>
 __global__ void __launch_bounds__(kRegThreads)
@@ -442,6 +629,20 @@ void launch_dwt_rowreg_t(const PassDesc *p, const int *tp, int n, int blocks, in
     case WL_U16: launch_t_len<uint16_t>(p, tp, n, blocks, L, s); break;
     case WL_I32: launch_t_len<int32_t>(p, tp, n, blocks, L, s); break;
     default: launch_t_len<float>(p, tp, n, blocks, L, s); break;
+  }
+}
+
+void launch_dwt_rowreg_inv(const PassDesc *p, const int *tp, int n, int blocks, int L,
+                           cudaStream_t s) {
+  switch (L) {
+    case 16: launch_ig<2>(p, tp, n, blocks, s); break;
+    case 32: launch_ig<4>(p, tp, n, blocks, s); break;
+    case 48: launch_ig<8, 6>(p, tp, n, blocks, s); break;
+    case 64: launch_ig<8>(p, tp, n, blocks, s); break;
+    case 96: launch_ig<16, 6>(p, tp, n, blocks, s); break;
+    case 128: launch_ig<16>(p, tp, n, blocks, s); break;
+    case 192: launch_ig<32, 6>(p, tp, n, blocks, s); break;
+    default: launch_ig<32>(p, tp, n, blocks, s); break;
   }
 }
 

@@ -88,6 +88,8 @@ int group_key(bool cols, int dtype, int L, bool vec = false) {
 // passes stored through a tile)
 int rowreg_key(int L) { return (1 << 20) | L; }
 int rowreg_t_key(int dtype, int L) { return (1 << 21) | (dtype << 16) | L; }
+int rowreg_inv_key(int L) { return (1 << 23) | L; }
+enum RegKind { kRegNone, kRegInPlace, kRegTile, kRegInvInPlace };
 
 // ---- result storage ------------------------------------------------------------
 // The arrays of all results of one compression call live in one page-locked
@@ -600,7 +602,7 @@ struct GroupLaunch {
   int n, tiles, smem, rows, warps, inType, outType;
   bool inverse, cols, vec;
   int regL;  // row-register pass of rows of regL elements (0: another kernel)
-  bool regT;  // ... stored through a tile (the forward x and y passes)
+  int regKind;  // which row-register kernel (RegKind)
   // bytes a launch moves, for ordering concurrent groups
   double weight() const { return (double)tiles * (regL ? 4.0 * regL * rows : (double)smem); }
 };
@@ -612,7 +614,7 @@ struct GroupLaunch {
 wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int kind, int inType,
                       int outType, bool inverse, bool cols, bool vec,
                       std::vector<GroupLaunch> &out, const TileShape *force = nullptr,
-                      int regL = 0, bool regT = false) {
+                      int regL = 0, int regKind = kRegNone) {
   if (g.empty()) return WL_OK;
   const size_t n = g.size();
   const size_t bytes = n * sizeof(PassDesc) + (n + 1) * sizeof(int);
@@ -620,7 +622,8 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
     return fail(ctx, WL_ENOMEM, "pass staging too small");
   int rows = 0, warps = 4;
   if (regL) {
-    rows = regT ? dwt_rowreg_t_rows_per_block(regL) : dwt_rowreg_rows_per_block(regL);
+    rows = regKind == kRegTile ? dwt_rowreg_t_rows_per_block(regL)
+                               : dwt_rowreg_rows_per_block(regL);
     for (PassDesc &d : g) {
       d.T = rows;
       d.tiles = (d.rows + rows - 1) / rows;
@@ -651,7 +654,7 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
   }
   tp[n] = tiles;
   out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec,
-                 regL, regT});
+                 regL, regKind});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
@@ -662,10 +665,11 @@ wl_status stage_groups(wl_ctx *ctx, const PassGroups &gs, size_t &hoff, int kind
   for (const auto &kv : gs) {
     const bool regT = (kv.first >> 21) & 1;
     const int regL = regT || ((kv.first >> 20) & 1) ? kv.second[0].L : 0;
+    const int regKind = regT ? kRegTile : regL ? kRegInPlace : kRegNone;
     const bool cols = !regL && ((kv.first >> 12) & 1), vec = !regL && ((kv.first >> 13) & 1);
     const int dt = regT ? (kv.first >> 16) & 15 : regL ? WL_F32 : (kv.first >> 8) & 15;
     TRY(stage_group(ctx, kv.second, hoff, kind, inverse ? WL_F32 : dt, outType, inverse, cols, vec,
-                    out, nullptr, regL, regT));
+                    out, nullptr, regL, regKind));
   }
   return WL_OK;
 }
@@ -674,8 +678,10 @@ wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
   const char *base = P<char>(ctx->passes);
   const PassDesc *dp = reinterpret_cast<const PassDesc *>(base + l.off);
   const int *dtp = reinterpret_cast<const int *>(base + l.off + l.n * sizeof(PassDesc));
-  if (l.regL && l.regT)
+  if (l.regKind == kRegTile)
     launch_dwt_rowreg_t(dp, dtp, l.n, l.tiles, l.regL, l.inType, s);
+  else if (l.regKind == kRegInvInPlace)
+    launch_dwt_rowreg_inv(dp, dtp, l.n, l.tiles, l.regL, s);
   else if (l.regL)
     launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, s);
   else if (l.cols)
@@ -1270,7 +1276,13 @@ void inverse_passes(const int size[3], const int steps[3], int wavelet, const in
   } else if (use_cols(Xp, Yp, Zp, identity, wp)) {
     PassDesc d[3];
     const int np = inverse_passes_cols(Xp, Yp, Zp, original_size, steps, wavelet, c1, c2, dst, d);
-    for (int i = 0; i < np; i++) put(3 - np + i, true, d[i]);
+    for (int i = 0; i < np; i++) {
+      const int phase = 3 - np + i;
+      if (phase == 0 && dwt_rowreg_fits(d[i].L, d[i].steps))  // z rows in registers
+        ph[0][rowreg_inv_key(d[i].L)].push_back(d[i]);
+      else
+        put(phase, true, d[i]);
+    }
   } else {
     if (!identity) {
       // inverse z pass: z-x-y -> y-z-x
@@ -1316,6 +1328,11 @@ wl_status run_inverse_phases(wl_ctx *ctx, PassGroups ph[3]) {
   const int kinds[3] = {kTuneInvZ, kTuneInvY, kTuneInvX};
   for (int k = 0; k < 3; k++) {
     for (const auto &kv : ph[k]) {
+      if ((kv.first >> 23) & 1) {
+        TRY(stage_group(ctx, kv.second, hoff, kinds[k], WL_F32, WL_F32, true, false, false, gl,
+                        nullptr, kv.second[0].L, kRegInvInPlace));
+        continue;
+      }
       const bool cols = (kv.first >> 12) & 1;
       const int outT = (kv.first >> 8) & 15;
       TRY(stage_group(ctx, kv.second, hoff, kinds[k], WL_F32, outT, true, cols, false, gl));

@@ -225,6 +225,9 @@ void launch_dwt_rowreg(const PassDesc *d_passes, const int *d_tilePrefix, int nP
 // the same with the rows read from any element type (REPEAT clamp) and
 // stored through a shared-memory tile to an output where consecutive rows
 // are neighbours (forward x and y passes)
+// the inverse of the in-place pass (the first inverse pass, z)
+void launch_dwt_rowreg_inv(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
+                           int blocks, int L, cudaStream_t s);
 int dwt_rowreg_t_rows_per_block(int L);
 void launch_dwt_rowreg_t(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
                          int blocks, int L, int inType, cudaStream_t s);
