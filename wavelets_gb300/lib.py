@@ -563,11 +563,9 @@ class Context:
         self._check(st)
         return out
 
-    def decompress_batch(self, cs: Sequence[Compressed], dtypes=None, device_outs=None):
-        """Restore many cubelets in one batched call (dtypes default to each
-        one's original).  With device_outs (one device address per cubelet,
-        original_size elements of its type each) the cubelets are restored
-        into device memory and nothing is returned; else into new arrays."""
+    def prepare_decompress(self, cs: Sequence[Compressed], dtypes=None, device_outs=None):
+        """The wl_decompress_batch arguments for these results (reusable:
+        run_decompress(prep) restores them again without rebuilding them)."""
         n = len(cs)
         rs = (WlResult * n)()
         keep = []
@@ -588,9 +586,21 @@ class Context:
                 outs.append(o)
                 ptrs[i] = o.ctypes.data
             dts[i] = wl_dt
-        self._check(self.lib.wl_decompress_batch(self.h, rs, n, dts, ptrs,
-                                                 1 if device_outs is not None else 0))
-        return None if device_outs is not None else outs
+        return {"n": n, "rs": rs, "dts": dts, "ptrs": ptrs, "outs": outs, "keep": keep,
+                "on_device": device_outs is not None}
+
+    def run_decompress(self, prep):
+        """One wl_decompress_batch call with prepared arguments."""
+        self._check(self.lib.wl_decompress_batch(self.h, prep["rs"], prep["n"], prep["dts"],
+                                                 prep["ptrs"], 1 if prep["on_device"] else 0))
+        return None if prep["on_device"] else prep["outs"]
+
+    def decompress_batch(self, cs: Sequence[Compressed], dtypes=None, device_outs=None):
+        """Restore many cubelets in one batched call (dtypes default to each
+        one's original).  With device_outs (one device address per cubelet,
+        original_size elements of its type each) the cubelets are restored
+        into device memory and nothing is returned; else into new arrays."""
+        return self.run_decompress(self.prepare_decompress(cs, dtypes, device_outs))
 
     def forward_transform(self, arr, params: Optional[P.Params] = None):
         """Coefficients of the forward transform in the stored (rotated) order
