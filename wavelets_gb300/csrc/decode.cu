@@ -53,17 +53,6 @@ __device__ __forceinline__ int find_cub(const DecCub *c, int n, long long sub) {
   return lo;
 }
 
-// 64 bits of the stream starting at bit p (zero past the end)
-__device__ __forceinline__ unsigned long long peek64(const uint32_t *w, long long nw, long long p) {
-  const long long i = p >> 5;
-  const int o = (int)(p & 31);
-  unsigned long long a = i < nw ? w[i] : 0u;
-  unsigned long long b = i + 1 < nw ? w[i + 1] : 0u;
-  unsigned long long c = i + 2 < nw ? w[i + 2] : 0u;
-  const unsigned long long lo = a | (b << 32);
-  return o ? ((lo >> o) | (c << (64 - o))) : lo;
-}
-
 // LUT entry: bit 31 leaf; leaf: bits 16-23 code length, bits 0-15 symbol;
 // not a leaf: bits 0-30 node offset in the decode table after kLutBits bits
 __global__ void build_lut_kernel(const DecCub *cubs, unsigned *lut) {
@@ -94,9 +83,40 @@ __global__ void build_lut_kernel(const DecCub *cubs, unsigned *lut) {
 
 // Decode one token at bit p.  Returns bits consumed (0 = malformed), sets the
 // element count and the value.
-__device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, long long p,
-                                            int &count, int &value) {
-  unsigned long long bits = peek64(c.words, c.nWords, p);
+// Three stream words from word i on (zero past the end), moved on a word at a
+// time as the bit position advances (it never goes back): a token loads a
+// word only when it crosses into the next one.
+struct Window {
+  const uint32_t *w;
+  long long nw, i;
+  unsigned a, b, c;
+  __device__ unsigned ld(long long k) const { return k < nw ? w[k] : 0u; }
+  __device__ void init(const uint32_t *words, long long n, long long p) {
+    w = words;
+    nw = n;
+    i = p >> 5;
+    a = ld(i);
+    b = ld(i + 1);
+    c = ld(i + 2);
+  }
+  // 64 bits of the stream from bit p (p >= 32 i), as peek64
+  __device__ unsigned long long peek(long long p) {
+    const long long k = p >> 5;
+    while (i < k) {
+      a = b;
+      b = c;
+      c = ld(i + 3);
+      i++;
+    }
+    const int o = (int)(p & 31);
+    const unsigned long long lo = a | ((unsigned long long)b << 32);
+    return o ? ((lo >> o) | ((unsigned long long)c << (64 - o))) : lo;
+  }
+};
+
+__device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, Window &win,
+                                            long long p, int &count, int &value) {
+  unsigned long long bits = win.peek(p);
   const unsigned e = L[bits & ((1u << kLutBits) - 1)];
   int len, sym;
   if (e & 0x80000000u) {
@@ -118,7 +138,7 @@ __device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, 
     sym = c.table[node + 1];
   }
   if (sym == c.dupKey && c.dupKey >= 0) {
-    const unsigned v = (unsigned)((peek64(c.words, c.nWords, p + len)) & 7u);
+    const unsigned v = (unsigned)(win.peek(p + len) & 7u);
     count = 1 << (v + 3);
     value = c.dupValue;
     return len + 3;
@@ -134,9 +154,11 @@ __device__ long long decode_span(const DecCub &c, const unsigned *L, long long s
                                  long long &elems, bool &bad) {
   long long p = start, e = 0;
   const long long total = c.nWords * 32;
+  Window win;
+  win.init(c.words, c.nWords, p);
   while (p < limit && p < total) {
     int cnt, val;
-    const int used = decode_token(c, L, p, cnt, val);
+    const int used = decode_token(c, L, win, p, cnt, val);
     if (used <= 0) { bad = true; break; }
     p += used;
     e += cnt;
@@ -214,13 +236,15 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
   const long long limit = exitPos[2 * i + (lastRound & 1)];
   long long p = start[i], o = offs[i];
   const long long total = c.nWords * 32;
+  Window win;
+  win.init(c.words, c.nWords, p);
   if (c.fout) {
     // dequantized on the way: a token's copies are one value, written a
     // 16-byte word at a time where the run allows
     float *F = c.fout;
     while (p < limit && p < total && o < c.n) {
       int cnt, val;
-      const int used = decode_token(c, L, p, cnt, val);
+      const int used = decode_token(c, L, win, p, cnt, val);
       if (used <= 0) break;
       p += used;
       const float fv = c.dq[min(max(val, 0), c.binCount - 1)];
@@ -233,7 +257,7 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
   }
   while (p < limit && p < total && o < c.n) {
     int cnt, val;
-    const int used = decode_token(c, L, p, cnt, val);
+    const int used = decode_token(c, L, win, p, cnt, val);
     if (used <= 0) break;
     p += used;
     for (int k = 0; k < cnt && o < c.n; k++) c.out[o++] = val;
