@@ -239,18 +239,22 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
   Window win;
   win.init(c.words, c.nWords, p);
   if (c.fout) {
-    // dequantized on the way: a token's copies are one value, written a
-    // 16-byte word at a time where the run allows
+    // dequantized on the way.  With zero runs the output already holds the
+    // zero bin's value everywhere (launch_fill_batch), so only the other
+    // values are written; runs and single zero-bin tokens just move on.
     float *F = c.fout;
+    const bool prefilled = c.dupValue >= 0;
     while (p < limit && p < total && o < c.n) {
       int cnt, val;
       const int used = decode_token(c, L, win, p, cnt, val);
       if (used <= 0) break;
       p += used;
+      if (prefilled && val == c.dupValue) {
+        o = min(o + cnt, c.n);
+        continue;
+      }
       const float fv = c.dq[min(max(val, 0), c.binCount - 1)];
       const long long e = min(o + cnt, c.n);
-      for (; o < e && (o & 3); o++) F[o] = fv;
-      for (; o + 4 <= e; o += 4) *reinterpret_cast<float4 *>(F + o) = make_float4(fv, fv, fv, fv);
       for (; o < e; o++) F[o] = fv;
     }
     return;
@@ -416,6 +420,29 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
   if (got < n) return 1;  // the reference stops with fewer values than the cubelet holds
   write_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, round);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+__global__ void __launch_bounds__(256) fill_batch_kernel(const FillItem *__restrict__ items,
+                                                         int nItems) {
+  int lo = 0, hi = nItems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (items[mid].blockBase <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const FillItem it = items[lo];
+  const long long b0 = ((long long)blockIdx.x - it.blockBase) * kFillBlock;
+  const long long e = min(b0 + kFillBlock, it.n);
+  const float4 v4 = make_float4(it.v, it.v, it.v, it.v);
+  // b0 is a multiple of kFillBlock, so whole float4 words up to the end
+  for (long long i = b0 + 4 * threadIdx.x; i + 4 <= e; i += 4 * 256)
+    *reinterpret_cast<float4 *>(it.out + i) = v4;
+  const long long tail = b0 + ((e - b0) & ~3LL);
+  if (threadIdx.x < e - tail) it.out[tail + threadIdx.x] = it.v;
+}
+
+void launch_fill_batch(const FillItem *items, int nItems, long long totalBlocks, cudaStream_t s) {
+  if (nItems > 0 && totalBlocks > 0)
+    fill_batch_kernel<<<(unsigned)totalBlocks, 256, 0, s>>>(items, nItems);
 }
 
 __global__ void fill_float_kernel(float *out, long long n, float v) {

@@ -1679,21 +1679,28 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
     }
   }
   const size_t decWsBytes = decode_batch_workspace_bytes(nStreams, totalSub);
+  const size_t fillOff = (decWsBytes + 255) & ~(size_t)255;
   TRY(ensure(ctx, ctx->coef, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->coef2, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->bins, (size_t)coefTotal * 4 + 256));
   TRY(ensure(ctx, ctx->decWords, (size_t)wordsTotal * 4 + 16));
   TRY(ensure(ctx, ctx->decTable, (size_t)tableTotal * 4 + 16));
   TRY(ensure(ctx, ctx->dqtable, (size_t)n * kMaxBins * 4));
-  TRY(ensure(ctx, ctx->decWs, decWsBytes));
+  TRY(ensure(ctx, ctx->decWs, fillOff + (size_t)n * sizeof(FillItem)));
   if (!outOnDevice) TRY(ensure(ctx, ctx->outbuf, (size_t)outTotal + 16));
   TRY(ensure_host(ctx, ctx->hDecode, (size_t)tableTotal * 4 + 16));
-  TRY(ensure_host(ctx, ctx->hVals, (size_t)n * kMaxBins * 4));
+  TRY(ensure_host(ctx, ctx->hVals, (size_t)n * kMaxBins * 4 + (size_t)n * sizeof(FillItem)));
   TRY(ensure_host(ctx, ctx->hFlags, 64 + (size_t)n * 8));
   cudaStream_t s = ctx->stream;
   // decode tables and dequantization tables gathered into page-locked staging
   int *ht = H<int>(ctx->hDecode);
   float *hq = H<float>(ctx->hVals);
+  // ranges set to one value before decoding: a single-symbol cubelet whole,
+  // and the cubelets with zero runs to the zero bin's value (the decoder
+  // then writes only the other values)
+  FillItem *hfill = reinterpret_cast<FillItem *>(hq + (size_t)n * kMaxBins);
+  int nFill = 0;
+  long long fillBlocks = 0;
   std::vector<DecodeItem> items;
   items.reserve(nStreams);
   for (int i = 0; i < n; i++) {
@@ -1701,7 +1708,14 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
     memcpy(ht + tableOff[i], r->decode, (size_t)r->n_decode * 4);
     dequant_values(r->quant_alg, r->bin_count, r->threshold_value, r->max_value, r->values,
                    hq + (size_t)i * kMaxBins);
-    if (!single_symbol(r)) {
+    const bool single = single_symbol(r);
+    if (single || r->dup_value >= 0) {
+      const int v = std::min(std::max(single ? r->decode[1] : r->dup_value, 0), r->bin_count - 1);
+      hfill[nFill++] = FillItem{P<float>(ctx->coef) + coefOff[i], N[i],
+                                hq[(size_t)i * kMaxBins + v], fillBlocks};
+      fillBlocks += (N[i] + kFillBlock - 1) / kFillBlock;
+    }
+    if (!single) {
       DecodeItem it{P<uint32_t>(ctx->decWords) + wordsOff[i], r->n_words,
                     P<int>(ctx->decTable) + tableOff[i], r->n_decode, r->dup_key,
                     r->dup_value, r->bin_count, N[i], P<int>(ctx->bins) + coefOff[i]};
@@ -1722,12 +1736,12 @@ wl_status decompress_batch_impl(wl_ctx *ctx, const wl_result *rs, int n, const i
   CU(cudaMemcpyAsync(ctx->decTable.p, ht, (size_t)tableTotal * 4, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(ctx->dqtable.p, hq, (size_t)n * kMaxBins * 4, cudaMemcpyHostToDevice, s));
   ctx->launches = 0;
-  for (int i = 0; i < n; i++)
-    if (single_symbol(rs + i)) {  // every element the one symbol's value
-      const int v = std::min(std::max(rs[i].decode[1], 0), rs[i].bin_count - 1);
-      fill_float(P<float>(ctx->coef) + coefOff[i], N[i], hq[(size_t)i * kMaxBins + v], s);
-      ctx->launches++;
-    }
+  if (nFill) {
+    FillItem *dfill = reinterpret_cast<FillItem *>(P<char>(ctx->decWs) + fillOff);
+    CU(cudaMemcpyAsync(dfill, hfill, (size_t)nFill * sizeof(FillItem), cudaMemcpyHostToDevice, s));
+    launch_fill_batch(dfill, nFill, fillBlocks, s);
+    ctx->launches++;
+  }
   if (!items.empty()) {
     int *hf = H<int>(ctx->hFlags);
     long long *totals = reinterpret_cast<long long *>(hf + 16);

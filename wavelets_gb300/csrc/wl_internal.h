@@ -297,6 +297,16 @@ struct DqItem {
   long long blockBase;
 };
 void launch_dequant_batch(const DqItem *items, int nItems, long long totalBlocks, cudaStream_t s);
+// n floats at out set to v, for many ranges in one launch (blocks of
+// kFillBlock elements; blockBase = the range's first block)
+constexpr int kFillBlock = 4096;
+struct FillItem {
+  float *out;  // 16-byte aligned
+  long long n;
+  float v;
+  long long blockBase;
+};
+void launch_fill_batch(const FillItem *items, int nItems, long long totalBlocks, cudaStream_t s);
 int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags, long long *hostTotals,
                    cudaStream_t s);
 int decode_stream(const uint32_t *words, long long nWords, const int *table, int nTable,
