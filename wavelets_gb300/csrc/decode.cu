@@ -445,18 +445,6 @@ void launch_fill_batch(const FillItem *items, int nItems, long long totalBlocks,
     fill_batch_kernel<<<(unsigned)totalBlocks, 256, 0, s>>>(items, nItems);
 }
 
-__global__ void fill_float_kernel(float *out, long long n, float v) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    out[i] = v;
-}
-
-void fill_float(float *out, long long n, float v, cudaStream_t s) {
-  long long blocks = (n + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  fill_float_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, s>>>(out, n, v);
-}
-
 void fill_value(int *out, long long n, int v, cudaStream_t s) {
   long long blocks = (n + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;

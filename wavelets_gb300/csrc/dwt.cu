@@ -381,25 +381,7 @@ __global__ void dequant_kernel(const int *__restrict__ bins, const float *__rest
 namespace {
 // dequantize many cubelets in one launch: blocks of 2048 elements, a block's
 // cubelet found by binary search over the items' first blocks
-__global__ void __launch_bounds__(256) dequant_batch_kernel(const DqItem *__restrict__ items,
-                                                            int nItems) {
-  int lo = 0, hi = nItems - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (items[mid].blockBase <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
-  }
-  const DqItem it = items[lo];
-  const long long b0 = ((long long)blockIdx.x - it.blockBase) * 2048;
-  const long long e = min(b0 + 2048, it.n);
-  for (long long i = b0 + threadIdx.x; i < e; i += 256)
-    it.out[i] = it.table[min(max(it.bins[i], 0), it.nTable - 1)];
-}
 }  // namespace
-
-void launch_dequant_batch(const DqItem *items, int nItems, long long totalBlocks, cudaStream_t s) {
-  if (nItems > 0 && totalBlocks > 0)
-    dequant_batch_kernel<<<(unsigned)totalBlocks, 256, 0, s>>>(items, nItems);
-}
 
 void launch_dequant(const int *bins, const float *table, float *out, long long n, int nTable,
                     cudaStream_t s) {

@@ -211,7 +211,7 @@ struct wl_ctx {
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr;
-  HostBuf hState, hWords, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
+  HostBuf hState, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   HostBuf hStage[2];  // staging buffers of the container pipeline
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
   // and replay it from then on
@@ -1923,7 +1923,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->meta};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
   for (GraphEntry &g : ctx->graphs) drop_graph(g);
-  HostBuf *hbs[] = {&ctx->hStage[0], &ctx->hStage[1], &ctx->hState, &ctx->hWords, &ctx->hDecode, &ctx->hPasses,
+  HostBuf *hbs[] = {&ctx->hStage[0], &ctx->hStage[1], &ctx->hState, &ctx->hDecode, &ctx->hPasses,
                     &ctx->hTab, &ctx->hLogHdr, &ctx->hPrefix, &ctx->hIn, &ctx->hVals,
                     &ctx->hFlags};
   for (HostBuf *h : hbs) if (h->p) cudaFreeHost(h->p);

@@ -286,17 +286,6 @@ inline long long decode_subsequences(long long nWords) {
   return k > 0 ? k : 1;
 }
 size_t decode_batch_workspace_bytes(int n, long long totalSub);
-// dequantize many cubelets in one launch (dwt.cu); blockBase counts blocks
-// of 2048 elements
-struct DqItem {
-  const int *bins;
-  float *out;
-  long long n;
-  const float *table;
-  int nTable;
-  long long blockBase;
-};
-void launch_dequant_batch(const DqItem *items, int nItems, long long totalBlocks, cudaStream_t s);
 // n floats at out set to v, for many ranges in one launch (blocks of
 // kFillBlock elements; blockBase = the range's first block)
 constexpr int kFillBlock = 4096;
@@ -313,7 +302,6 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
                   int dupKey, int dupValue, int binCount, long long n, int *out, void *ws,
                   int *hostFlags, cudaStream_t s);
 void fill_value(int *out, long long n, int v, cudaStream_t s);
-void fill_float(float *out, long long n, float v, cudaStream_t s);
 
 // host-side exact log-quantizer tables (quant_host.cpp)
 struct LogTable {
