@@ -876,8 +876,21 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       if (pl.pitchY == pl.X && pl.pitchZ == (long long)pl.X * pl.Y) {
         CU(cudaMemcpyAsync(dst, pl.data, (size_t)pl.X * pl.Y * pl.Z * es,
                            cudaMemcpyHostToDevice, s));
+      } else if (pl.pitchZ % pl.pitchY == 0) {
+        // a sub-volume of a larger array (slices a whole number of rows
+        // apart): gathered dense by one three-dimensional copy
+        cudaMemcpy3DParms cp;
+        memset(&cp, 0, sizeof cp);
+        cp.srcPtr = make_cudaPitchedPtr(const_cast<void *>(pl.data), (size_t)pl.pitchY * es,
+                                        (size_t)pl.X * es, (size_t)(pl.pitchZ / pl.pitchY));
+        cp.dstPtr = make_cudaPitchedPtr(dst, (size_t)pl.X * es, (size_t)pl.X * es, (size_t)pl.Y);
+        cp.extent = make_cudaExtent((size_t)pl.X * es, (size_t)pl.Y, (size_t)pl.Z);
+        cp.kind = cudaMemcpyHostToDevice;
+        CU(cudaMemcpy3DAsync(&cp, s));
+        pl.pitchY = pl.X;
+        pl.pitchZ = (long long)pl.X * pl.Y;
       } else {
-        // a sub-volume of a pageable array: gathered dense, slice by slice
+        // other layouts: slice by slice
         for (int z = 0; z < pl.Z; z++)
           CU(cudaMemcpy2DAsync(dst + (size_t)z * pl.X * pl.Y * es, (size_t)pl.X * es,
                                static_cast<const char *>(pl.data) + (size_t)z * pl.pitchZ * es,
