@@ -454,6 +454,8 @@ def test_decompress_batch_equals_single(ctx):
                                   quant_alg=[P.LOG, P.UNIFORM, P.LLOYD][i % 3],
                                   transform_2d=(i == 6), threshold_fraction=0.8)))
     items.append((np.full((4, 8, 8), 7, np.uint8), P.Params(steps=(2, 2, 2))))  # one symbol
+    items.append((synth.scaled_blob_cubelet(rng, (12, 20, 16), np.uint16),  # no zero runs
+                  P.Params(steps=(2, 2, 2), compress_zeros=False, threshold_fraction=0.7)))
     comp = ctx.compress_batch(items)
     for name in ("uint8_1x64x64.p1.cube", "float32_12x20x24.p2.cube", "uint8_5x7x9.p8.cube"):
         c = cubefile.read_file(os.path.join(GOLDEN, name))[0]
@@ -477,3 +479,15 @@ def test_decompress_batch_equals_single(ctx):
     batch = ctx.decompress_batch(comp)
     for i, (x, y) in enumerate(zip(batch, single)):
         assert x.dtype == y.dtype and np.array_equal(x, y), i
+    # the same into device memory
+    offs, total = [], 0
+    for y in single:
+        offs.append(total)
+        total += (y.nbytes + 255) // 256 * 256
+    buf = lib.DeviceBuffer(total)
+    try:
+        ctx.decompress_batch(comp, device_outs=[buf.ptr + o for o in offs])
+        for i, (o, y) in enumerate(zip(offs, single)):
+            assert np.array_equal(buf.download(y.shape, y.dtype, o), y), i
+    finally:
+        buf.free()

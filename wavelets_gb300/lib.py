@@ -801,6 +801,16 @@ class DeviceBuffer:
         if st != WL_OK:
             raise WlError(st, "upload failed")
 
+    def download(self, shape, dtype, offset: int = 0) -> np.ndarray:
+        """A host copy of the bytes at offset as an array of shape and dtype."""
+        out = np.empty(shape, dtype)
+        assert offset + out.nbytes <= self.nbytes
+        st = self.lib.wl_copy_to_host(ctypes.c_void_p(out.ctypes.data),
+                                      ctypes.c_void_p(self.ptr + offset), out.nbytes)
+        if st != WL_OK:
+            raise WlError(st, "download failed")
+        return out
+
     def free(self):
         if self.ptr:
             self.lib.wl_device_free(self.ptr)
