@@ -28,7 +28,7 @@ constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
 constexpr int kCandSlices = 64;
 constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float order key
 constexpr int kLutStride = kLutCells + 8;  // per-cubelet table stride (16-byte rows)
-constexpr int kQuantGroup = 4;          // chunks per quantize CTA         // CTAs per cubelet over its threshold candidates
+constexpr int kQuantGroup = 8;          // chunks per quantize CTA         // CTAs per cubelet over its threshold candidates
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
 constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
 
