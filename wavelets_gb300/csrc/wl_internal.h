@@ -25,10 +25,10 @@ constexpr int kChunk = 4096;            // elements per quantize/encode chunk
 constexpr int kChunkThreads = 256;
 constexpr int kSelectBins = 4096;       // radix-select digit histogram
 constexpr int kLloydBins = 4096;        // |coefficient| histogram for Lloyd
-constexpr int kCandSlices = 64;
+constexpr int kCandSlices = 64;        // CTAs per cubelet over its threshold candidates
 constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float order key
 constexpr int kLutStride = kLutCells + 8;  // per-cubelet table stride (16-byte rows)
-constexpr int kQuantGroup = 8;          // chunks per quantize CTA         // CTAs per cubelet over its threshold candidates
+constexpr int kQuantGroup = 8;          // chunks per select / quantize / encode CTA
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
 constexpr int kMaxAxis = 16384;         // longest padded axis (one row per tile)
 
