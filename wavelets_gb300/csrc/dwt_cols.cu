@@ -66,14 +66,6 @@ template <> __device__ __forceinline__ void stage<float>(float *dst, const float
   cp_async4(dst, src);
 }
 
-// in-place position p -> band index q and level (S for the low band)
-__device__ __forceinline__ int pos_to_band(int p, int L, int S, int &lev) {
-  const int t = p ? __ffs(p) - 1 : S;
-  if (t >= S) { lev = S; return p >> S; }
-  lev = t;
-  return (L >> (t + 1)) + (p >> (t + 1));
-}
-
 // ---- one level of one column segment -----------------------------------------
 // x points at position 0 of the lane's row; consecutive elements of the level
 // are P = 2^k * 33 words apart.  Pair j is (e_j, o_j) = elements (2j, 2j+1),
