@@ -223,11 +223,11 @@ def _shuffled(items, seed=7):
     return [items[i] for i in order]
 
 
-def _timed_pool(sample, procs, budget_s, windows=1):
+def _timed_pool(sample, procs, budget_s, windows=None):
     """Compress cubelets of `sample` on `procs` spawned processes until the
     budget runs out; returns (bytes of completed cubelets, elapsed, count),
-    or with windows > 1 a list of those per equal time window.  Unfinished
-    cubelets are abandoned (the pool is terminated)."""
+    or with `windows` given a list of those per equal time window.
+    Unfinished cubelets are abandoned (the pool is terminated)."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     pool = ctx.Pool(procs)
@@ -253,7 +253,7 @@ def _timed_pool(sample, procs, budget_s, windows=1):
     finally:
         pool.terminate()
         pool.join()
-    if windows <= 1:
+    if windows is None:
         return sum(b for _, b in done), elapsed, len(done)
     w = elapsed / windows
     out = []
