@@ -1,21 +1,26 @@
-// Row-register wavelet pass: rows contiguous in memory on both sides, of a
-// power-of-two length L = 8 G (16 .. 256), each held by G lanes of a warp in
-// registers -- eight consecutive elements per lane, loaded and stored as
-// 16-byte words.  This is the forward z pass (the last forward pass, which
-// works in place on rows of the z-x-y layout), where the column-tile kernel
-// would stage every row through shared memory and split its levels into
-// segments with halos.
+// Row-register wavelet passes: a row of L = E G elements (E = 8: L a power
+// of two, 16 .. 256; E = 6: L = 48, 96, 192) is held by G lanes of a warp in
+// registers, E consecutive elements per lane, read with one to three vector
+// loads.  Three kernels use it:
+//   - the forward z pass, in place on rows contiguous on both sides (the
+//     column-tile kernel would stage every row through shared memory and
+//     split its levels into segments with halos);
+//   - the forward x pass, from the source rows (any element type, REPEAT
+//     clamp) through a shared-memory tile to an output in which consecutive
+//     rows are neighbours;
+//   - the inverse z pass, in place, reading a row's band values first.
 //
-// A level with m pairs per lane (m = 4, 2, 1 for levels 0, 1, 2) lifts the
-// lane's pairs in registers and takes the neighbouring pair values from the
-// next and previous lane (four shuffles per level).  After level 2 a lane holds
-// one low-pass value; each later level gathers pair j into lane j (two
-// shuffles) and runs with fewer lanes.  Detail bands leave as soon as they
-// are final, at their band positions (low band, then detail bands of the
-// last level down to the first, dwt_cpu.cc:703-728) with the deferred
-// lifting scale, so the band order costs nothing.  Every lifting step does the
-// same arithmetic as dwt.cu and dwt_cols.cu (the same operands in the same
-// order), so the coefficients are identical.
+// A level with m pairs per lane (m = 4, 2, 1 for levels 0, 1, 2 with E = 8;
+// 3, then two per lane on 3G/4 lanes, then one, with E = 6) lifts the lane's
+// pairs in registers and takes the neighbouring pair values from the next and
+// previous lane (four shuffles per level).  After level 2 a lane holds one
+// low-pass value; each later level gathers pair j into lane j (two shuffles)
+// and runs with fewer lanes.  Detail bands leave as soon as they are final,
+// at their band positions (low band, then detail bands of the last level down
+// to the first, dwt_cpu.cc:703-728) with the deferred lifting scale, so the
+// band order costs nothing.  Every lifting step does the same arithmetic as
+// dwt.cu and dwt_cols.cu (the same operands in the same order), so the
+// coefficients are identical.
 #include <cuda_runtime.h>
 
 #include <type_traits>
