@@ -14,8 +14,11 @@
 // predecessor's exit is decoded again from that exit; rounds repeat until no
 // start changes (each round fixes at least the first wrong subsequence).
 // Then an exclusive scan of the element counts gives every subsequence its
-// output offset, and a last pass decodes again and writes the elements.
-// A 12-bit lookup table resolves most codes in one step.
+// output offset, and a last pass decodes again and writes the elements (the
+// bins, or for batched decompression their dequantized values, where zero-bin
+// runs were set beforehand and are only skipped).  A 12-bit lookup table
+// resolves most codes in one step; each thread reads its stream through a
+// window of three words in registers.
 #include <cstring>
 #include <vector>
 
