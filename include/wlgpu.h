@@ -399,7 +399,11 @@ const char *wl_graph_error(const wl_ctx *ctx);
  * that device, so make the first call on each device before any stream
  * capture.  Every call shares the one array and clears what must start at
  * zero; calls whose work overlaps on the GPU (other streams, other host
- * threads) race and must be serialized by the caller. */
+ * threads) race and must be serialized by the caller.  The looked-up address
+ * is kept for the life of the process: after cudaDeviceReset on a device the
+ * library must be unloaded and loaded again before this entry point is used
+ * on that device.  A launch that fails returns WL_ECUDA; an error left pending
+ * by earlier, unrelated CUDA work is neither reported nor cleared. */
 #define WL_NOALLOC_MAX_ELEMENTS (64LL * 1024 * 1024)
 wl_status wl_select_threshold_noalloc(const float *coeffs, long long n,
                                       float fraction, void *stream, float *out);

@@ -37,6 +37,15 @@ def build_port(verbose=False):
     return lib, cli
 
 
+def reference_dir():
+    """The reference checkout: $WL_REFERENCE_DIR, else a directory named
+    `reference` beside this repository (None when neither exists; the GPU
+    box has no checkout, and nothing there needs one)."""
+    d = os.environ.get("WL_REFERENCE_DIR") or os.path.join(
+        os.path.dirname(os.path.dirname(HERE)), "reference")
+    return d if os.path.isdir(d) else None
+
+
 def build_reference(ref_dir):
     """Compile the reference CPU path (only where its sources exist)."""
     if not ref_dir or not os.path.isdir(ref_dir):

@@ -92,9 +92,9 @@ def kat_cdf97(ref_dump, tmp):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if not os.path.isdir(ref):
-        sys.exit("reference checkout not found: " + ref)
+    ref = sys.argv[1] if len(sys.argv) > 1 else build_oracle.reference_dir()
+    if not ref or not os.path.isdir(ref):
+        sys.exit("reference checkout not found: pass its path or set WL_REFERENCE_DIR")
     build_oracle.build_reference(ref)
     cli = os.path.join(ROOT, "oracle", "_ref", "test_compress_cpu")
     dump = os.path.join(ROOT, "oracle", "_ref", "ref_dump")

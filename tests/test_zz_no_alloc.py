@@ -3,13 +3,17 @@ allocation, for callers that may not call cudaMalloc (stream capture, fixed
 memory budgets, real-time loops).  Its scratch is a static device array, so
 this test also checks that a second call right after the first (different
 data) starts from clean scratch.  Compared against wl_compress_cubelet on
-the same coefficients; the values are order statistics and extremes, so they
-must match exactly.  Named test_zz_* so pytest collects it last."""
+the same coefficients and against the oracle (thresh_cpu, thresh_cpu.cc:80-109,
+fed those coefficients); the values are order statistics and extremes, so
+they must match exactly.  The cases include element counts that are not a
+multiple of the 4096-element chunk (a ragged last chunk, and a single partial
+chunk) and the fraction 1.0.  Named test_zz_* so pytest collects it last."""
 import ctypes
 
 import numpy as np
 import pytest
 
+from oracle import oracle
 from wavelets_gb300 import lib, params as P, synth
 
 pytestmark = pytest.mark.gpu
@@ -24,6 +28,14 @@ def test_noalloc_threshold_matches_compress():
         (synth.volume_f32(21, (32, 48, 64), 20),
          P.Params(steps=(3, 3, 3), threshold_fraction=0.95, quant_alg=P.UNIFORM, bin_count=1024)),
         (synth.plain_2d(22, 512), P.Params(steps=(9, 9, 0), threshold_fraction=0.9)),
+        # 2 x 33 x 17 (padded 2 x 40 x 24 = 1920 < one chunk)
+        (synth.scaled_blob_cubelet(np.random.default_rng(23), (2, 33, 17), np.uint8),
+         P.Params(steps=(3, 3, 1), threshold_fraction=0.7)),
+        # 37 x 41 x 43, no steps: 65231 elements, the last chunk ragged
+        (synth.scaled_blob_cubelet(np.random.default_rng(24), (37, 41, 43), np.float32),
+         P.Params(steps=(0, 0, 0), threshold_fraction=0.5)),
+        (synth.volume_f32(25, (24, 40, 48), 10),
+         P.Params(steps=(3, 3, 3), threshold_fraction=1.0)),
     ]
     dout = lib.DeviceBuffer(64)
     try:
@@ -44,6 +56,12 @@ def test_noalloc_threshold_matches_compress():
             assert got[1] == np.float32(comp.min_coef)
             assert got[2] == np.float32(comp.max_coef)
             assert got[3] == np.float32(comp.max_value)
+            ref = oracle.encode(coeffs, p.threshold_fraction, p.bin_count, oracle.UNIFORM)
+            assert got[0] == np.float32(ref["threshold"])
+            assert (got[1], got[2], got[3]) == (np.float32(ref["min"]), np.float32(ref["max"]),
+                                                np.float32(ref["max_abs"]))
+            # second largest |c|
+            assert got[4] == np.sort(np.abs(coeffs))[-2]
             dbuf.free()
     finally:
         dout.free()

@@ -230,18 +230,27 @@ extern "C" wl_status wl_select_threshold_noalloc(const float *coeffs, long long 
   if (n > WL_NOALLOC_MAX_ELEMENTS) return WL_EINVAL;
   if (!(fraction >= 0.f && fraction <= 1.f)) return WL_EINVAL;
   NoallocScratch *s = nullptr;
-  if (noalloc_scratch_ptr(&s) != cudaSuccess) {
-    cudaGetLastError();
-    return WL_ECUDA;
-  }
+  if (noalloc_scratch_ptr(&s) != cudaSuccess) return WL_ECUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nChunks = (int)((n + kChunk - 1) / kChunk);
-  noalloc_clear<<<1, 1024, 0, st>>>(s);
-  noalloc_pass<0><<<nChunks, kThreads, 0, st>>>(coeffs, n, s);
-  noalloc_resolve<0><<<1, 1024, 0, st>>>(n, nChunks, fraction, s, out);
-  noalloc_pass<1><<<nChunks, kThreads, 0, st>>>(coeffs, n, s);
-  noalloc_resolve<1><<<1, 1024, 0, st>>>(n, nChunks, fraction, s, out);
-  noalloc_pass<2><<<nChunks, kThreads, 0, st>>>(coeffs, n, s);
-  noalloc_resolve<2><<<1, 1024, 0, st>>>(n, nChunks, fraction, s, out);
-  return cudaGetLastError() == cudaSuccess ? WL_OK : WL_ECUDA;
+  // Each launch's own status is checked (cudaLaunchKernel returns it), so an
+  // error left pending by earlier, unrelated work is neither reported here
+  // nor cleared.
+  const float *cp = coeffs;
+  long long nn = n;
+  int nc = nChunks;
+  float fr = fraction;
+  float *op = out;
+  void *aClear[] = {&s};
+  void *aPass[] = {&cp, &nn, &s};
+  void *aRes[] = {&nn, &nc, &fr, &s, &op};
+  const dim3 one(1), big(1024), grid(nChunks), blk(kThreads);
+  cudaError_t e = cudaLaunchKernel((const void *)noalloc_clear, one, big, aClear, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_pass<0>, grid, blk, aPass, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_resolve<0>, one, big, aRes, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_pass<1>, grid, blk, aPass, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_resolve<1>, one, big, aRes, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_pass<2>, grid, blk, aPass, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void *)noalloc_resolve<2>, one, big, aRes, 0, st);
+  return e == cudaSuccess ? WL_OK : WL_ECUDA;
 }
