@@ -26,6 +26,7 @@
 #include <type_traits>
 
 #include "dwt_common.cuh"
+#include "select_common.cuh"
 #include "wl_internal.h"
 
 namespace wl {
@@ -84,6 +85,29 @@ struct GlobalRow {  // the row itself, in place (float row, 16-byte aligned)
   }
   __device__ void put4(int q, float a, float b, float c, float d) const {
     *reinterpret_cast<float4 *>(dst + q) = make_float4(a, b, c, d);
+  }
+};
+// The last pass of a compression: the row in place, every value also counted
+// into the select statistics (first radix-select digit, extremes) while it is
+// still in a register.
+struct GlobalRowSel {
+  float *dst;
+  selc::SelAcc *acc;
+  __device__ void put(int q, float v) const {
+    dst[q] = v;
+    acc->visit(v);
+  }
+  __device__ void put2(int q, float a, float b) const {
+    *reinterpret_cast<float2 *>(dst + q) = make_float2(a, b);
+    acc->visit(a);
+    acc->visit(b);
+  }
+  __device__ void put4(int q, float a, float b, float c, float d) const {
+    *reinterpret_cast<float4 *>(dst + q) = make_float4(a, b, c, d);
+    acc->visit(a);
+    acc->visit(b);
+    acc->visit(c);
+    acc->visit(d);
   }
 };
 struct TileRow {  // column r of a shared-memory tile, position q at q * P + r
@@ -176,12 +200,13 @@ __device__ __forceinline__ void rowreg_levels(float (&e)[E / 2], float (&o)[E / 
 }
 
 // The rows [row0, row0 + kRegThreads / G) of one in-place pass of float rows;
-// E = 8 or 6 elements per lane (L = E G).
-template <int G, int E, bool HAAR>
-__device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *scaleTab) {
+// E = 8 or 6 elements per lane (L = E G).  scaleTab holds the deferred
+// lifting scales; SEL: every value written is also visited by acc.
+template <int G, int E, bool HAAR, bool SEL>
+__device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, const float *scaleTab,
+                                           selc::SelAcc &acc) {
   constexpr int M = E / 2;
   const int S = d.steps;
-  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
   const int row = row0 + (int)threadIdx.x / G;
   const int sub = threadIdx.x & (G - 1);
   const bool ok = row < d.rows;
@@ -212,11 +237,12 @@ __device__ __forceinline__ void rowreg_fwd(const PassDesc &d, int row0, float *s
 #pragma unroll
     for (int k = 0; k < M; k++) e[k] = o[k] = 0.f;
   }
-  // the row is read by all its lanes before any of them stores (in place);
-  // the scale table is written
-  __syncthreads();
-  rowreg_levels<G, E, HAAR>(e, o, sub, S, scaleTab, ok,
-                            GlobalRow{static_cast<float *>(d.out) + bo});
+  // in place: the row (held by lanes of one warp) is read by all its lanes
+  // before any of them stores
+  __syncwarp();
+  float *dst = static_cast<float *>(d.out) + bo;
+  if (SEL) rowreg_levels<G, E, HAAR>(e, o, sub, S, scaleTab, ok, GlobalRowSel{dst, &acc});
+  else rowreg_levels<G, E, HAAR>(e, o, sub, S, scaleTab, ok, GlobalRow{dst});
 }
 
 // E elements [first, first + E) of a row of n real elements as floats: one
@@ -578,12 +604,20 @@ void launch_ig(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t
   dwt_rowreg_inv_kernel<G, E><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
 }
 
-// One block: kRegThreads / G rows of the pass found by the tile prefix.
-template <int G, int E>
+// Row rounds per block of the forward pass that also gathers the select
+// statistics: about 16 K values per block, so that the block's shared digit
+// histogram is flushed once per 16 K values.
+__host__ __device__ constexpr int rowreg_sel_rounds(int E) { return E == 8 ? 8 : 10; }
+
+// One block: kRegThreads / G rows of the pass found by the tile prefix (SEL:
+// rowreg_sel_rounds(E) such row rounds, and the select statistics of every
+// value written, merged into the cubelet's once at the end).
+template <int G, int E, bool SEL>
 __global__ void __launch_bounds__(kRegThreads)
 dwt_rowreg_fwd_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                       int nPasses) {
   __shared__ float scaleTab[16];
+  __shared__ unsigned hist[SEL ? kSelectBins : 1];
   const int bid = blockIdx.x;
   int lo = 0, hi = nPasses - 1;
   while (lo < hi) {
@@ -591,14 +625,28 @@ dwt_rowreg_fwd_kernel(const PassDesc *__restrict__ passes, const int *__restrict
     if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
   }
   const PassDesc &d = passes[lo];
-  const int row0 = (bid - tilePrefix[lo]) * (kRegThreads / G);
-  if (d.wavelet == WL_HAAR) rowreg_fwd<G, E, true>(d, row0, scaleTab);
-  else rowreg_fwd<G, E, false>(d, row0, scaleTab);
+  constexpr int kRows = kRegThreads / G;
+  constexpr int kRounds = SEL ? rowreg_sel_rounds(E) : 1;
+  const int row0 = (bid - tilePrefix[lo]) * kRounds * kRows;
+  const int S = d.steps;
+  const bool haar = d.wavelet == WL_HAAR;
+  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = haar ? 1.0f : lifting_scale(threadIdx.x, S);
+  if (SEL) selc::clear_hist<kRegThreads>(hist);
+  selc::SelAcc acc{hist};
+  __syncthreads();
+  for (int r = 0; r < kRounds; r++) {
+    const int rr = row0 + r * kRows;
+    if (rr >= d.rows) break;  // the same for every thread of the block
+    if (haar) rowreg_fwd<G, E, true, SEL>(d, rr, scaleTab, acc);
+    else rowreg_fwd<G, E, false, SEL>(d, rr, scaleTab, acc);
+  }
+  if (SEL) selc::flush<kRegThreads>(acc, d.selHist, d.selState);
 }
 
 template <int G, int E = 8>
-void launch_g(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
-  dwt_rowreg_fwd_kernel<G, E><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
+void launch_g(const PassDesc *p, const int *tp, int n, int blocks, bool sel, cudaStream_t s) {
+  if (sel) dwt_rowreg_fwd_kernel<G, E, true><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
+  else dwt_rowreg_fwd_kernel<G, E, false><<<blocks, kRegThreads, 0, s>>>(p, tp, n);
 }
 
 }  // namespace
@@ -610,7 +658,10 @@ static int rowreg_lanes(int L) {
   return 0;
 }
 
-int dwt_rowreg_rows_per_block(int L) { return kRegThreads / rowreg_lanes(L); }
+int dwt_rowreg_rows_per_block(int L, bool sel) {
+  const int rows = kRegThreads / rowreg_lanes(L);
+  return sel ? rows * rowreg_sel_rounds((L & (L - 1)) ? 6 : 8) : rows;
+}
 
 bool dwt_rowreg_fits(int L, int steps) {
   return rowreg_lanes(L) > 0 && steps >= 1 && L % (1 << steps) == 0 &&
@@ -651,17 +702,17 @@ void launch_dwt_rowreg_inv(const PassDesc *p, const int *tp, int n, int blocks, 
   }
 }
 
-void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int L,
+void launch_dwt_rowreg(const PassDesc *p, const int *tp, int n, int blocks, int L, bool sel,
                        cudaStream_t s) {
   switch (L) {
-    case 16: launch_g<2>(p, tp, n, blocks, s); break;
-    case 32: launch_g<4>(p, tp, n, blocks, s); break;
-    case 48: launch_g<8, 6>(p, tp, n, blocks, s); break;
-    case 64: launch_g<8>(p, tp, n, blocks, s); break;
-    case 96: launch_g<16, 6>(p, tp, n, blocks, s); break;
-    case 128: launch_g<16>(p, tp, n, blocks, s); break;
-    case 192: launch_g<32, 6>(p, tp, n, blocks, s); break;
-    default: launch_g<32>(p, tp, n, blocks, s); break;
+    case 16: launch_g<2>(p, tp, n, blocks, sel, s); break;
+    case 32: launch_g<4>(p, tp, n, blocks, sel, s); break;
+    case 48: launch_g<8, 6>(p, tp, n, blocks, sel, s); break;
+    case 64: launch_g<8>(p, tp, n, blocks, sel, s); break;
+    case 96: launch_g<16, 6>(p, tp, n, blocks, sel, s); break;
+    case 128: launch_g<16>(p, tp, n, blocks, sel, s); break;
+    case 192: launch_g<32, 6>(p, tp, n, blocks, sel, s); break;
+    default: launch_g<32>(p, tp, n, blocks, sel, s); break;
   }
 }
 

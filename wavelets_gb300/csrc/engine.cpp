@@ -418,8 +418,12 @@ wl_status check_params(wl_ctx *ctx, const wl_params &p) {
 // z pass z-x-y in place (a-b-c lists axes from fastest to slowest).  Rows
 // are numbered so that neighbouring rows are neighbours in memory on every
 // side whose element stride is not 1.
-void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
-                         PassGroups &xs, PassGroups &ys, PassGroups &zs) {
+// selHist / selState: the cubelet's select histogram and state; a z pass on
+// the row-register kernel, the last pass, gathers the first select digit and
+// the extremes into them.  Returns true when it does.
+bool forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
+                         PassGroups &xs, PassGroups &ys, PassGroups &zs,
+                         unsigned *selHist = nullptr, CubeletState *selState = nullptr) {
   const int big = 0x7fffffff;
   const long long Xp = pl.Xp, Yp = pl.Yp, Zp = pl.Zp;
   float *o = coef + pl.coefOff;
@@ -458,7 +462,7 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   e.steps = pl.sy;
   e.T = dwt_cols_tile_rows(e.L); e.tiles = (e.rows + e.T - 1) / e.T;
   ys[group_key(true, WL_F32, e.L)].push_back(e);
-  if (pl.sz == 0) return;
+  if (pl.sz == 0) return false;
   // z pass: rows (a = y, b = x) of z-x-y, in place
   PassDesc f = e;
   f.in = o;
@@ -468,12 +472,16 @@ void forward_passes_cols(const Plan &pl, const void *in, bool hostIn, float *coe
   f.outSA = Zp * Xp; f.outSB = Zp; f.outSC = 1;
   f.steps = pl.sz;
   if (dwt_rowreg_fits(f.L, f.steps)) {
-    f.T = dwt_rowreg_rows_per_block(f.L); f.tiles = (f.rows + f.T - 1) / f.T;
+    f.selHist = selHist;
+    f.selState = selState;
+    f.T = dwt_rowreg_rows_per_block(f.L, selHist != nullptr);
+    f.tiles = (f.rows + f.T - 1) / f.T;
     zs[rowreg_key(f.L)].push_back(f);
-    return;
+    return selHist != nullptr;
   }
   f.T = dwt_cols_tile_rows(f.L); f.tiles = (f.rows + f.T - 1) / f.T;
   zs[group_key(true, WL_F32, f.L)].push_back(f);
+  return false;
 }
 
 // 2-D mode (cdf97_2d / haar_2d, dwt_cpu.cc:811-864 and :495-547): x and y
@@ -528,16 +536,17 @@ void forward_passes_2d(const Plan &pl, const void *in, bool hostIn, float *coef,
   ys[group_key(pl.cols, WL_F32, e.L)].push_back(e);
 }
 
-void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
-                    PassGroups &xs, PassGroups &ys, PassGroups &zs) {
+// Returns true when the last pass gathers the first select digit and the
+// extremes (see forward_passes_cols).
+bool forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, float *coef2,
+                    PassGroups &xs, PassGroups &ys, PassGroups &zs, unsigned *selHist = nullptr,
+                    CubeletState *selState = nullptr) {
   if (pl.two_d && !pl.identity) {
     forward_passes_2d(pl, in, hostIn, coef, coef2, xs, ys);
-    return;
+    return false;
   }
-  if (pl.cols) {
-    forward_passes_cols(pl, in, hostIn, coef, coef2, xs, ys, zs);
-    return;
-  }
+  if (pl.cols)
+    return forward_passes_cols(pl, in, hostIn, coef, coef2, xs, ys, zs, selHist, selState);
   const int big = 0x7fffffff;
   const float *c = coef + pl.coefOff;
   float *o = coef + pl.coefOff;
@@ -566,7 +575,7 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
   d.T = dwt_tile_rows(d.L, d.exact && d.wavelet == WL_CDF97);
   d.tiles = (d.rows + d.T - 1) / d.T;
   xs[group_key(false, pl.dtype, d.L)].push_back(d);
-  if (pl.identity) return;
+  if (pl.identity) return false;
   // y pass: rows (x, z) of the y-z-x cube -> z-x-y
   PassDesc e;
   memset(&e, 0, sizeof e);
@@ -581,7 +590,7 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
   e.T = dwt_tile_rows(e.L, e.exact && e.wavelet == WL_CDF97);
   e.tiles = (e.rows + e.T - 1) / e.T;
   ys[group_key(false, WL_F32, e.L)].push_back(e);
-  if (pl.sz == 0) return;
+  if (pl.sz == 0) return false;
   // z pass: rows (y, x) of the z-x-y cube, in place
   PassDesc f = e;
   f.in = c;
@@ -593,6 +602,7 @@ void forward_passes(const Plan &pl, const void *in, bool hostIn, float *coef, fl
   f.T = dwt_tile_rows(f.L, f.exact && f.wavelet == WL_CDF97);
   f.tiles = (f.rows + f.T - 1) / f.T;
   zs[group_key(false, WL_F32, f.L)].push_back(f);
+  return false;
 }
 
 // One launch of a transform pass group: its descriptors and tile prefix sit
@@ -603,6 +613,7 @@ struct GroupLaunch {
   bool inverse, cols, vec;
   int regL;  // row-register pass of rows of regL elements (0: another kernel)
   int regKind;  // which row-register kernel (RegKind)
+  bool sel;     // in-place row-register pass gathering the select statistics
   // bytes a launch moves, for ordering concurrent groups
   double weight() const { return (double)tiles * (regL ? 4.0 * regL * rows : (double)smem); }
 };
@@ -621,9 +632,13 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
   if (hoff + bytes > ctx->hPasses.cap || hoff + bytes > ctx->passes.cap)
     return fail(ctx, WL_ENOMEM, "pass staging too small");
   int rows = 0, warps = 4;
+  const bool sel = regKind == kRegInPlace && g[0].selHist != nullptr;
+  for (const PassDesc &d : g)
+    if ((d.selHist != nullptr) != sel)
+      return fail(ctx, WL_EINVAL, "internal: mixed select-gathering passes in one group");
   if (regL) {
     rows = regKind == kRegTile ? dwt_rowreg_t_rows_per_block(regL)
-                               : dwt_rowreg_rows_per_block(regL);
+                               : dwt_rowreg_rows_per_block(regL, sel);
     for (PassDesc &d : g) {
       d.T = rows;
       d.tiles = (d.rows + rows - 1) / rows;
@@ -654,7 +669,7 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
   }
   tp[n] = tiles;
   out.push_back({hoff, (int)n, tiles, smem, rows, warps, inType, outType, inverse, cols, vec,
-                 regL, regKind});
+                 regL, regKind, sel});
   hoff += (bytes + 255) & ~(size_t)255;
   return WL_OK;
 }
@@ -683,7 +698,7 @@ wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
   else if (l.regKind == kRegInvInPlace)
     launch_dwt_rowreg_inv(dp, dtp, l.n, l.tiles, l.regL, s);
   else if (l.regL)
-    launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, s);
+    launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, l.sel, s);
   else if (l.cols)
     launch_dwt_cols(dp, dtp, l.n, l.tiles, l.smem, l.rows, l.warps, l.inType, l.outType, l.inverse,
                     l.vec, s);
@@ -960,8 +975,13 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.totalChunks = chunkTotal;
 
   PassGroups xs, ys, zs;
-  for (int i = 0; i < n; i++)
-    forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs, ys, zs);
+  bool pass0 = false;  // some cubelet needs the stand-alone first select pass
+  for (int i = 0; i < n; i++) {
+    const bool fused = forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs, ys,
+                                      zs, b.selHist + (size_t)i * kSelectBins, b.state + i);
+    hc[i].selFused = fused ? 1 : 0;
+    pass0 |= !fused;
+  }
   std::vector<GroupLaunch> gl;
   size_t hoff = cubBytes + prefBytes;
   TRY(stage_groups(ctx, xs, hoff, kTuneFwdX, WL_F32, false, gl));
@@ -1013,6 +1033,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     CU(cudaMemsetAsync(ctx->selHist.p, 0, (size_t)n * kSelectBins * 4, s));
     CU(cudaMemsetAsync(ctx->hist.p, 0, (size_t)n * kMaxSymbols * 8, s));
     if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
+    launch_select_init(b, s);
+    ctx->launches += 1;
     mark(ctx, 0);
     TRY(launch_phase(ctx, gl, 0, gx));
     mark(ctx, 1);
@@ -1022,8 +1044,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     mark(ctx, 3);
     CU(record(ctx, ctx->ev[1]));
     if (coefOut) return WL_OK;
-    launch_select(b, b.coef, s);
-    ctx->launches += 9;
+    launch_select(b, b.coef, pass0, s);
+    ctx->launches += pass0 ? 8 : 7;
     CU(cudaGetLastError());
     mark(ctx, 4);
     if (anyLog)

@@ -20,6 +20,7 @@
 #include <cfloat>
 #include <type_traits>
 
+#include "select_common.cuh"
 #include "wl_internal.h"
 
 namespace wl {
@@ -29,23 +30,9 @@ constexpr int kThreads = kChunkThreads;
 constexpr int kPerThread = kChunk / kThreads;
 static_assert(kPerThread == 16, "load_chunk assumes four float4 per thread");
 
-// float -> unsigned with the same order (for atomicMin/Max on signed values)
-__device__ __forceinline__ unsigned ord_enc(float f) {
-  unsigned u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float ord_dec(unsigned u) {
-  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
-}
-
-// top-2 merge of multisets {a1,a2} and {b1,b2} (a1>=a2, b1>=b2)
-__device__ __forceinline__ void top2_merge(unsigned &a1, unsigned &a2, unsigned b1, unsigned b2) {
-  unsigned t1 = max(a1, b1);
-  unsigned t2 = max(min(a1, b1), max(a2, b2));
-  a1 = t1;
-  a2 = t2;
-}
-
+using selc::ord_dec;
+using selc::ord_enc;
+using selc::top2_merge;
 
 // element of the chunk held in v[k] by this thread: float4 j = threadIdx.x +
 // kThreads * (k / 4), so every warp load is 512 contiguous bytes
@@ -77,80 +64,33 @@ __device__ __forceinline__ void load_chunk(const float *src, int len, float (&v)
 __global__ void __launch_bounds__(kThreads, 6)
 select_pass0(DevBatch b, const float *__restrict__ coef) {
   __shared__ unsigned hist[kSelectBins];
-  __shared__ unsigned sMin[kThreads / 32], sMax[kThreads / 32], sA1[kThreads / 32], sA2[kThreads / 32];
   const int ci = b.groupCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
+  if (cd.selFused) return;  // the last transform pass gathered these already
   const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
   const int nc = min(kQuantGroup, cd.nChunks - c0);
-  CubeletState *st = b.state + ci;
   auto chunk_len = [&](int k) {
     return (int)min((long long)kChunk, cd.n - (long long)(c0 + k) * kChunk);
   };
   auto chunk_src = [&](int k) { return coef + cd.coefOff + (long long)(c0 + k) * kChunk; };
 
-  for (int i = threadIdx.x; i < kSelectBins; i += kThreads) hist[i] = 0;
+  selc::clear_hist<kThreads>(hist);
   __syncthreads();
-
-  // min and max as floats, like the reference's x < min / x > max from FLT_MAX
-  // and FLT_MIN (a NaN never replaces either); ordered keys for the merge
-  float fmn = FLT_MAX, fmx = FLT_MIN;
-  unsigned a1 = 0u, a2 = 0u;
-  auto visit = [&](float x) {
-    const unsigned a = __float_as_uint(x) & 0x7fffffffu;
-    atomicAdd(&hist[a >> 20], 1u);
-    fmn = fminf(fmn, x);
-    fmx = fmaxf(fmx, x);
-    a2 = max(a2, min(a1, a));  // top2_merge(a1, a2, a, 0)
-    a1 = max(a1, a);
-  };
+  selc::SelAcc acc{hist};
   for (int k = 0; k < nc; k++) {
     const int len = chunk_len(k);
     float v[kPerThread];
     load_chunk(chunk_src(k), len, v);
     if (len == kChunk) {
 #pragma unroll
-      for (int j = 0; j < kPerThread; j++) visit(v[j]);
+      for (int j = 0; j < kPerThread; j++) acc.visit(v[j]);
     } else {
 #pragma unroll
       for (int j = 0; j < kPerThread; j++)
-        if (chunk_index(j) < len) visit(v[j]);
+        if (chunk_index(j) < len) acc.visit(v[j]);
     }
   }
-  unsigned mn = ord_enc(fmn), mx = ord_enc(fmx);
-  for (int off = 16; off > 0; off >>= 1) {
-    mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-    unsigned b1 = __shfl_xor_sync(0xffffffffu, a1, off);
-    unsigned b2 = __shfl_xor_sync(0xffffffffu, a2, off);
-    top2_merge(a1, a2, b1, b2);
-  }
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { sMin[w] = mn; sMax[w] = mx; sA1[w] = a1; sA2[w] = a2; }
-  __syncthreads();
-  unsigned *g = b.selHist + (size_t)ci * kSelectBins;
-  for (int i = threadIdx.x; i < kSelectBins; i += kThreads)
-    if (hist[i]) atomicAdd(&g[i], hist[i]);
-  if (threadIdx.x == 0) {
-    for (int w2 = 1; w2 < kThreads / 32; w2++) {
-      mn = min(mn, sMin[w2]);
-      mx = max(mx, sMax[w2]);
-      top2_merge(a1, a2, sA1[w2], sA2[w2]);
-    }
-    atomicMin(&st->minOrd, mn);
-    atomicMax(&st->maxOrd, mx);
-    // merge the pair into (absMax, absMax2) with a 64-bit CAS loop
-    unsigned long long *pair = reinterpret_cast<unsigned long long *>(&st->absMax);
-    unsigned long long old = *pair, assumed;
-    do {
-      assumed = old;
-      unsigned c1 = (unsigned)(assumed & 0xffffffffu), c2 = (unsigned)(assumed >> 32);
-      unsigned n1 = c1, n2 = c2;
-      top2_merge(n1, n2, a1, a2);
-      unsigned long long nv = ((unsigned long long)n2 << 32) | n1;
-      if (nv == assumed) break;
-      old = atomicCAS(pair, assumed, nv);
-    } while (old != assumed);
-  }
+  selc::flush<kThreads>(acc, b.selHist + (size_t)ci * kSelectBins, b.state + ci);
 }
 
 // Second full pass: compact the coefficients of the threshold bucket
@@ -372,12 +312,15 @@ __global__ void select_init(DevBatch b) {
 
 }  // namespace
 
-void launch_select(DevBatch &b, const float *coef, cudaStream_t s) {
-  chunk_map_kernel<<<b.n, 256, 0, s>>>(b);
+void launch_select_init(DevBatch &b, cudaStream_t s) {
   select_init<<<(b.n + 127) / 128, 128, 0, s>>>(b);
+}
+
+void launch_select(DevBatch &b, const float *coef, bool pass0, cudaStream_t s) {
+  chunk_map_kernel<<<b.n, 256, 0, s>>>(b);
   unsigned *cand = reinterpret_cast<unsigned *>(b.coef2);
   const unsigned groups = (unsigned)b.totalGroups;
-  select_pass0<<<groups, kThreads, 0, s>>>(b, coef);
+  if (pass0) select_pass0<<<groups, kThreads, 0, s>>>(b, coef);
   select_resolve<0><<<b.n, 1024, 0, s>>>(b);
   select_compact<<<groups, kThreads, 0, s>>>(b, coef, cand);
   cand_hist<1><<<dim3(kCandSlices, b.n), kThreads, 0, s>>>(b, cand);

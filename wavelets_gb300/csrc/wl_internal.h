@@ -86,6 +86,8 @@ __host__ __device__ inline int run_token_count(long long L) {
   return q + big + lo;
 }
 
+struct CubeletState;
+
 struct PassDesc {
   const void *in;
   void *out;
@@ -103,6 +105,11 @@ struct PassDesc {
   int clampL, clampB, clampA;  // forward load: source sizes (REPEAT padding)
   int cropL, cropB, cropA;     // inverse store: destination sizes (crop)
   int vecLoad;                 // source is page-locked host memory: 16-byte row loads
+  // last forward pass of a compression (row-register z pass): also gather the
+  // first radix-select digit histogram and the extremes of the values it
+  // writes into these (null: no statistics)
+  unsigned *selHist;
+  CubeletState *selState;
 };
 
 // Per-cubelet state written by the kernels and read back by the host.
@@ -158,6 +165,8 @@ struct CubeletDev {
   int tableOff;           // offset into per-cubelet quantizer tables (floats)
   int nTable;             // entries in the table (log: boundaries; lloyd: boundaries)
   int groupBase;          // first quantize group (kQuantGroup chunks per group)
+  int selFused;           // 1: the last transform pass gathered the first select
+                          // digit and the extremes (no stand-alone first pass)
 };
 
 // Device workspace for one batch.
@@ -219,9 +228,12 @@ bool dwt_cols_rows_fit(int L, int rows);      // rows in {32, 64, 128} and smem 
 // row-register forward passes (dwt_rows.cu): float rows contiguous on both
 // sides, L a power of two in 16 .. 256, 1 <= steps <= log2 L
 bool dwt_rowreg_fits(int L, int steps);
-int dwt_rowreg_rows_per_block(int L);
+// rows per block; sel: the last pass, which also gathers the select
+// statistics of the values it writes (PassDesc::selHist), several row rounds
+// per block
+int dwt_rowreg_rows_per_block(int L, bool sel = false);
 void launch_dwt_rowreg(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses, int blocks,
-                       int L, cudaStream_t s);
+                       int L, bool sel, cudaStream_t s);
 // the same with the rows read from any element type (REPEAT clamp) and
 // stored through a shared-memory tile to an output where consecutive rows
 // are neighbours (forward x and y passes)
@@ -249,7 +261,12 @@ void set_tuned_cols_shape(int kind, int typeIdx, int cls, TileShape t,
 unsigned tune_version();  // changes whenever the table does
 
 // launchers (select.cu)
-void launch_select(DevBatch &b, const float *coef, cudaStream_t s);
+// per-cubelet select state (extremes from FLT_MAX / FLT_MIN); runs before the
+// transform, whose last pass may gather the first digit
+void launch_select_init(DevBatch &b, cudaStream_t s);
+// pass0: run the stand-alone first digit pass for the cubelets whose last
+// transform pass did not gather it (CubeletDev::selFused == 0)
+void launch_select(DevBatch &b, const float *coef, bool pass0, cudaStream_t s);
 
 // launchers (quant.cu)
 void launch_quant_params(DevBatch &b, cudaStream_t s);
