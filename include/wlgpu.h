@@ -193,6 +193,15 @@ wl_status wl_last_timings(const wl_ctx *ctx, float out[6]);
  * overlap).  Results are identical. */
 wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode);
 
+/* Cap the device workspace a context holds (its grow-only buffers) at
+ * `bytes` (0, the default: no cap), for hosts that give the library a fixed
+ * memory budget.  A call that would need more fails with WL_ENOMEM before
+ * anything is freed or launched, and the context stays usable.  Buffers
+ * already held above a new, lower cap are kept until they must grow.
+ * wl_memory_held: the bytes held now. */
+wl_status wl_set_memory_limit(wl_ctx *ctx, size_t bytes);
+size_t wl_memory_held(const wl_ctx *ctx);
+
 /* Synchronize the context's stream. */
 wl_status wl_sync(wl_ctx *ctx);
 
@@ -407,6 +416,35 @@ const char *wl_graph_error(const wl_ctx *ctx);
 #define WL_NOALLOC_MAX_ELEMENTS (64LL * 1024 * 1024)
 wl_status wl_select_threshold_noalloc(const float *coeffs, long long n,
                                       float fraction, void *stream, float *out);
+
+/* ---- Error metrics (-err) -------------------------------------------------
+ * The reference's -err (computeErrorRates / computeErrorRatesAfterDequant,
+ * test_compress_common.cc:587-694; ErrorAccumulator,
+ * test_compress_common.h:90-160): the compressed cubelet is restored on the
+ * device and compared with its original element by element.  Each pair adds
+ * (in double) a, a*a, |a-b| and |a-b|^2 with the products and the difference
+ * taken in float, a being the original value and b the restored value as the
+ * reference converts it: 8-bit clamped to 0..255 and truncated, 32-bit and
+ * 16-bit integers (int)(f + 0.5f), float32 (int)f (a quirk of the reference,
+ * kept).  max_possible is the PSNR peak: <= 0 means 255 for 8-bit data; other
+ * types without a positive maximum get no metrics (count 0 and zeros, as the
+ * reference prints "Cannot compute error rates").  The float fields are the
+ * reference's getters: average = sum|d| / count, l1 = sum|d|,
+ * l2 = sqrt(sum d^2), mse = sum d^2 / count, psnr = 10 log10(max^2 / mse)
+ * (0 when mse is 0), relative_error = sum d^2 / sum a^2. */
+typedef struct {
+  long long count;
+  float average_error, l1, l2, mse, psnr, relative_error;
+  double sum_value, sum_value_squared, sum_diff, sum_diff_squared;
+} wl_error_stats;
+wl_status wl_error_metrics(wl_ctx *ctx, const wl_result *compressed, const void *original,
+                           int original_dtype, int original_on_device, float max_possible,
+                           wl_error_stats *out);
+/* The same for files: the first uncompressed cubelet of original_path (its
+ * maximum_value field is the PSNR peak) against the first compressed cubelet
+ * of compressed_path. */
+wl_status wl_error_metrics_file(wl_ctx *ctx, const char *original_path,
+                                const char *compressed_path, wl_error_stats *out);
 
 /* Page-locked host memory for inputs and outputs of the host-pointer entry
  * points (copies from it overlap with device work). */

@@ -158,6 +158,23 @@ def compress_volume(arr_zyx, steps, wavelet, frac, bin_count, quant_alg,
     return res
 
 
+def error_metrics(orig_path, comp_path):
+    """-err metrics of the first compressed cubelet of comp_path against the
+    first uncompressed cubelet of orig_path (computeErrorRates,
+    test_compress_common.cc:587-694).  Returns a dict of the accumulator's
+    sums, count and getters."""
+    sums = (ctypes.c_double * 4)()
+    count = ctypes.c_longlong()
+    g = (ctypes.c_float * 6)()
+    rc = lib().orc_error_metrics(orig_path.encode(), comp_path.encode(), sums,
+                                 ctypes.byref(count), g)
+    if rc != 0:
+        raise RuntimeError("oracle error metrics failed")
+    return {"sum_value": sums[0], "sum_value_squared": sums[1], "sum_diff": sums[2],
+            "sum_diff_squared": sums[3], "count": count.value, "average_error": g[0],
+            "l1": g[1], "l2": g[2], "mse": g[3], "psnr": g[4], "relative_error": g[5]}
+
+
 def main(args):
     """Run the oracle's command line (the reference's flags)."""
     argv = ["oracle_cli"] + list(args)

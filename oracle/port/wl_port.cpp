@@ -781,19 +781,16 @@ int compress_common(const void *data, int dtype, int X, int Y, int Z, int sx,
   return write_cube_file(out_path, {m}, {words}, false) ? 0 : 1;
 }
 
-// Decompress the first compressed INT32 cubelet of in_path to out_path
-// (decompressFile, test_compress_cpu.cc:187-241).
-int decompress_file(const char *in_path, const char *out_path) {
-  std::vector<ReadCube> cubes;
-  if (!read_cube_file(in_path, cubes)) return 1;
-  const ReadCube *rc = nullptr;
-  for (auto &c : cubes)
-    if (c.meta.data_type() == CubeletBuffer_DataType_INT32 &&
-        c.meta.compression_algorithm() == CubeletBuffer_CompressionAlgorithm_WAVELET) {
-      rc = &c;
-      break;
-    }
-  if (!rc) return 1;
+// A compressed cubelet's dequantized, inverse-transformed floats in the
+// padded x-fastest layout (Xp x Yp x Zp): readQuantData + dequantize +
+// inverse waveletTransform (test_compress_cpu.cc:187-220).
+struct Restored {
+  std::vector<float> v;
+  int Xp = 0, Yp = 0, Zp = 0;
+  int ox = 0, oy = 0, oz = 0, odt = ORC_FLOAT32;
+};
+
+int restore_floats(const ReadCube *rc, Restored &R) {
   const CompressionParametersBuffer &p = rc->meta.compression_parameters();
   int W = rc->meta.width(), H = rc->meta.height(), D = rc->meta.depth();
   long n = (long)W * H * D;
@@ -821,8 +818,32 @@ int decompress_file(const char *in_path, const char *out_path) {
   int Xp = rotated ? H : W, Yp = rotated ? D : H, Zp = rotated ? W : D;
   if (!two_d) inverse3d(v, Xp, Yp, Zp, sx, sy, sz, p.wavelet_algorithm());
   else if (any) transform2d(v, Xp, Yp, Zp, sx, sy, p.wavelet_algorithm(), true);
-  int ox = p.original_width(), oy = p.original_height(), oz = p.original_depth();
-  int odt = p.has_original_data_type() ? p.original_data_type() : ORC_FLOAT32;
+  R.v.swap(v);
+  R.Xp = Xp; R.Yp = Yp; R.Zp = Zp;
+  R.ox = p.original_width(); R.oy = p.original_height(); R.oz = p.original_depth();
+  R.odt = p.has_original_data_type() ? p.original_data_type() : ORC_FLOAT32;
+  return 0;
+}
+
+const ReadCube *first_compressed(const std::vector<ReadCube> &cubes) {
+  for (auto &c : cubes)
+    if (c.meta.data_type() == CubeletBuffer_DataType_INT32 &&
+        c.meta.compression_algorithm() == CubeletBuffer_CompressionAlgorithm_WAVELET)
+      return &c;
+  return nullptr;
+}
+
+// Decompress the first compressed INT32 cubelet of in_path to out_path
+// (decompressFile, test_compress_cpu.cc:187-241).
+int decompress_file(const char *in_path, const char *out_path) {
+  std::vector<ReadCube> cubes;
+  if (!read_cube_file(in_path, cubes)) return 1;
+  const ReadCube *rc = first_compressed(cubes);
+  if (!rc) return 1;
+  Restored R;
+  if (restore_floats(rc, R)) return 1;
+  const std::vector<float> &v = R.v;
+  const int Xp = R.Xp, Yp = R.Yp, ox = R.ox, oy = R.oy, oz = R.oz, odt = R.odt;
   // translateCubeDataToOriginal (test_compress_common.cc:699-746), cropped to
   // the original size when written
   std::string out;
@@ -849,9 +870,102 @@ int decompress_file(const char *in_path, const char *out_path) {
   return write_cube_file(out_path, {m}, {out}, true) ? 0 : 1;
 }
 
+// ErrorAccumulator (test_compress_common.h:90-160): sums in double of float
+// values, products and differences.
+struct ErrAcc {
+  double sumValue = 0, sumValueSquared = 0, sumDiff = 0, sumDiffSquared = 0;
+  float maxValue = 0;
+  long long count = 0;
+  void add(float a, float b) {
+    sumValue += a;
+    sumValueSquared += a * a;
+    float diff = fabsf(a - b);
+    sumDiff += diff;
+    sumDiffSquared += diff * diff;
+    count++;
+  }
+};
+
+// computeErrorRatesAfterDequant (test_compress_common.cc:616-694): the
+// original cubelet against the restored floats, converted the way the
+// reference compares each type.  Returns false (nothing accumulated) when no
+// maximum possible value is known for a non-8-bit input.
+bool error_rates(const ReadCube &orig, const Restored &R, ErrAcc &acc) {
+  const int dt = orig.meta.data_type();
+  const int maxPossible = orig.meta.has_maximum_value() ? orig.meta.maximum_value() : 0;
+  if (dt == ORC_UINT8) acc.maxValue = maxPossible > 0 ? (float)maxPossible : 255.f;
+  else if (maxPossible > 0) acc.maxValue = (float)maxPossible;
+  else return false;
+  const int W = orig.meta.width(), H = orig.meta.height(), D = orig.meta.depth();
+  for (int z = 0; z < D; z++)
+    for (int y = 0; y < H; y++) {
+      const float *row = R.v.data() + ((size_t)z * R.Yp + y) * R.Xp;
+      const size_t o = ((size_t)z * H + y) * W;
+      for (int x = 0; x < W; x++) {
+        if (dt == ORC_UINT8) {
+          const float f = row[x];
+          unsigned char b = f <= 0 ? 0 : (f >= 255 ? 255 : (unsigned char)f);
+          acc.add((unsigned char)orig.data[o + x], b);
+        } else if (dt == ORC_INT32) {
+          int32_t a;
+          memcpy(&a, orig.data.data() + 4 * (o + x), 4);
+          acc.add((float)a, (float)(int)(row[x] + 0.5f));
+        } else {
+          float a;
+          memcpy(&a, orig.data.data() + 4 * (o + x), 4);
+          acc.add(a, (float)(int)row[x]);
+        }
+      }
+    }
+  return true;
+}
+
+const ReadCube *first_uncompressed(const std::vector<ReadCube> &cubes) {
+  for (auto &c : cubes)
+    if (c.meta.compression_algorithm() != CubeletBuffer_CompressionAlgorithm_WAVELET) return &c;
+  return nullptr;
+}
+
+// The getters of ErrorAccumulator: average, L1, L2, MSE, PSNR, relative.
+void err_getters(const ErrAcc &e, float g[6]) {
+  g[0] = e.count ? (float)(e.sumDiff / e.count) : 0.f;
+  g[1] = (float)e.sumDiff;
+  g[2] = (float)sqrt(e.sumDiffSquared);
+  g[3] = e.count ? (float)(e.sumDiffSquared / e.count) : 0.f;
+  const float mse = g[3];
+  g[4] = (e.maxValue == 0 || mse == 0) ? 0.f : (float)(10 * log10(e.maxValue * e.maxValue / mse));
+  g[5] = e.sumValueSquared == 0 ? 0.f : (float)(e.sumDiffSquared / e.sumValueSquared);
+}
+
+int error_metrics_files(const char *orig_path, const char *comp_path, ErrAcc &acc,
+                        bool &computed) {
+  std::vector<ReadCube> oc, cc;
+  if (!read_cube_file(orig_path, oc) || !read_cube_file(comp_path, cc)) return 1;
+  const ReadCube *o = first_uncompressed(oc), *c = first_compressed(cc);
+  if (!o || !c) return 1;
+  Restored R;
+  if (restore_floats(c, R)) return 1;
+  computed = error_rates(*o, R, acc);
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+int orc_error_metrics(const char *orig_path, const char *comp_path, double sums[4],
+                      long long *count, float getters[6]) {
+  ErrAcc acc;
+  bool computed = false;
+  if (error_metrics_files(orig_path, comp_path, acc, computed)) return 1;
+  sums[0] = acc.sumValue;
+  sums[1] = acc.sumValueSquared;
+  sums[2] = acc.sumDiff;
+  sums[3] = acc.sumDiffSquared;
+  *count = acc.count;
+  err_getters(acc, getters);
+  return 0;
+}
 
 int orc_forward(const float *in, int X, int Y, int Z, int sx, int sy, int sz,
                 int wavelet, float *out) {
@@ -1010,7 +1124,7 @@ int orc_compress_volume(const void *data, int dtype, int X, int Y, int Z,
 // test_compress_common.cc:73-192): -d -steps -thresh -qcount -wave -qalg
 // -noz -2d -q (other reference flags are accepted and ignored).
 int orc_main(int argc, const char **argv) {
-  bool decompress = false, zeros = true, two_d = false;
+  bool decompress = false, zeros = true, two_d = false, errors = false;
   int sx = -1, sy = -1, sz = -1, bins = 256, wave = ORC_CDF97, qalg = ORC_LOG;
   float frac = 0.5f;
   int i = 1;
@@ -1019,7 +1133,8 @@ int orc_main(int argc, const char **argv) {
     if (a == "-d") decompress = true;
     else if (a == "-noz") zeros = false;
     else if (a == "-2d") two_d = true;
-    else if (a == "-q" || a == "-v" || a == "-err" || a == "-pb" || a == "-enc") {}
+    else if (a == "-err") errors = true;
+    else if (a == "-q" || a == "-v" || a == "-pb" || a == "-enc") {}
     else if (i + 1 < argc && a == "-steps") {
       int x = 1, y = 1, z = 1;
       int k = sscanf(argv[++i], "%d,%d,%d", &x, &y, &z);
@@ -1054,9 +1169,22 @@ int orc_main(int argc, const char **argv) {
   for (auto &c : cubes) {
     if (c.meta.compression_algorithm() == CubeletBuffer_CompressionAlgorithm_WAVELET) continue;
     int dt = c.meta.data_type();
-    return compress_common(c.data.data(), dt, c.meta.width(), c.meta.height(),
-                           c.meta.depth(), sx, sy, sz, wave, frac, bins, qalg,
-                           zeros, out, nullptr, two_d);
+    int rc = compress_common(c.data.data(), dt, c.meta.width(), c.meta.height(),
+                             c.meta.depth(), sx, sy, sz, wave, frac, bins, qalg,
+                             zeros, out, nullptr, two_d);
+    if (rc == 0 && errors) {
+      // computeErrorRates after quantizing (test_compress_cpu.cc:150-157)
+      ErrAcc acc;
+      bool computed = false;
+      if (error_metrics_files(in, out, acc, computed)) return 1;
+      if (!computed)
+        fprintf(stderr, "Cannot compute error rates: no maximum possible input value set.\n");
+      float g[6];
+      err_getters(acc, g);
+      printf("Mean squared error: %.3f, relative error: %g, peak SNR: %.3f\n", g[3], g[5], g[4]);
+      fflush(stdout);
+    }
+    return rc;
   }
   return 1;
 }

@@ -37,6 +37,16 @@ typedef struct {
   int dup_key, dup_value;            /* -1 when unused */
 } orc_result;
 
+/* Error metrics of the first compressed cubelet of comp_path against the
+ * first uncompressed cubelet of orig_path (computeErrorRates,
+ * test_compress_common.cc:587-694; ErrorAccumulator,
+ * test_compress_common.h:90-160): sums = {sum a, sum a*a, sum |a-b|,
+ * sum |a-b|^2}, getters = {average, L1, L2, MSE, PSNR, relative error}.
+ * count = 0 when no maximum possible value is known (non-8-bit input without
+ * maximum_value).  Returns 0 on success. */
+int orc_error_metrics(const char *orig_path, const char *comp_path, double sums[4],
+                      long long *count, float getters[6]);
+
 /* Run the reference's command line (test_compress_cpu.cc:37-65) in-process:
  * same flags, same .cube output.  Returns 0 on success. */
 int orc_main(int argc, const char **argv);

@@ -11,8 +11,11 @@ the reference.
 Writes, per case: ``<case>.in.cube`` (input), ``<case>.<p>.cube`` (reference
 compressed output), ``<case>.<p>.d.cube`` (reference decompression of it),
 ``<case>.<p>.coeffs.f32`` (reference transform output, rotated Z-X-Y order),
-``<case>.<o>.opt.txt`` (the table the reference's -opt sweep prints) and
-``manifest.json`` (flags, sizes, threshold statistics, hashes).
+``<case>.<o>.opt.txt`` (the table the reference's -opt sweep prints),
+``<case>.<p>.err.txt`` (the error line the reference's -err prints; float
+inputs also from a copy ``<case>.max1.in.cube`` whose maximum_value is 1) and
+``manifest.json`` (flags, sizes, threshold statistics, hashes).  ``--err``
+regenerates only the -err fixtures.
 """
 import hashlib
 import json
@@ -91,7 +94,54 @@ def kat_cdf97(ref_dump, tmp):
     return np.fromfile(os.path.join(d, "coeffs.f32"), np.float32)
 
 
+# -err fixtures: the reference's printed error line for these (case, params)
+# pairs; float32 inputs also as a copy whose maximum_value is set to 1 (the
+# reference computes nothing for float input without one)
+ERR_CASES = [("uint8_1x64x64", "p1"), ("uint8_1x64x64", "p3"), ("uint8_2x33x17", "p3"),
+             ("uint8_5x7x9", "p1"), ("uint8_1x256x256", "p4"), ("uint16_16x16x16", "p2"),
+             ("uint16_16x16x16", "p7"), ("float32_8x16x32", "p1"), ("float32_8x16x32", "p4"),
+             ("float32_12x20x24", "p2"), ("float32_3x2x5", "p5")]
+
+
+def make_err(cli, manifest):
+    """Run the reference with -err on ERR_CASES; write <case>.<p>.err.txt
+    (its stdout) and manifest["err"]."""
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, p in ERR_CASES:
+            inputs = [(name + ".in.cube", "")]
+            if name.startswith("float32"):
+                c = cubefile.read_file(os.path.join(HERE, name + ".in.cube"))[0]
+                m1 = name + ".max1.in.cube"
+                cubefile.write_file(os.path.join(HERE, m1),
+                                    [cubefile.from_array(c.array(), maximum_value=1)])
+                inputs.append((m1, ".max1"))
+            for inp, tag in inputs:
+                txt = f"{name}{tag}.{p}.err.txt"
+                r = subprocess.run([cli, "-q", "-err", *PARAMS[p], os.path.join(HERE, inp),
+                                    os.path.join(tmp, "x.cube")],
+                                   capture_output=True, text=True, check=True)
+                line = [ln for ln in r.stdout.splitlines() if ln.startswith("Mean squared")]
+                with open(os.path.join(HERE, txt), "w") as f:
+                    f.write("\n".join(line) + "\n")
+                out.append({"case": name, "params": p, "input": inp, "err": txt})
+    manifest["err"] = out
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--err":
+        # only the -err fixtures, added to the existing manifest
+        ref = sys.argv[2] if len(sys.argv) > 2 else build_oracle.reference_dir()
+        if not ref or not os.path.isdir(ref):
+            sys.exit("reference checkout not found: pass its path or set WL_REFERENCE_DIR")
+        build_oracle.build_reference(ref)
+        mpath = os.path.join(HERE, "manifest.json")
+        manifest = json.load(open(mpath))
+        make_err(os.path.join(ROOT, "oracle", "_ref", "test_compress_cpu"), manifest)
+        with open(mpath, "w") as f:
+            json.dump(manifest, f, indent=1)
+        print("wrote", len(manifest["err"]), "-err fixtures")
+        return
     ref = sys.argv[1] if len(sys.argv) > 1 else build_oracle.reference_dir()
     if not ref or not os.path.isdir(ref):
         sys.exit("reference checkout not found: pass its path or set WL_REFERENCE_DIR")
@@ -150,6 +200,7 @@ def main():
                 manifest["opt"]["cases"].append({"case": name, "params": o,
                                                  "input": os.path.basename(inp),
                                                  "table": os.path.basename(txt)})
+        make_err(cli, manifest)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     print("wrote", len(manifest["cases"]), "cases")

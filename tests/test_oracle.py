@@ -108,3 +108,24 @@ def test_float64_lifting_agrees_with_reference_coefficients(case):
         assert np.abs(ref).max() == 0
         return
     assert float(np.abs(got - ref).max()) / scale <= 2e-6
+
+
+ERR = MANIFEST.get("err", [])
+
+
+@pytest.mark.parametrize("e", ERR, ids=[f"{e['input']}.{e['params']}" for e in ERR])
+def test_oracle_err_line_matches_reference(e, tmp_path):
+    """-err: the error line the reference printed (computeErrorRates,
+    test_compress_common.cc:587-694, printed at test_compress_cpu.cc:155-156),
+    reproduced character for character by the oracle's command line."""
+    args = MANIFEST["params"][e["params"]]
+    r = subprocess.run([oracle.cli_path(), "-q", "-err", *args,
+                        os.path.join(GOLDEN, e["input"]), str(tmp_path / "o.cube")],
+                       capture_output=True, text=True, check=True)
+    got = [ln for ln in r.stdout.splitlines() if ln.startswith("Mean squared")]
+    want = open(os.path.join(GOLDEN, e["err"])).read().split("\n")[0]
+    assert got == [want]
+    # the library-level numbers print to the same line
+    m = oracle.error_metrics(os.path.join(GOLDEN, e["input"]), str(tmp_path / "o.cube"))
+    assert "Mean squared error: %.3f, relative error: %g, peak SNR: %.3f" % (
+        np.float32(m["mse"]), np.float32(m["relative_error"]), np.float32(m["psnr"])) == want

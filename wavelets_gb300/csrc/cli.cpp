@@ -4,10 +4,11 @@
 //
 // Flags and defaults follow parseOptions / printHelp
 // (test_compress_common.cc:35-192): -d, -steps, -thresh, -qcount, -wave,
-// -qalg, -noz, -2d, -opt, -q, -v; -exact selects the reference float order
-// for the CDF 9/7 transform (bit-identical output files).  Flags of the
-// reference that only print diagnostics (-err, -pb, -enc, -bq, -aq) are
-// rejected with a message rather than silently ignored.
+// -qalg, -noz, -2d, -opt, -err, -q, -v; -exact selects the reference float
+// order for the CDF 9/7 transform (bit-identical output files).  -err prints
+// the reference's error line after compressing (test_compress_cpu.cc:150-157).
+// Flags of the reference that only print diagnostics (-pb, -enc, -bq, -aq)
+// are rejected with a message rather than silently ignored.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -30,6 +31,7 @@ static void help() {
           "    -noz : disable compression of long strings of zeros\n"
           "    -2d : rather than 3d transform, do 2d transform at each layer\n"
           "    -opt : print the threshold / bin count sweep (8-bit input; no output)\n"
+          "    -err : compute error metrics\n"
           "    -exact : CDF9/7 in the reference's float order\n"
           "    -q : be quiet\n\n");
   exit(1);
@@ -38,7 +40,7 @@ static void help() {
 int main(int argc, char **argv) {
   wl_params p;
   wl_params_default(&p);
-  bool decompress = false, quiet = false, optimize = false;
+  bool decompress = false, quiet = false, optimize = false, errors = false;
   int i = 1;
   for (; i < argc && argv[i][0] == '-'; i++) {
     const char *a = argv[i];
@@ -53,6 +55,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(a, "-exact")) p.exact_transform = 1;
     else if (!strcmp(a, "-2d")) p.transform_2d = 1;
     else if (!strcmp(a, "-opt")) optimize = true;
+    else if (!strcmp(a, "-err")) errors = true;
     else if (!strcmp(a, "-steps")) {
       const char *v = need();
       int x = 1, y = 1, z = 1;
@@ -124,6 +127,20 @@ int main(int argc, char **argv) {
     fprintf(stderr, "error: %s\n", wl_last_error(ctx));
     wl_destroy(ctx);
     return 1;
+  }
+  if (errors && !decompress) {
+    // computeErrorRates after quantizing (test_compress_cpu.cc:150-157)
+    wl_error_stats es;
+    st = wl_error_metrics_file(ctx, argv[i], argv[i + 1], &es);
+    if (st != WL_OK) {
+      fprintf(stderr, "error: %s\n", wl_last_error(ctx));
+      wl_destroy(ctx);
+      return 1;
+    }
+    if (es.count == 0)
+      fprintf(stderr, "Cannot compute error rates: no maximum possible input value set.\n");
+    printf("Mean squared error: %.3f, relative error: %g, peak SNR: %.3f\n", es.mse,
+           es.relative_error, es.psnr);
   }
   if (!quiet) {
     printf("Total: %.2f ms\n", std::chrono::duration<double, std::milli>(t1 - t0).count());

@@ -210,7 +210,8 @@ struct wl_ctx {
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
       hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
-      words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr;
+      words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr,
+      errIn, errRest, errPart;
   HostBuf hState, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
   HostBuf hStage[2];  // staging buffers of the container pipeline
   // CUDA graphs: 0 = off, 1 = capture a batch geometry seen twice in a row
@@ -235,6 +236,8 @@ struct wl_ctx {
   cudaEvent_t pev[10] = {};
   float ktimes[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int launches = 0;
+  size_t devBytes = 0;     // device workspace held (grow-only buffers)
+  size_t memLimit = 0;     // wl_set_memory_limit (0: none)
 };
 
 namespace {
@@ -259,17 +262,28 @@ wl_status fail(wl_ctx *c, wl_status s, const char *fmt, ...) {
 wl_status ensure(wl_ctx *ctx, DevBuf &b, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (b.cap >= bytes) return WL_OK;
+  size_t want = bytes + bytes / 4;
+  if (ctx->memLimit) {
+    // the context's workspace cap: grow to what is needed, no slack, and
+    // fail before freeing anything
+    const size_t others = ctx->devBytes - b.cap;
+    if (others + bytes > ctx->memLimit)
+      return fail(ctx, WL_ENOMEM, "device workspace limit of %zu bytes reached (%zu held, %zu "
+                  "more needed)", ctx->memLimit, ctx->devBytes, bytes - b.cap);
+    if (others + want > ctx->memLimit) want = bytes;
+  }
   if (b.p) cudaFree(b.p);
+  ctx->devBytes -= b.cap;
   b.p = nullptr;
   b.cap = 0;
   ctx->gen++;
-  size_t want = bytes + bytes / 4;
   cudaError_t e = cudaMalloc(&b.p, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(ctx, WL_ENOMEM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
   }
   b.cap = want;
+  ctx->devBytes += want;
   return WL_OK;
 }
 
@@ -1480,6 +1494,62 @@ wl_status decompress_impl(wl_ctx *ctx, const wl_result *r, int outType, void *ou
                       outOnDevice, r->transform_2d != 0);
 }
 
+// ---- error metrics (-err) ----------------------------------------------------------
+// computeErrorRatesAfterDequant (test_compress_common.cc:616-694) with
+// ErrorAccumulator (test_compress_common.h:90-160): the cubelet restored to
+// floats on the device (the reference dequantizes its bins, which the
+// lossless Huffman stream gives back exactly, and runs the inverse
+// transform), compared there, the per-CTA sums added here in CTA order.
+wl_status error_impl(wl_ctx *ctx, const wl_result *r, const void *orig, int odt, int origOnDevice,
+                     float maxPossible, wl_error_stats *out) {
+  if (!out) return fail(ctx, WL_EINVAL, "null argument");
+  memset(out, 0, sizeof *out);
+  if (!r || !orig) return fail(ctx, WL_EINVAL, "null argument");
+  if (dtype_size(odt) == 0) return fail(ctx, WL_EINVAL, "bad original dtype %d", odt);
+  if (odt == WL_U8 && !(maxPossible > 0)) maxPossible = 255.f;
+  if (!(maxPossible > 0)) return WL_OK;  // nothing computed, like the reference
+  const long long n = (long long)r->original_size[0] * r->original_size[1] * r->original_size[2];
+  if (n <= 0) return fail(ctx, WL_EINVAL, "empty cubelet");
+  const int blocks = err_sums_blocks(n);
+  TRY(ensure(ctx, ctx->errRest, (size_t)n * 4));
+  TRY(ensure(ctx, ctx->errPart, (size_t)blocks * 4 * sizeof(double)));
+  TRY(decompress_impl(ctx, r, WL_F32, ctx->errRest.p, 1));
+  cudaStream_t s = ctx->stream;
+  const void *dOrig = orig;
+  if (!origOnDevice) {
+    TRY(ensure(ctx, ctx->errIn, (size_t)n * dtype_size(odt)));
+    CU(cudaMemcpyAsync(ctx->errIn.p, orig, (size_t)n * dtype_size(odt), cudaMemcpyHostToDevice, s));
+    dOrig = ctx->errIn.p;
+  }
+  launch_err_sums(dOrig, odt, P<float>(ctx->errRest), n, P<double>(ctx->errPart), blocks, s);
+  CU(cudaGetLastError());
+  std::vector<double> part((size_t)blocks * 4);
+  CU(cudaMemcpyAsync(part.data(), ctx->errPart.p, part.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  double sv = 0, svv = 0, sd = 0, sdd = 0;
+  for (int b = 0; b < blocks; b++) {
+    sv += part[4 * b];
+    svv += part[4 * b + 1];
+    sd += part[4 * b + 2];
+    sdd += part[4 * b + 3];
+  }
+  out->count = n;
+  out->sum_value = sv;
+  out->sum_value_squared = svv;
+  out->sum_diff = sd;
+  out->sum_diff_squared = sdd;
+  // the reference's getters (float results)
+  out->average_error = (float)(sd / n);
+  out->l1 = (float)sd;
+  out->l2 = (float)sqrt(sdd);
+  out->mse = (float)(sdd / n);
+  const float peak2 = maxPossible * maxPossible;
+  out->psnr = out->mse == 0.f ? 0.f : (float)(10.0 * log10((double)(peak2 / out->mse)));
+  out->relative_error = svv == 0 ? 0.f : (float)(sdd / svv);
+  return WL_OK;
+}
+
 // ---- tile autotuner -------------------------------------------------------------
 // For every size class of the column-tile transform -- pass (forward x / y / z,
 // inverse z / y / x), element type of its global side, row-length class 2^k --
@@ -2053,6 +2123,48 @@ wl_status wl_compress_file(wl_ctx *ctx, const char *inPath, const char *outPath,
   return fail(ctx, WL_EFORMAT, "No uncompressed cubelets in the input data.");
 }
 
+wl_status wl_error_metrics(wl_ctx *ctx, const wl_result *compressed, const void *original,
+                           int original_dtype, int original_on_device, float max_possible,
+                           wl_error_stats *out) {
+  if (!ctx) return WL_EINVAL;
+  CU(cudaSetDevice(ctx->device));
+  return error_impl(ctx, compressed, original, original_dtype, original_on_device, max_possible,
+                    out);
+}
+
+wl_status wl_error_metrics_file(wl_ctx *ctx, const char *origPath, const char *compPath,
+                                wl_error_stats *out) {
+  if (!ctx || !origPath || !compPath || !out) return fail(ctx, WL_EINVAL, "null argument");
+  std::string ob, cb, err;
+  if (!read_whole_file(origPath, ob)) return fail(ctx, WL_EIO, "cannot read %s", origPath);
+  if (!read_whole_file(compPath, cb)) return fail(ctx, WL_EIO, "cannot read %s", compPath);
+  std::vector<CubeMeta> om, cm;
+  std::vector<std::string> od, cd;
+  if (!decode_file(ob, om, od, err)) return fail(ctx, WL_EFORMAT, "%s: %s", origPath, err.c_str());
+  if (!decode_file(cb, cm, cd, err)) return fail(ctx, WL_EFORMAT, "%s: %s", compPath, err.c_str());
+  int oi = -1, ci = -1;
+  for (size_t i = 0; i < om.size() && oi < 0; i++)
+    if (!om[i].compressed) oi = (int)i;
+  for (size_t i = 0; i < cm.size() && ci < 0; i++)
+    if (cm[i].compressed) ci = (int)i;
+  if (oi < 0) return fail(ctx, WL_EFORMAT, "No uncompressed cubelets in %s", origPath);
+  if (ci < 0) return fail(ctx, WL_EFORMAT, "No compressed cubelets in %s", compPath);
+  const CubeMeta &m = om[oi];
+  const int dt = m.data_type == kPbUint8 ? WL_U8 : m.data_type == kPbInt32 ? WL_I32
+                 : m.data_type == kPbFloat32 ? WL_F32 : 0;
+  if (!dt) return fail(ctx, WL_EFORMAT, "unknown data type %d", m.data_type);
+  if (od[oi].size() < (size_t)m.width * m.height * m.depth * dtype_size(dt))
+    return fail(ctx, WL_EFORMAT, "cubelet data truncated");
+  wl_result r;
+  meta_to_result(cm[ci], cd[ci], r);
+  if (r.original_size[0] != m.width || r.original_size[1] != m.height ||
+      r.original_size[2] != m.depth)
+    return fail(ctx, WL_EINVAL, "the compressed cubelet is %dx%dx%d, the original %dx%dx%d",
+                r.original_size[0], r.original_size[1], r.original_size[2], m.width, m.height,
+                m.depth);
+  return wl_error_metrics(ctx, &r, od[oi].data(), dt, 0, (float)m.maximum_value, out);
+}
+
 wl_status wl_optimize_file(wl_ctx *ctx, const char *inPath, const wl_params *params,
                            wl_opt_point *points, int cap, int *n_points) {
   if (!ctx || !inPath || !params) return fail(ctx, WL_EINVAL, "null argument");
@@ -2085,6 +2197,9 @@ wl_status wl_decompress_file(wl_ctx *ctx, const char *inPath, const char *outPat
   for (size_t i = 0; i < metas.size(); i++) {
     CubeMeta &m = metas[i];
     if (!m.compressed || m.data_type != kPbInt32) continue;
+    if (datas[i].size() % 4)
+      return fail(ctx, WL_EFORMAT, "compressed data of %zu bytes is not a whole number of "
+                  "32-bit words", datas[i].size());
     wl_result r;
     meta_to_result(m, datas[i], r);
     const int odt = r.original_dtype;
@@ -2150,6 +2265,14 @@ wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps) {
   if (reps > 64) reps = 64;
   return autotune_impl(ctx, max_len, reps);
 }
+
+wl_status wl_set_memory_limit(wl_ctx *ctx, size_t bytes) {
+  if (!ctx) return WL_EINVAL;
+  ctx->memLimit = bytes;
+  return WL_OK;
+}
+
+size_t wl_memory_held(const wl_ctx *ctx) { return ctx ? ctx->devBytes : 0; }
 
 wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode) {
   if (!ctx || mode < 0 || mode > 1) return WL_EINVAL;

@@ -278,6 +278,12 @@ void launch_quantize(DevBatch &b, const float *coef, int maxTable, int maxSymbol
                      cudaStream_t s);
 void launch_runs(DevBatch &b, cudaStream_t s);
 
+// error metrics (errors.cu): per-CTA double sums {a, a*a, |d|, d*d} of the
+// original (dtype) against the restored floats, blocks = err_sums_blocks(n)
+int err_sums_blocks(long long n);
+void launch_err_sums(const void *orig, int dtype, const float *rest, long long n, double *part,
+                     int blocks, cudaStream_t s);
+
 // launchers (huffman.cu)
 void launch_huffman_build(DevBatch &b, int maxSymbols, cudaStream_t s);
 void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s);

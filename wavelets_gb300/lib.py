@@ -88,6 +88,17 @@ class WlOptPoint(ctypes.Structure):
                 ("size_bytes", ctypes.c_int), ("psnr", ctypes.c_float)]
 
 
+class WlErrorStats(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_longlong), ("average_error", ctypes.c_float),
+                ("l1", ctypes.c_float), ("l2", ctypes.c_float), ("mse", ctypes.c_float),
+                ("psnr", ctypes.c_float), ("relative_error", ctypes.c_float),
+                ("sum_value", ctypes.c_double), ("sum_value_squared", ctypes.c_double),
+                ("sum_diff", ctypes.c_double), ("sum_diff_squared", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class WlRequestInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("queue_ms", ctypes.c_double),
                 ("service_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
@@ -176,6 +187,13 @@ EXPORTS = {
     "wl_set_graph_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "wl_graph_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "wl_graph_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "wl_error_metrics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlResult),
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_float, ctypes.POINTER(WlErrorStats)]),
+    "wl_set_memory_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
+    "wl_memory_held": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "wl_error_metrics_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                             ctypes.POINTER(WlErrorStats)]),
 }
 
 _lib = None
@@ -635,6 +653,24 @@ class Context:
         self._check(st)
         return out
 
+    def error_metrics(self, c: Compressed, original: np.ndarray, max_possible: float = 0.0):
+        """The reference's -err metrics of a compressed cubelet against its
+        original array (wl_error_metrics)."""
+        a = np.ascontiguousarray(original)
+        st = WlErrorStats()
+        r = c.to_struct()
+        self._check(self.lib.wl_error_metrics(self.h, ctypes.byref(r),
+                                              ctypes.c_void_p(a.ctypes.data),
+                                              NP_TO_WL[a.dtype], 0, ctypes.c_float(max_possible),
+                                              ctypes.byref(st)))
+        return st.as_dict()
+
+    def error_metrics_file(self, original_path: str, compressed_path: str):
+        st = WlErrorStats()
+        self._check(self.lib.wl_error_metrics_file(self.h, original_path.encode(),
+                                                   compressed_path.encode(), ctypes.byref(st)))
+        return st.as_dict()
+
     def compress_file(self, inp: str, out: str, params: Optional[P.Params] = None):
         self._check(self.lib.wl_compress_file(self.h, inp.encode(), out.encode(),
                                               ctypes.byref(make_params(params))))
@@ -708,6 +744,13 @@ class Context:
         """0: read page-locked host inputs in place; 1: copy them with the
         copy engine first."""
         self._check(self.lib.wl_set_host_input_mode(self.h, int(mode)))
+
+    def set_memory_limit(self, nbytes: int):
+        """Cap the context's device workspace (0: no cap); see wl_set_memory_limit."""
+        self._check(self.lib.wl_set_memory_limit(self.h, nbytes))
+
+    def memory_held(self) -> int:
+        return self.lib.wl_memory_held(self.h)
 
     def set_graph_mode(self, mode: int):
         """1: capture a batch geometry seen twice in a row as a CUDA graph
