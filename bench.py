@@ -306,7 +306,12 @@ def run_reference(args, items, desc, rank, world):
 
 
 # ------------------------------------------------------------------ serving
-def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=2, budget=16 << 30, device=0):
+SERVE_CLASSES = ((0, 1 << 20, "<=1MiB"), (1 << 20, 8 << 20, "1-8MiB"),
+                 (8 << 20, 32 << 20, "8-32MiB"), (32 << 20, 1 << 62, ">32MiB"))
+
+
+def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30, device=0,
+              express_lanes=1, small_bytes=4 << 20, max_batch_bytes=32 << 20):
     """Poisson stream of requests (80% compress, 20% decompress) against the
     library's serving loop: payloads with axes log-uniform in 16..512 (at most
     256 MiB each), uint8/uint16/float32 in equal parts, CDF 9/7 with 3 steps
@@ -340,12 +345,15 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=2, budget=16 << 30
     times = np.sort(rng.uniform(0.0, seconds, n))
     is_comp = rng.uniform(size=n) < 0.8
     which = rng.integers(0, 1 << 30, n)
-    srv = lib.Server(lanes=lanes, memory_budget=budget)
+    srv = lib.Server(lanes=lanes, memory_budget=budget, device=device,
+                     express_lanes=express_lanes, small_request_bytes=small_bytes,
+                     max_batch_bytes=max_batch_bytes)
     # warm the lanes' buffers with one request of every payload
     for ptr, dt, size, _ in reqs:
         srv.wait(srv.submit_compress(ptr=ptr, dtype=dt, size=size, params=prm))
     q = queue.Queue()
     lat = {"compress": [], "decompress": []}
+    by_class = {name: [] for _, _, name in SERVE_CLASSES}
     done_bytes = [0]
     t_last = [0.0]
     errors = []
@@ -362,6 +370,10 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=2, budget=16 << 30
                 errors.append(str(e))
                 continue
             lat[kind].append(info["total_ms"])
+            for lo, hi, name in SERVE_CLASSES:
+                if lo < nbytes <= hi or (lo == 0 and nbytes <= hi):
+                    by_class[name].append(info["total_ms"])
+                    break
             done_bytes[0] += nbytes
             t_last[0] = time.perf_counter()
 
@@ -389,13 +401,126 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=2, budget=16 << 30
         return float(np.percentile(v, p_)) if len(v) else None
 
     return {"requests": n, "failed": len(errors), "seconds": seconds, "rate_per_s": rate,
-            "lanes": lanes, "memory_budget_gib": budget / (1 << 30),
+            "lanes": lanes, "express_lanes": express_lanes,
+            "small_request_mib": small_bytes / (1 << 20),
+            "max_batch_mib": max_batch_bytes / (1 << 20),
+            "memory_budget_gib": budget / (1 << 30),
+            "by_size": {name: {"requests": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)}
+                        for name, v in by_class.items()},
             "value": done_bytes[0] / elapsed / 1e9, "unit": "GB/s",
             "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
             "compress_p50_ms": pct(lat["compress"], 50), "compress_p99_ms": pct(lat["compress"], 99),
             "decompress_p50_ms": pct(lat["decompress"], 50),
             "decompress_p99_ms": pct(lat["decompress"], 99),
             "mean_request_mb": float(np.mean([r[3] for r in reqs]) / 1e6)}
+
+
+# ------------------------------------------------------------------ other workloads
+def workload_line(lib, ctx, name, steps, warmup, hbm):
+    """One of the single-GPU workloads besides the mixed batch, measured like
+    the headline: value = input bytes / device time of one batched call with
+    the inputs resident in HBM (CUDA events on the library's stream); e2e =
+    the same call reading page-locked host inputs in place, its compressed
+    output copied back, wall clock; the round-trip PSNR of the restored
+    data."""
+    gen, desc = WORKLOADS[name]
+    items = gen(20261205, 0)
+    vol = getattr(gen, "volume", None)
+    if vol is not None:  # split volume: cubelets read in place through pitches
+        Zv, Yv, Xv = vol.shape
+        es = vol.dtype.itemsize
+        in_bytes = vol.nbytes
+        dev = lib.DeviceBuffer(vol.nbytes)
+        dev.upload(vol)
+        pin = lib.PinnedBuffer(vol.nbytes)
+        pin.array(vol.dtype, vol.shape)[...] = vol
+        offs = [(ox + Xv * (oy + Yv * oz)) * es for (ox, oy, oz), _ in gen.grid]
+        pitch = (Xv, Xv * Yv)
+        dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p, pitch)
+                     for (a, p), o in zip(items, offs)]
+        host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p, pitch)
+                      for (a, p), o in zip(items, offs)]
+    else:
+        in_bytes = sum(a.nbytes for a, _ in items)
+        offs, off = [], 0
+        for a, _ in items:
+            offs.append(off)
+            off += (a.nbytes + 255) // 256 * 256
+        dev = lib.DeviceBuffer(off)
+        pin = lib.PinnedBuffer(off)
+        for (a, _), o in zip(items, offs):
+            dev.upload(a, o)
+            pin.array(np.uint8, (off,))[o:o + a.nbytes] = a.view(np.uint8).ravel()
+        dev_items = [(dev.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                     for (a, p), o in zip(items, offs)]
+        host_items = [(pin.ptr + o, lib.NP_TO_WL[a.dtype], lib._size_of(a), p)
+                      for (a, p), o in zip(items, offs)]
+    pb_dev = ctx.prepare_batch(dev_items, on_device=True)
+    out = None
+    for _ in range(max(3, warmup)):
+        out = ctx.compress_prepared(pb_dev)
+    t = []
+    for _ in range(steps):
+        out = ctx.compress_prepared(pb_dev)
+        t.append(ctx.timings()[5])
+    dev_ms = statistics.mean(t)
+    comp_bytes = sum(c.compressed_bytes for c in out)
+    pb = ctx.prepare_batch(host_items, raw=True)
+    prev = None
+    for _ in range(3):
+        rb = ctx.compress_prepared(pb, lazy=True)
+        if prev is not None:
+            prev.release()
+        prev = rb
+    w = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        rb = ctx.compress_prepared(pb, lazy=True)
+        w.append(time.perf_counter() - t0)
+        prev.release()
+        prev = rb
+    outh = prev.results()
+    same = all(np.array_equal(a.words, b.words) for a, b in zip(out, outh))
+    d2h = sum(c.compressed_bytes + c.decode.nbytes + c.boundaries.nbytes + c.values.nbytes
+              for c in outh)
+    del outh, prev, rb
+    e2e_ms = statistics.mean(w) * 1e3
+    # round-trip PSNR
+    if vol is not None:
+        # every cubelet restored as 16-bit data (later cubelets overwrite the
+        # overlaps), the whole volume compared
+        back = np.zeros(vol.shape, vol.dtype)
+        rest = ctx.decompress_batch(out)
+        for ((ox, oy, oz), (sx, sy, sz)), r in zip(gen.grid, rest):
+            back[oz:oz + sz, oy:oy + sy, ox:ox + sx] = r
+        del rest
+        sq = 0.0
+        for z0 in range(0, vol.shape[0], 64):
+            d = back[z0:z0 + 64].astype(np.float64) - vol[z0:z0 + 64]
+            sq += float(np.sum(d * d))
+        mse, peak = sq / vol.size, 65535.0
+        del back
+    else:
+        a = items[0][0]
+        b = ctx.decompress(out[0]).astype(np.float64)
+        x = a.astype(np.float64)
+        peak = 255.0 if a.dtype == np.uint8 else float(x.max() - x.min())
+        mse = float(np.mean((b - x) ** 2))
+    psnr = 10 * np.log10(peak * peak / mse) if mse > 0 else 999.0
+    dev.free()
+    pin.free()
+    pipe = (in_bytes + comp_bytes) / (dev_ms / 1e3) / 1e9
+    return {"workload": desc, "cubelets": len(items), "input_bytes": in_bytes,
+            "compressed_bytes": comp_bytes, "steps": steps,
+            "value": in_bytes / (dev_ms / 1e3) / 1e9, "unit": UNIT, "ms_per_step": dev_ms,
+            "e2e": {"value": in_bytes / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
+                    "how": "one synchronous wl_compress_batch per step, page-locked inputs "
+                           "read in place, results copied to page-locked host memory",
+                    "identical_to_device_resident": bool(same)},
+            "pipeline_roofline": {"achieved": pipe, "peak": hbm, "unit": "GB/s",
+                                  "frac": pipe / hbm},
+            "psnr_db": float(psnr), "psnr_peak": peak}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -413,7 +538,10 @@ def main():
                     help="keep the default tile heights (profiling runs)")
     ap.add_argument("--no-stream", action="store_true",
                     help="skip the streamed two-lane end-to-end section (profiling runs)")
-    ap.add_argument("--serve-seconds", type=float, default=10.0,
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the other single-GPU workloads (2048^2 image, 256^3 volume, "
+                         "1024^3 split volume) in the default run")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the serving measurement (0: skip)")
     args = ap.parse_args()
 
@@ -744,6 +872,13 @@ def main():
                "best_psnr": {"fraction": round(best[0], 3), "bins": best[1],
                              "bytes": best[2], "psnr_db": best[3]}}
 
+    # ---- the other single-GPU workloads ----
+    workloads = None
+    if rank == 0 and args.workload == "mixed" and not args.no_workloads:
+        workloads = {}
+        for name in ("plain2d", "volume", "split1024"):
+            workloads[name] = workload_line(lib, ctx, name, max(3, min(args.steps, 20)),
+                                            args.warmup, hbm)
     # ---- serving: Poisson request stream, p50/p99 latency ----
     serving = None
     if rank == 0 and args.serve_seconds > 0 and args.workload == "mixed":
@@ -784,6 +919,7 @@ def main():
                                   "frac": pipe_gbs / hbm,
                                   "bytes": "input + compressed output per step"},
             "serving": serving,
+            "workloads": workloads,
             "opt_sweep": opt,
             "decompress": decomp,
             "autotune": {"ms": tune_ms, "classes": len(tune_rows),

@@ -209,10 +209,14 @@ wl_status wl_sync(wl_ctx *ctx);
  * No reference counterpart (the reference compresses one file per process).
  * A server runs a request loop over several lanes, each a context (stream and
  * buffers) driven by its own host thread: compress and decompress requests of
- * any size are admitted as they arrive, compress requests waiting together
- * are batched onto the next free lane (continuous batching), admission is
- * gated by a device working-memory budget, and batches on different lanes
- * overlap on the GPU.  Compress inputs may be device, page-locked or pageable
+ * any size are admitted as they arrive, requests of one kind waiting together
+ * are batched onto the next free lane (continuous batching), and batches on
+ * different lanes overlap on the GPU.  Admission counts the device memory
+ * every lane holds (its grow-only workspace, or the estimate of its running
+ * batch if larger) against the memory budget, and a batch that needs its lane
+ * to grow waits unless the device has that much memory free
+ * (cudaMemGetInfo); a request larger than the whole budget runs alone once
+ * nothing else is in flight.  Compress inputs may be device, page-locked or pageable
  * host pointers; they, and a decompress request's input and output, must stay
  * valid until the request is waited for. */
 enum { WL_REQ_COMPRESS = 1, WL_REQ_DECOMPRESS = 2 };
@@ -225,6 +229,13 @@ typedef struct {
                                with the copy engine (wl_set_host_input_mode 1),
                                so one lane's transfer overlaps another's
                                compute; 0: lanes read them in place */
+  size_t max_batch_bytes;   /* input (compress) or output (decompress) bytes of
+                               one batch; a larger request runs alone (0, the
+                               default: no cap) */
+  int express_lanes;        /* lanes that take only requests of at most
+                               small_request_bytes, so small requests never
+                               wait behind large ones (default 0) */
+  size_t small_request_bytes; /* the express lanes' limit (default 4 MiB) */
 } wl_serve_config;
 
 typedef struct {

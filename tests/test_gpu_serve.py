@@ -41,13 +41,21 @@ def _same(a, b):
             and np.array_equal(a.boundaries, b.boundaries))
 
 
-def test_served_results_equal_standalone(ctx):
+@pytest.mark.parametrize("cfg", [dict(lanes=3, memory_budget=1 << 30, max_batch=16),
+                                 dict(lanes=3, memory_budget=1 << 30, max_batch=64,
+                                      express_lanes=1, small_request_bytes=64 << 10,
+                                      max_batch_bytes=256 << 10)],
+                         ids=["fifo", "express+bytecap"])
+def test_served_results_equal_standalone(ctx, cfg):
+    """With or without an express lane for small requests and a byte cap per
+    batch (requests then complete out of submission order), every result is
+    the standalone one."""
     items = _mix(11, 48)
     ref = [ctx.compress(a, p) for a, p in items]
     dec_src = ref[:12]
     ref_dec = [ctx.decompress(c) for c in dec_src]
 
-    srv = lib.Server(lanes=3, memory_budget=1 << 30, max_batch=16)
+    srv = lib.Server(**cfg)
     tickets = [None] * (len(items) + len(dec_src))
     outs = [np.empty_like(r) for r in ref_dec]
 

@@ -2,13 +2,17 @@
 //
 // Each lane is an ordinary context (its own stream and grow-only buffers)
 // driven by its own host thread, so a batch on one lane overlaps on the GPU
-// with batches on the others.  Requests wait in one FIFO queue.  A free lane
-// takes every request of the head's kind at the head of the queue that fits
-// (continuous batching: whatever arrived while the lanes were busy forms the
-// next batch); compress and decompress batches each run as one batched call.
-// Admission is gated by an estimate of each request's device working memory
-// against the configured budget; a request larger than the whole budget runs
-// alone once nothing else is in flight.
+// with batches on the others.  Requests wait in one queue, oldest first.  A
+// free lane takes the oldest request it may serve and every later request
+// of the same kind it may serve that fits beside it (continuous batching:
+// whatever arrived while the lanes were busy forms the next batch), up to a
+// request count and an optional byte cap, so that small requests do not wait
+// for a large one's batch.  Express lanes serve only small requests.
+// Admission counts the device memory of every lane -- what its context holds
+// (grow-only), or the estimate of its running batch if that is larger --
+// against the budget, and a batch that needs its lane to grow also needs that
+// much free device memory (cudaMemGetInfo); a request larger than the whole
+// budget runs alone once nothing else is in flight.
 #include <chrono>
 #include <condition_variable>
 #include <cstdarg>
@@ -18,8 +22,11 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <algorithm>
 #include <unordered_map>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "wlgpu.h"
 
@@ -70,10 +77,22 @@ double estimate(const wl_request &r) {
   return 12.0 * n + 4.0 * x->n_words + out + (1 << 20);
 }
 
+// Bytes a request moves on the host side: its input (compress) or output
+// (decompress); the size classes of the byte cap and the express lanes.
+double request_bytes(const wl_request &r) {
+  if (r.kind == WL_REQ_COMPRESS)
+    return (double)r.cubelet.size[0] * r.cubelet.size[1] * r.cubelet.size[2] *
+           dtype_bytes(r.cubelet.dtype);
+  const wl_result *x = r.compressed;
+  return (double)x->original_size[0] * x->original_size[1] * x->original_size[2] *
+         dtype_bytes(r.out_dtype);
+}
+
 struct Job {
   unsigned long long id = 0;
   wl_request req;
   double est = 0;
+  double bytes = 0;
   Clock::time_point submitted, started, finished;
   bool done = false;
   wl_status st = WL_OK;
@@ -90,7 +109,9 @@ struct wl_server {
   std::condition_variable cvWork, cvDone;
   std::deque<Job *> pending;
   std::unordered_map<unsigned long long, Job *> jobs;
-  double inflight = 0;
+  double inflight = 0;          // estimates of the running batches
+  std::vector<double> held;     // device bytes each lane's context holds
+  std::vector<double> running;  // estimate of each lane's running batch (0: idle)
   bool stop = false;
   unsigned long long nextId = 1;
   std::vector<wl_ctx *> ctxs;
@@ -113,11 +134,66 @@ wl_status serve_fail(wl_server *s, wl_status st, const char *fmt, ...) {
   return st;
 }
 
-// Can the request at the head of the queue start now?
-bool head_fits(const wl_server *s) {
-  if (s->pending.empty()) return false;
-  const Job *j = s->pending.front();
-  return s->inflight == 0 || s->inflight + j->est <= (double)s->cfg.memory_budget;
+// Device bytes committed by the lanes other than `lane`.
+double committed_others(const wl_server *s, int lane) {
+  double c = 0;
+  for (size_t l = 0; l < s->held.size(); l++)
+    if ((int)l != lane) c += std::max(s->held[l], s->running[l]);
+  return c;
+}
+
+bool any_running(const wl_server *s) {
+  for (double r : s->running)
+    if (r > 0) return true;
+  return false;
+}
+
+bool express(const wl_server *s, int lane) { return lane < s->cfg.express_lanes; }
+
+bool may_take(const wl_server *s, int lane, const Job *j) {
+  return !express(s, lane) || j->bytes <= (double)s->cfg.small_request_bytes;
+}
+
+// Free device memory, refreshed at most every few milliseconds (the call
+// goes through the driver).
+double free_device_bytes(wl_server *s) {
+  static thread_local Clock::time_point last;
+  static thread_local double cached = 0;
+  const Clock::time_point now = Clock::now();
+  if (cached == 0 || now - last > std::chrono::milliseconds(5)) {
+    size_t f = 0, t = 0;
+    if (cudaSetDevice(s->device) == cudaSuccess && cudaMemGetInfo(&f, &t) == cudaSuccess)
+      cached = (double)f;
+    else
+      cudaGetLastError();
+    last = now;
+  }
+  return cached;
+}
+
+// Would a batch of estimate `est` fit on `lane` now?  A first request may
+// always run when nothing else is in flight (alone: it gets what it needs);
+// requests joining a batch must fit the budget in any case.
+bool fits(wl_server *s, int lane, double est, bool first = true) {
+  const double grow = std::max(0.0, est - s->held[lane]);
+  if (first && !any_running(s)) return true;
+  if (committed_others(s, lane) + std::max(s->held[lane], est) > (double)s->cfg.memory_budget)
+    return false;
+  // the lane's workspace grows only into memory the device has free
+  constexpr double kMargin = 256.0 * (1 << 20);
+  return grow == 0 || grow + kMargin <= free_device_bytes(s);
+}
+
+// The oldest request `lane` may serve, or the end of the queue.
+std::deque<Job *>::iterator first_for(wl_server *s, int lane) {
+  for (auto it = s->pending.begin(); it != s->pending.end(); ++it)
+    if (may_take(s, lane, *it)) return it;
+  return s->pending.end();
+}
+
+bool can_start(wl_server *s, int lane) {
+  auto it = first_for(s, lane);
+  return it != s->pending.end() && fits(s, lane, (*it)->est);
 }
 
 void worker(wl_server *s, int lane) {
@@ -130,26 +206,35 @@ void worker(wl_server *s, int lane) {
     double est = 0;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      s->cvWork.wait(lk, [&] { return s->stop || head_fits(s); });
+      s->cvWork.wait(lk, [&] { return (s->stop && s->pending.empty()) || can_start(s, lane); });
       if (s->stop && s->pending.empty()) return;
-      if (!head_fits(s)) continue;
-      const double budget = (double)s->cfg.memory_budget;
-      // every request of the head's kind that waited behind it and fits
-      // (decompress requests whose outputs are all on the host, or all on
-      // the device, batch together)
-      const int kind = s->pending.front()->req.kind;
-      const int dev = s->pending.front()->req.out_on_device;
-      while (!s->pending.empty() && (int)batch.size() < s->cfg.max_batch) {
-        Job *j = s->pending.front();
-        if (j->req.kind != kind) break;
-        if (kind == WL_REQ_DECOMPRESS && j->req.out_on_device != dev) break;
-        if (!batch.empty() && s->inflight + est + j->est > budget) break;
-        if (batch.empty() && s->inflight > 0 && s->inflight + j->est > budget) break;
+      if (!can_start(s, lane)) continue;
+      const double cap = (double)s->cfg.max_batch_bytes;
+      auto it = first_for(s, lane);
+      const int kind = (*it)->req.kind;
+      const int dev = (*it)->req.out_on_device;
+      double bytes = 0;
+      // the oldest request this lane may serve, then every later one of its
+      // kind (decompress: outputs all on the host or all on the device) that
+      // fits beside it
+      while (it != s->pending.end() && (int)batch.size() < s->cfg.max_batch) {
+        Job *j = *it;
+        const bool same = j->req.kind == kind &&
+                          (kind != WL_REQ_DECOMPRESS || j->req.out_on_device == dev);
+        const bool ok = batch.empty() ||
+                        (same && may_take(s, lane, j) && (cap <= 0 || bytes + j->bytes <= cap) &&
+                         fits(s, lane, est + j->est, false));
+        if (!ok) {
+          ++it;
+          continue;
+        }
         batch.push_back(j);
         est += j->est;
-        s->pending.pop_front();
+        bytes += j->bytes;
+        it = s->pending.erase(it);
       }
       s->inflight += est;
+      s->running[lane] = est;
       const Clock::time_point now = Clock::now();
       for (Job *j : batch) {
         j->started = now;
@@ -157,7 +242,7 @@ void worker(wl_server *s, int lane) {
         j->lane = lane;
       }
       // more work may fit beside this batch
-      if (head_fits(s)) s->cvWork.notify_one();
+      if (!s->pending.empty()) s->cvWork.notify_all();
     }
 
     if (batch[0]->req.kind == WL_REQ_DECOMPRESS) {
@@ -202,6 +287,8 @@ void worker(wl_server *s, int lane) {
       }
       s->inflight -= est;
       if (s->inflight < 1.0) s->inflight = 0;
+      s->running[lane] = 0;
+      s->held[lane] = (double)wl_memory_held(ctx);
     }
     s->cvDone.notify_all();
     s->cvWork.notify_all();
@@ -222,6 +309,9 @@ void wl_serve_config_default(wl_serve_config *cfg) {
   cfg->memory_budget = (size_t)16 << 30;
   cfg->max_batch = 1024;
   cfg->stage_host_inputs = 1;
+  cfg->max_batch_bytes = 0;
+  cfg->express_lanes = 0;
+  cfg->small_request_bytes = (size_t)4 << 20;
 }
 
 wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out) {
@@ -233,6 +323,10 @@ wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **ou
   if (cfg) s->cfg = *cfg;
   if (s->cfg.lanes < 1) s->cfg.lanes = 1;
   if (s->cfg.max_batch < 1) s->cfg.max_batch = 1;
+  if (s->cfg.express_lanes < 0) s->cfg.express_lanes = 0;
+  if (s->cfg.express_lanes >= s->cfg.lanes) s->cfg.express_lanes = s->cfg.lanes - 1;
+  s->held.assign(s->cfg.lanes, 0.0);
+  s->running.assign(s->cfg.lanes, 0.0);
   for (int i = 0; i < s->cfg.lanes; i++) {
     wl_ctx *c = nullptr;
     const wl_status st = wl_init(device, &c);
@@ -275,6 +369,7 @@ wl_status wl_serve_submit_batch(wl_server *s, const wl_request *reqs, int n,
     j->req = reqs[i];
     memset(&j->res, 0, sizeof j->res);
     j->est = estimate(reqs[i]);
+    j->bytes = request_bytes(reqs[i]);
     j->submitted = now;
     js[i] = j;
   }

@@ -67,7 +67,9 @@ REQ_COMPRESS, REQ_DECOMPRESS = 1, 2
 
 class WlServeConfig(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("memory_budget", ctypes.c_size_t),
-                ("max_batch", ctypes.c_int), ("stage_host_inputs", ctypes.c_int)]
+                ("max_batch", ctypes.c_int), ("stage_host_inputs", ctypes.c_int),
+                ("max_batch_bytes", ctypes.c_size_t), ("express_lanes", ctypes.c_int),
+                ("small_request_bytes", ctypes.c_size_t)]
 
 
 class WlRequest(ctypes.Structure):
@@ -901,12 +903,16 @@ class Server:
     until their request has been waited for."""
 
     def __init__(self, lanes: int = 2, memory_budget: int = 16 << 30, max_batch: int = 1024,
-                 device: int = 0, stage_host_inputs: bool = True):
+                 device: int = 0, stage_host_inputs: bool = True, max_batch_bytes: int = 0,
+                 express_lanes: int = 0, small_request_bytes: int = 4 << 20):
         self.lib = load()
         cfg = WlServeConfig()
         self.lib.wl_serve_config_default(ctypes.byref(cfg))
         cfg.lanes, cfg.memory_budget, cfg.max_batch = lanes, memory_budget, max_batch
         cfg.stage_host_inputs = 1 if stage_host_inputs else 0
+        cfg.max_batch_bytes = max_batch_bytes
+        cfg.express_lanes = express_lanes
+        cfg.small_request_bytes = small_request_bytes
         h = ctypes.c_void_p()
         st = self.lib.wl_serve_create(device, ctypes.byref(cfg), ctypes.byref(h))
         if st != WL_OK:
