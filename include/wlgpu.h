@@ -202,6 +202,12 @@ wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode);
 wl_status wl_set_memory_limit(wl_ctx *ctx, size_t bytes);
 size_t wl_memory_held(const wl_ctx *ctx);
 
+/* high = 1: the context's streams get the device's greatest scheduling
+ * priority, so its kernels are scheduled ahead of pending blocks of other
+ * contexts' kernels (the serving loop's express lanes); 0: the default.
+ * Call it while the context is idle. */
+wl_status wl_set_stream_priority(wl_ctx *ctx, int high);
+
 /* Synchronize the context's stream. */
 wl_status wl_sync(wl_ctx *ctx);
 
@@ -233,8 +239,9 @@ typedef struct {
                                one batch; a larger request runs alone (0, the
                                default: no cap) */
   int express_lanes;        /* lanes that take only requests of at most
-                               small_request_bytes, so small requests never
-                               wait behind large ones (default 0) */
+                               small_request_bytes, on high-priority streams,
+                               so small requests do not wait behind large
+                               ones (default 0) */
   size_t small_request_bytes; /* the express lanes' limit (default 4 MiB) */
 } wl_serve_config;
 

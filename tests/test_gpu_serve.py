@@ -181,3 +181,20 @@ def test_staged_host_inputs_match(ctx):
     ctx.set_host_input_mode(0)
     for g, r in zip(got, ref):
         assert _same(g, r)
+
+
+def test_express_lane_does_not_hold_large_requests(ctx):
+    """Requests too large for the express lane, submitted one at a time and
+    waited for, are served by the other lane (each submission wakes every
+    lane)."""
+    items = _mix(14, 4)
+    ref = [ctx.compress(a, p) for a, p in items]
+    srv = lib.Server(lanes=2, express_lanes=1, small_request_bytes=1 << 10)
+    try:
+        for (a, p), r in zip(items, ref):
+            assert a.nbytes > 1 << 10
+            c, info = srv.wait(srv.submit_compress(a, p), timeout_ms=30000)
+            assert c is not None and _same(c, r)
+            assert info["lane"] == 1
+    finally:
+        srv.close()

@@ -456,29 +456,73 @@ __device__ __forceinline__ void inv_level(const float (&s2)[M], const float (&d2
   for (int k = 0; k < M; k++) o[k] = fmaf(-kAlpha, e[k] + (k + 1 < M ? e[k + 1] : eN), d1[k]);
 }
 
-// The inverse of rowreg_fwd, in place on rows of L = E G floats stored in
-// band order: every band value the row's lanes need is read first (with the
-// deferred scale undone by division), the levels run from the deepest up
-// in registers, and the lanes store their E elements of the restored row.
-template <int G, int E, bool HAAR>
-__device__ __forceinline__ void rowreg_inv(const PassDesc &d, int row0, float *scaleTab) {
+// Where the inverse reads a row's stored (band-order, scaled) values and
+// writes its restored elements.  A lane writes elements 2 (M sub + k) and
+// 2 (M sub + k) + 1 (e[k], o[k]).
+struct InGlobalRow {  // the row in global memory
+  const float *src;
+  __device__ float get(int q) const { return src[q]; }
+};
+struct InTileCol {  // column r of a shared-memory tile, position q at q * P + r
+  const float *col;
+  int P;
+  __device__ float get(int q) const { return col[q * P]; }
+};
+struct OutGlobalInPlace {  // the float row itself (16-byte aligned for E = 8)
+  float *dst;
+  template <int M>
+  __device__ void put(int sub, const float (&e0)[M], const float (&o0)[M]) const {
+    if (M == 4) {
+      float4 *d4 = reinterpret_cast<float4 *>(dst) + 2 * sub;
+      d4[0] = make_float4(e0[0], o0[0], e0[1 % M], o0[1 % M]);
+      d4[1] = make_float4(e0[2 % M], o0[2 % M], e0[3 % M], o0[3 % M]);
+    } else {
+      float2 *d2p = reinterpret_cast<float2 *>(dst) + M * sub;
+#pragma unroll
+      for (int k = 0; k < M; k++) d2p[k] = make_float2(e0[k], o0[k]);
+    }
+  }
+};
+template <typename OutT> struct OutRowCrop {  // an output row of n real elements
+  OutT *row;
+  int n;
+  template <int M>
+  __device__ void put(int sub, const float (&e0)[M], const float (&o0)[M]) const {
+    const int b = 2 * M * sub;
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      if (b + 2 * k < n) store_from_float(row + b + 2 * k, e0[k]);
+      if (b + 2 * k + 1 < n) store_from_float(row + b + 2 * k + 1, o0[k]);
+    }
+  }
+};
+struct OutTileCol {  // back into the tile column, natural order
+  float *col;
+  int P;
+  template <int M>
+  __device__ void put(int sub, const float (&e0)[M], const float (&o0)[M]) const {
+    const int b = 2 * M * sub;
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      col[(b + 2 * k) * P] = e0[k];
+      col[(b + 2 * k + 1) * P] = o0[k];
+    }
+  }
+};
+
+// The inverse of rowreg_levels for one row of L = E G values in band order,
+// held by G lanes: every band value the row's lanes need is read first (the
+// deferred scale undone by multiplying with its reciprocal, rscale), the
+// levels run from the deepest up in registers, and each lane hands its E
+// restored elements to out.  ok: the row exists (else nothing is read or
+// written; the lanes still take part in the shuffles).
+template <int G, int E, bool HAAR, class Src, class Dst>
+__device__ __forceinline__ void rowreg_inv_core(int S, const float *rscale, int sub, bool ok,
+                                                const Src &in, const Dst &out) {
   constexpr int L = E * G;
   constexpr int M = E / 2;
   constexpr int NA1 = M == 4 ? G : 3 * G / 4;  // lanes of levels 1 and 2
-  const int S = d.steps;
-  if ((int)threadIdx.x <= S) scaleTab[threadIdx.x] = HAAR ? 1.0f : lifting_scale(threadIdx.x, S);
-  __syncthreads();
-  const int row = row0 + (int)threadIdx.x / G;
-  const int sub = threadIdx.x & (G - 1);
-  const bool ok = row < d.rows;
-  long long bi = 0, bo = 0;
-  if (ok) {
-    const int a = row / d.B, b = row - a * d.B;
-    bi = (long long)a * d.inSA + (long long)b * d.inSB;
-    bo = (long long)a * d.outSA + (long long)b * d.outSB;
-  }
-  const float *src = static_cast<const float *>(d.in) + bi;
-  auto rd = [&](int q, int t) { return ok ? src[q] / scaleTab[t] : 0.f; };
+  auto rd = [&](int q, int t) { return ok ? in.get(q) * rscale[t] : 0.f; };
   const bool act1 = sub < NA1;
   // ---- every input value, read before anything is stored
   float d0[M], d1v[2] = {0.f, 0.f}, d2v = 0.f, lowv[4] = {0.f, 0.f, 0.f, 0.f};
@@ -568,25 +612,32 @@ __device__ __forceinline__ void rowreg_inv(const PassDesc &d, int row0, float *s
   }
   float e0[M], o0[M];
   inv_level<M, G, HAAR>(s0, d0, sub, G, e0, o0);
+  if (ok) out.put(sub, e0, o0);
+}
+
+// The inverse z pass, in place: rows [row0, row0 + kRegThreads / G) of a pass
+// of float rows contiguous in memory.
+template <int G, int E, bool HAAR>
+__device__ __forceinline__ void rowreg_inv(const PassDesc &d, int row0, const float *rscale) {
+  const int row = row0 + (int)threadIdx.x / G;
+  const int sub = threadIdx.x & (G - 1);
+  const bool ok = row < d.rows;
+  long long bi = 0, bo = 0;
   if (ok) {
-    float *dst = static_cast<float *>(d.out) + bo;
-    if (M == 4) {
-      float4 *d4 = reinterpret_cast<float4 *>(dst) + 2 * sub;
-      d4[0] = make_float4(e0[0], o0[0], e0[1 % M], o0[1 % M]);
-      d4[1] = make_float4(e0[2 % M], o0[2 % M], e0[3 % M], o0[3 % M]);
-    } else {
-      float2 *d2p = reinterpret_cast<float2 *>(dst) + M * sub;
-#pragma unroll
-      for (int k = 0; k < M; k++) d2p[k] = make_float2(e0[k], o0[k]);
-    }
+    const int a = row / d.B, b = row - a * d.B;
+    bi = (long long)a * d.inSA + (long long)b * d.inSB;
+    bo = (long long)a * d.outSA + (long long)b * d.outSB;
   }
+  rowreg_inv_core<G, E, HAAR>(d.steps, rscale, sub, ok,
+                              InGlobalRow{static_cast<const float *>(d.in) + bi},
+                              OutGlobalInPlace{static_cast<float *>(d.out) + bo});
 }
 
 template <int G, int E>
 __global__ void __launch_bounds__(kRegThreads)
 dwt_rowreg_inv_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
                       int nPasses) {
-  __shared__ float scaleTab[16];
+  __shared__ float rscale[16];
   const int bid = blockIdx.x;
   int lo = 0, hi = nPasses - 1;
   while (lo < hi) {
@@ -595,8 +646,133 @@ dwt_rowreg_inv_kernel(const PassDesc *__restrict__ passes, const int *__restrict
   }
   const PassDesc &d = passes[lo];
   const int row0 = (bid - tilePrefix[lo]) * (kRegThreads / G);
-  if (d.wavelet == WL_HAAR) rowreg_inv<G, E, true>(d, row0, scaleTab);
-  else rowreg_inv<G, E, false>(d, row0, scaleTab);
+  const int S = d.steps;
+  const bool haar = d.wavelet == WL_HAAR;
+  if ((int)threadIdx.x <= S) rscale[threadIdx.x] = haar ? 1.0f : 1.0f / lifting_scale(threadIdx.x, S);
+  __syncthreads();
+  if (haar) rowreg_inv<G, E, true>(d, row0, rscale);
+  else rowreg_inv<G, E, false>(d, row0, rscale);
+}
+
+// Inverse passes whose rows are strided in the input (band order along the
+// row, consecutive rows neighbours in memory): the y pass (z-x-y -> z-y-x)
+// and the x pass into the output type with the crop (z-y-x -> x-y-z).  A
+// block takes R rows: warps load one position of 32 neighbouring rows at a
+// time (coalesced) into a shared-memory tile (odd stride), the G lanes of
+// each row run its levels up in registers from its tile column, and the
+// restored elements leave either straight into the output row (x pass: the
+// output rows are contiguous; typed, cropped) or back through the tile,
+// position by position, 32 neighbouring rows per warp store (y pass).
+template <typename OutT, int G, int E, bool HAAR>
+__device__ __forceinline__ void rowreg_inv_t(const PassDesc &d, int tile, float *tileSm,
+                                             const float *rscale, const long long *rowIn,
+                                             const long long *rowOut) {
+  constexpr int L = E * G;
+  constexpr int R = TileRows<G>::R, P = TileRows<G>::P, kPerRound = TileRows<G>::kPerRound;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kWarps = kRegThreads / 32;
+  const float *in = static_cast<const float *>(d.in);
+  const long long inSC = d.inSC;
+  for (int rr = lane; rr < R; rr += 32) {
+    const long long bi = rowIn[rr];
+    if (bi < 0) continue;
+    const float *src = in + bi + warp * inSC;
+    float *t = tileSm + warp * P + rr;
+#pragma unroll 4
+    for (int q = warp; q < L; q += kWarps) {
+      *t = *src;
+      src += kWarps * inSC;
+      t += kWarps * P;
+    }
+  }
+  __syncthreads();
+  OutT *out = static_cast<OutT *>(d.out);
+  const bool contig = d.outSC == 1;
+  const int sub = threadIdx.x & (G - 1);
+  for (int rr = (int)threadIdx.x / G; rr < R; rr += kPerRound) {
+    const bool ok = rowIn[rr] >= 0;
+    const InTileCol src{tileSm + rr, P};
+    if (contig) {
+      const long long bo = rowOut[rr];
+      rowreg_inv_core<G, E, HAAR>(d.steps, rscale, sub, ok && bo >= 0, src,
+                                  OutRowCrop<OutT>{out + (bo < 0 ? 0 : bo), min(L, d.cropL)});
+    } else {
+      rowreg_inv_core<G, E, HAAR>(d.steps, rscale, sub, ok, src, OutTileCol{tileSm + rr, P});
+    }
+  }
+  if (contig) return;
+  __syncthreads();
+  const long long outSC = d.outSC;
+  const int n = min(L, d.cropL);
+  for (int rr = lane; rr < R; rr += 32) {
+    const long long bo = rowOut[rr];
+    if (bo < 0) continue;
+    OutT *dst = out + bo + warp * outSC;
+    const float *t = tileSm + warp * P + rr;
+#pragma unroll 4
+    for (int q = warp; q < n; q += kWarps) {
+      store_from_float(dst, *t);
+      dst += kWarps * outSC;
+      t += kWarps * P;
+    }
+  }
+}
+
+template <typename OutT, int G, int E>
+__global__ void __launch_bounds__(kRegThreads)
+dwt_rowreg_inv_t_kernel(const PassDesc *__restrict__ passes, const int *__restrict__ tilePrefix,
+                        int nPasses) {
+  extern __shared__ float tileSm[];
+  __shared__ float rscale[16];
+  __shared__ long long rowIn[TileRows<G>::R], rowOut[TileRows<G>::R];
+  const int bid = blockIdx.x;
+  int lo = 0, hi = nPasses - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tilePrefix[mid] <= bid) lo = mid; else hi = mid - 1;
+  }
+  const PassDesc &d = passes[lo];
+  const int tile = bid - tilePrefix[lo];
+  constexpr int R = TileRows<G>::R;
+  const int S = d.steps;
+  const bool haar = d.wavelet == WL_HAAR;
+  if ((int)threadIdx.x <= S) rscale[threadIdx.x] = haar ? 1.0f : 1.0f / lifting_scale(threadIdx.x, S);
+  for (int t = threadIdx.x; t < R; t += kRegThreads) {
+    const int row = tile * R + t;
+    long long bi = -1, bo = -1;
+    if (row < d.rows) {
+      const int a = row / d.B, b = row - a * d.B;
+      bi = (long long)a * d.inSA + (long long)b * d.inSB;
+      if (a < d.cropA && b < d.cropB) bo = (long long)a * d.outSA + (long long)b * d.outSB;
+    }
+    rowIn[t] = bi;
+    rowOut[t] = bo;
+  }
+  __syncthreads();
+  if (haar) rowreg_inv_t<OutT, G, E, true>(d, tile, tileSm, rscale, rowIn, rowOut);
+  else rowreg_inv_t<OutT, G, E, false>(d, tile, tileSm, rscale, rowIn, rowOut);
+}
+
+template <typename OutT, int G, int E = 8>
+void launch_itg(const PassDesc *p, const int *tp, int n, int blocks, cudaStream_t s) {
+  const int smem = E * G * TileRows<G>::P * (int)sizeof(float);
+  auto k = dwt_rowreg_inv_t_kernel<OutT, G, E>;
+  if (smem > 48 * 1024) raise_smem_limit(k, smem);
+  k<<<blocks, kRegThreads, smem, s>>>(p, tp, n);
+}
+
+template <typename OutT>
+void launch_it_len(const PassDesc *p, const int *tp, int n, int blocks, int L, cudaStream_t s) {
+  switch (L) {
+    case 16: launch_itg<OutT, 2>(p, tp, n, blocks, s); break;
+    case 32: launch_itg<OutT, 4>(p, tp, n, blocks, s); break;
+    case 48: launch_itg<OutT, 8, 6>(p, tp, n, blocks, s); break;
+    case 64: launch_itg<OutT, 8>(p, tp, n, blocks, s); break;
+    case 96: launch_itg<OutT, 16, 6>(p, tp, n, blocks, s); break;
+    case 128: launch_itg<OutT, 16>(p, tp, n, blocks, s); break;
+    case 192: launch_itg<OutT, 32, 6>(p, tp, n, blocks, s); break;
+    default: launch_itg<OutT, 32>(p, tp, n, blocks, s); break;
+  }
 }
 
 template <int G, int E = 8>
@@ -699,6 +875,16 @@ void launch_dwt_rowreg_inv(const PassDesc *p, const int *tp, int n, int blocks, 
     case 128: launch_ig<16>(p, tp, n, blocks, s); break;
     case 192: launch_ig<32, 6>(p, tp, n, blocks, s); break;
     default: launch_ig<32>(p, tp, n, blocks, s); break;
+  }
+}
+
+void launch_dwt_rowreg_inv_t(const PassDesc *p, const int *tp, int n, int blocks, int L,
+                             int outType, cudaStream_t s) {
+  switch (outType) {
+    case WL_U8: launch_it_len<uint8_t>(p, tp, n, blocks, L, s); break;
+    case WL_U16: launch_it_len<uint16_t>(p, tp, n, blocks, L, s); break;
+    case WL_I32: launch_it_len<int32_t>(p, tp, n, blocks, L, s); break;
+    default: launch_it_len<float>(p, tp, n, blocks, L, s); break;
   }
 }
 

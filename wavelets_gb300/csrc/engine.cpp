@@ -89,7 +89,8 @@ int group_key(bool cols, int dtype, int L, bool vec = false) {
 int rowreg_key(int L) { return (1 << 20) | L; }
 int rowreg_t_key(int dtype, int L) { return (1 << 21) | (dtype << 16) | L; }
 int rowreg_inv_key(int L) { return (1 << 23) | L; }
-enum RegKind { kRegNone, kRegInPlace, kRegTile, kRegInvInPlace };
+int rowreg_inv_t_key(int outType, int L) { return (1 << 24) | (outType << 16) | L; }
+enum RegKind { kRegNone, kRegInPlace, kRegTile, kRegInvInPlace, kRegInvTile };
 
 // ---- result storage ------------------------------------------------------------
 // The arrays of all results of one compression call live in one page-locked
@@ -651,8 +652,8 @@ wl_status stage_group(wl_ctx *ctx, std::vector<PassDesc> g, size_t &hoff, int ki
     if ((d.selHist != nullptr) != sel)
       return fail(ctx, WL_EINVAL, "internal: mixed select-gathering passes in one group");
   if (regL) {
-    rows = regKind == kRegTile ? dwt_rowreg_t_rows_per_block(regL)
-                               : dwt_rowreg_rows_per_block(regL, sel);
+    rows = (regKind == kRegTile || regKind == kRegInvTile) ? dwt_rowreg_t_rows_per_block(regL)
+                                                          : dwt_rowreg_rows_per_block(regL, sel);
     for (PassDesc &d : g) {
       d.T = rows;
       d.tiles = (d.rows + rows - 1) / rows;
@@ -711,6 +712,8 @@ wl_status launch_one(wl_ctx *ctx, const GroupLaunch &l, cudaStream_t s) {
     launch_dwt_rowreg_t(dp, dtp, l.n, l.tiles, l.regL, l.inType, s);
   else if (l.regKind == kRegInvInPlace)
     launch_dwt_rowreg_inv(dp, dtp, l.n, l.tiles, l.regL, s);
+  else if (l.regKind == kRegInvTile)
+    launch_dwt_rowreg_inv_t(dp, dtp, l.n, l.tiles, l.regL, l.outType, s);
   else if (l.regL)
     launch_dwt_rowreg(dp, dtp, l.n, l.tiles, l.regL, l.sel, s);
   else if (l.cols)
@@ -1329,6 +1332,8 @@ void inverse_passes(const int size[3], const int steps[3], int wavelet, const in
       const int phase = 3 - np + i;
       if (phase == 0 && dwt_rowreg_fits(d[i].L, d[i].steps))  // z rows in registers
         ph[0][rowreg_inv_key(d[i].L)].push_back(d[i]);
+      else if (phase > 0 && dwt_rowreg_fits(d[i].L, d[i].steps))  // y, x: through a tile
+        ph[phase][rowreg_inv_t_key(phase == 2 ? outType : WL_F32, d[i].L)].push_back(d[i]);
       else
         put(phase, true, d[i]);
     }
@@ -1377,6 +1382,11 @@ wl_status run_inverse_phases(wl_ctx *ctx, PassGroups ph[3]) {
   const int kinds[3] = {kTuneInvZ, kTuneInvY, kTuneInvX};
   for (int k = 0; k < 3; k++) {
     for (const auto &kv : ph[k]) {
+      if ((kv.first >> 24) & 1) {
+        TRY(stage_group(ctx, kv.second, hoff, kinds[k], WL_F32, (kv.first >> 16) & 15, true, false,
+                        false, gl, nullptr, kv.second[0].L, kRegInvTile));
+        continue;
+      }
       if ((kv.first >> 23) & 1) {
         TRY(stage_group(ctx, kv.second, hoff, kinds[k], WL_F32, WL_F32, true, false, false, gl,
                         nullptr, kv.second[0].L, kRegInvInPlace));
@@ -2025,7 +2035,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->chunkSpan, &ctx->optIn, &ctx->optOut, &ctx->optErr,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
-                   &ctx->meta};
+                   &ctx->meta, &ctx->errIn, &ctx->errRest, &ctx->errPart};
   for (DevBuf *d : dbs) if (d->p) cudaFree(d->p);
   for (GraphEntry &g : ctx->graphs) drop_graph(g);
   HostBuf *hbs[] = {&ctx->hStage[0], &ctx->hStage[1], &ctx->hState, &ctx->hDecode, &ctx->hPasses,
@@ -2264,6 +2274,37 @@ wl_status wl_autotune(wl_ctx *ctx, int max_len, int reps) {
   if (reps <= 0) reps = 5;
   if (reps > 64) reps = 64;
   return autotune_impl(ctx, max_len, reps);
+}
+
+wl_status wl_set_stream_priority(wl_ctx *ctx, int high) {
+  if (!ctx) return WL_EINVAL;
+  CU(cudaSetDevice(ctx->device));
+  int least = 0, greatest = 0;
+  CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  const int prio = high ? greatest : least;
+  // new streams, once the old ones have drained (captured graphs are not
+  // bound to a stream and stay valid)
+  cudaStream_t ns = nullptr;
+  CU(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+  cudaStream_t nside[wl_ctx::kSide] = {};
+  for (int k = 0; k < wl_ctx::kSide; k++)
+    if (ctx->side[k] &&
+        cudaStreamCreateWithPriority(&nside[k], cudaStreamNonBlocking, prio) != cudaSuccess) {
+      cudaGetLastError();
+      for (int j = 0; j < k; j++) cudaStreamDestroy(nside[j]);
+      cudaStreamDestroy(ns);
+      return fail(ctx, WL_ECUDA, "cannot create a stream of priority %d", prio);
+    }
+  CU(cudaStreamSynchronize(ctx->stream));
+  cudaStreamDestroy(ctx->stream);
+  ctx->stream = ns;
+  for (int k = 0; k < wl_ctx::kSide; k++)
+    if (ctx->side[k]) {
+      cudaStreamSynchronize(ctx->side[k]);
+      cudaStreamDestroy(ctx->side[k]);
+      ctx->side[k] = nside[k];
+    }
+  return WL_OK;
 }
 
 wl_status wl_set_memory_limit(wl_ctx *ctx, size_t bytes) {

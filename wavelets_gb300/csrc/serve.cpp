@@ -337,6 +337,7 @@ wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **ou
     }
     s->ctxs.push_back(c);
     wl_set_host_input_mode(c, s->cfg.stage_host_inputs ? 1 : 0);
+    if (i < s->cfg.express_lanes) wl_set_stream_priority(c, 1);
   }
   for (int i = 0; i < s->cfg.lanes; i++) s->workers.emplace_back(worker, s, i);
   *out = s;
@@ -387,7 +388,8 @@ wl_status wl_serve_submit_batch(wl_server *s, const wl_request *reqs, int n,
       tickets[i] = j->id;
     }
   }
-  s->cvWork.notify_one();
+  // every lane: an express lane may not serve what was queued, another may
+  s->cvWork.notify_all();
   return WL_OK;
 }
 

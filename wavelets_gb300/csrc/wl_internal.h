@@ -241,6 +241,12 @@ void launch_dwt_rowreg(const PassDesc *d_passes, const int *d_tilePrefix, int nP
 void launch_dwt_rowreg_inv(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
                            int blocks, int L, cudaStream_t s);
 int dwt_rowreg_t_rows_per_block(int L);
+// inverse y and x passes (rows strided in the input, neighbouring rows
+// neighbours in memory): rows through a shared-memory tile of
+// dwt_rowreg_t_rows_per_block(L) rows, out to outType (the x pass: rows
+// contiguous in the output, cropped) or back through the tile (the y pass)
+void launch_dwt_rowreg_inv_t(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
+                             int blocks, int L, int outType, cudaStream_t s);
 void launch_dwt_rowreg_t(const PassDesc *d_passes, const int *d_tilePrefix, int nPasses,
                          int blocks, int L, int inType, cudaStream_t s);
 

@@ -193,6 +193,7 @@ EXPORTS = {
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_float, ctypes.POINTER(WlErrorStats)]),
     "wl_set_memory_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
+    "wl_set_stream_priority": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "wl_memory_held": (ctypes.c_size_t, [ctypes.c_void_p]),
     "wl_error_metrics_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
                                              ctypes.POINTER(WlErrorStats)]),
