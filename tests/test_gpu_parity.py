@@ -498,15 +498,20 @@ def test_decompress_batch_equals_single(ctx):
 @pytest.mark.parametrize("axis", ["x", "y"])
 @pytest.mark.parametrize("dtype", [np.float32, np.uint8, np.uint16])
 def test_row_register_inverse_xy_lengths_round_trip(ctx, L, s, axis, dtype):
-    """Inverse y and x passes on every row length the row-register tile kernel
-    takes (padded 16..256, 48, 96, 192), the x pass cropping to the original
-    length and converting to the output type: the restored volume equals the
-    input (floats within 2e-6, integers within 1)."""
+    """Inverse y and x passes (and the forward y pass) on every row length the
+    row-register tile kernels take (padded 16..256, 48, 96, 192), the inverse
+    x pass cropping to the original length and converting to the output type:
+    forward against the float64 lifting yardstick, and the restored volume
+    equals the input (floats within 2e-6, integers within 1)."""
     shape = (9, 7, L) if axis == "x" else (9, L, 7)
     steps = (s, 1, 1) if axis == "x" else (1, s, 1)
     a = synth.scaled_blob_cubelet(np.random.default_rng(L * 7 + s), shape, dtype)
     p = P.Params(steps=steps)
     coeffs, stored = ctx.forward_transform(a, p)
+    # the forward y pass on these lengths runs through the tile kernel too
+    from oracle import lifting64
+    ref64, _ = lifting64.forward(a, steps, p.wavelet)
+    assert float(np.abs(coeffs - ref64).max()) / float(np.abs(ref64).max()) <= FP64_RTOL
     cs = P.clamp_steps(steps, lib._size_of(a))
     back = ctx.inverse_transform(coeffs, stored, cs, p.wavelet, lib._size_of(a), dtype)
     if dtype == np.float32:
