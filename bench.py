@@ -354,6 +354,7 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30
     q = queue.Queue()
     lat = {"compress": [], "decompress": []}
     by_class = {name: [] for _, _, name in SERVE_CLASSES}
+    split = {"queue": [], "service": [], "batch": []}
     done_bytes = [0]
     t_last = [0.0]
     errors = []
@@ -370,6 +371,9 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30
                 errors.append(str(e))
                 continue
             lat[kind].append(info["total_ms"])
+            split["queue"].append(info["queue_ms"])
+            split["service"].append(info["service_ms"])
+            split["batch"].append(info["batch_size"])
             for lo, hi, name in SERVE_CLASSES:
                 if lo < nbytes <= hi or (lo == 0 and nbytes <= hi):
                     by_class[name].append(info["total_ms"])
@@ -407,6 +411,10 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30
             "memory_budget_gib": budget / (1 << 30),
             "by_size": {name: {"requests": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)}
                         for name, v in by_class.items()},
+            "queue_p50_ms": pct(split["queue"], 50), "queue_p99_ms": pct(split["queue"], 99),
+            "service_p50_ms": pct(split["service"], 50),
+            "service_p99_ms": pct(split["service"], 99),
+            "batch_size_p50": pct(split["batch"], 50), "batch_size_p99": pct(split["batch"], 99),
             "value": done_bytes[0] / elapsed / 1e9, "unit": "GB/s",
             "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
             "compress_p50_ms": pct(lat["compress"], 50), "compress_p99_ms": pct(lat["compress"], 99),

@@ -21,6 +21,10 @@
 #include <map>
 #include <unordered_map>
 #include <mutex>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -118,7 +122,9 @@ class SlabPool {
       }
     }
     ResultSlab *s = new ResultSlab;
-    const size_t cap = std::max<size_t>(bytes + bytes / 4, (size_t)1 << 20);
+    // power-of-two sizes from 1 MiB, so that freed slabs fit later requests
+    size_t cap = (size_t)1 << 20;
+    while (cap < bytes) cap <<= 1;
     if (cudaHostAlloc(reinterpret_cast<void **>(&s->base), cap, cudaHostAllocDefault) != cudaSuccess) {
       cudaGetLastError();
       delete s;
@@ -139,10 +145,85 @@ class SlabPool {
   }
 
  private:
-  static constexpr size_t kKeep = 4;  // free slabs kept for reuse
+  static constexpr size_t kKeep = 16;  // free slabs kept for reuse
   std::mutex mu_;
   std::vector<ResultSlab *> free_;
 };
+
+// Host worker threads shared by every context (the log quantizer's boundary
+// tables): started once, kept for the life of the process, so that a call
+// does not pay for creating threads.  run(n, f) calls f(i) for i in [0, n)
+// on the caller and the workers and returns when all are done; calls from
+// several host threads share the workers.
+class HostPool {
+ public:
+  HostPool() {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int n = std::min(hw, 16) - 1;
+    for (int i = 0; i < n; i++) threads_.emplace_back([this] { loop(); });
+  }
+  void run(int n, const std::function<void(int)> &f) {
+    if (n <= 0) return;
+    auto job = std::make_shared<Job>();
+    job->f = &f;
+    job->n = n;
+    if (n > 1 && !threads_.empty()) {
+      std::lock_guard<std::mutex> g(mu_);
+      jobs_.push_back(job);
+      cv_.notify_all();
+    }
+    work(*job);
+    std::unique_lock<std::mutex> lk(job->mu);
+    job->cv.wait(lk, [&] { return job->done == job->n; });
+  }
+
+ private:
+  struct Job {
+    const std::function<void(int)> *f = nullptr;
+    int n = 0;
+    std::atomic<int> next{0};
+    int done = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+  };
+  static void work(Job &j) {
+    int k, mine = 0;
+    while ((k = j.next.fetch_add(1)) < j.n) {
+      (*j.f)(k);
+      mine++;
+    }
+    if (mine) {
+      std::lock_guard<std::mutex> g(j.mu);
+      j.done += mine;
+      if (j.done == j.n) j.cv.notify_all();
+    }
+  }
+  void loop() {
+    for (;;) {
+      std::shared_ptr<Job> j;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !jobs_.empty(); });
+        j = jobs_.front();
+        if (j->next.load() >= j->n) {  // nothing left to take: retire it
+          jobs_.pop_front();
+          continue;
+        }
+      }
+      work(*j);
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::shared_ptr<Job>> jobs_;
+  std::vector<std::thread> threads_;
+};
+
+// never destroyed: its threads live until the process exits
+HostPool &host_pool() {
+  static HostPool *p = new HostPool;
+  return *p;
+}
 
 // never destroyed: results may be released during process teardown
 SlabPool &slab_pool() {
@@ -1119,26 +1200,19 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       lh[i] = make_int4(0, 0, 0, 0);
       if (plans[i].p.quant_alg == WL_LOG) logIdx.push_back(i);
     }
-    std::atomic<int> next{0}, bad{-1};
-    auto work = [&]() {
+    std::atomic<int> bad{-1};
+    const std::function<void(int)> one = [&](int k) {
       LogTable t;
-      for (int k; (k = next.fetch_add(1)) < (int)logIdx.size();) {
-        const int i = logIdx[k];
-        log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
-        if (t.nPos + t.nNeg > 2 * plans[i].p.bin_count) {
-          bad.store(i);
-          continue;
-        }
-        lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
-        std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
+      const int i = logIdx[k];
+      log_quant_table(plans[i].p.bin_count, hs[i].threshold, hs[i].maxAbs, t);
+      if (t.nPos + t.nNeg > 2 * plans[i].p.bin_count) {
+        bad.store(i);
+        return;
       }
+      lh[i] = make_int4(t.lowBin, t.highNeg, t.nPos, t.nNeg);
+      std::copy(t.bounds.begin(), t.bounds.end(), tab + plans[i].tableOff);
     };
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int nThreads = std::min<int>({hw, 16, ((int)logIdx.size() + 7) / 8});
-    std::vector<std::thread> pool;
-    for (int k = 1; k < nThreads; k++) pool.emplace_back(work);
-    work();
-    for (std::thread &th : pool) th.join();
+    host_pool().run((int)logIdx.size(), one);
     if (bad.load() >= 0)
       return fail(ctx, WL_EINVAL, "cubelet %d: log quantizer degenerate (largest |c| ~ threshold)",
                   bad.load());
