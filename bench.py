@@ -858,8 +858,8 @@ def main():
     dom = max((k for k in per_step if group_bytes.get(k, 0) > 0), key=lambda k: per_step[k])
     dom_gbs = group_bytes[dom] / (per_step[dom] / 1e3) / 1e9 if per_step[dom] > 0 else 0.0
     # measured DRAM bytes (read + write) per padded voxel of the mixed batch,
-    # from the ncu captures summarised in profiles/kernels_mixed128.md
-    traffic_per_voxel = {"quantize": 4.80, "select": 8.20} if args.workload == "mixed" else {}
+    # from the ncu capture summarised in profiles/step_metrics_mixed128.md
+    traffic_per_voxel = {"quantize": 4.76, "select": 4.44} if args.workload == "mixed" else {}
     traffic = traffic_per_voxel[dom] * n_pad if dom in traffic_per_voxel else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": dom_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": dom_gbs / hbm, "traffic": traffic,
