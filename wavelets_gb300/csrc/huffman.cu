@@ -470,6 +470,21 @@ __global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
           v |= (unsigned long long)(t >> 13) << l;
           l += 3;
         }
+        // the common case: at most 32 bits, one OR into the 64-bit
+        // accumulator (bits < 32 here, and a code has no bits above its
+        // length)
+        if (l <= 32) {
+          acc |= v << bits;
+          bits += l;
+          if (bits >= 32) {
+            if (w == wFirst) atomicOr(&dstw[w], (unsigned)acc);
+            else dstw[w] = (unsigned)acc;
+            w++;
+            acc >>= 32;
+            bits -= 32;
+          }
+          continue;
+        }
         // up to 61 bits, appended at most 32 at a time (bits < 32 here)
         while (l > 0) {
           const int take = l < 32 ? l : 32;

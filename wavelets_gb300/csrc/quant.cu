@@ -373,6 +373,12 @@ __device__ __forceinline__ int quant_value(float x, const QParams &q, const floa
   if (x >= tab[q.nb - 1]) return q.nb;
   const int c = (int)(order_key(x) >> 20);
   const int lo = lut[c], hi = lut[c + 1];
+  // a cell (1/8 octave) rarely holds more than two boundaries: compare with
+  // them directly, search only when there are more
+  if (hi - lo <= 2) {
+    const int n = hi - lo;
+    return lo + (n > 0 && tab[lo] < x ? 1 : 0) + (n > 1 && tab[lo + 1] < x ? 1 : 0);
+  }
   return lo + count_lt(tab + lo, hi - lo, x);
 }
 
@@ -672,8 +678,9 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
       const int gw = __shfl_sync(kAll, g0, w);
       const int nw = fr + __shfl_sync(kAll, I, w);
       uint16_t *g = b.tok + cd.coefOff + start + lead + o;
-      for (int j = lane; j < nw; j += 32)
-        g[j] = j < fr ? run_token_at(gw, j, B, dupV) : stage[j - fr];
+      // the first run's few tokens, then the staged ones (a plain copy)
+      for (int j = lane; j < fr; j += 32) g[j] = run_token_at(gw, j, B, dupV);
+      for (int j = fr + lane; j < nw; j += 32) g[j] = stage[j - fr];
     }
     __syncwarp();  // the staged tokens are read before the next prefill
     if (threadIdx.x == 0) {
