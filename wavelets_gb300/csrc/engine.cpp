@@ -153,8 +153,9 @@ class SlabPool {
 // Host worker threads shared by every context (the log quantizer's boundary
 // tables): started once, kept for the life of the process, so that a call
 // does not pay for creating threads.  run(n, f) calls f(i) for i in [0, n)
-// on the caller and the workers and returns when all are done; calls from
-// several host threads share the workers.
+// on the caller and the workers (about one per 8 items; fewer than 16 items
+// run on the caller alone) and returns when all are done; calls from several
+// host threads share the workers.
 class HostPool {
  public:
   HostPool() {
@@ -164,13 +165,19 @@ class HostPool {
   }
   void run(int n, const std::function<void(int)> &f) {
     if (n <= 0) return;
+    if (n < kMinShared) {  // a few items: on the caller, no thread woken
+      for (int i = 0; i < n; i++) f(i);
+      return;
+    }
     auto job = std::make_shared<Job>();
     job->f = &f;
     job->n = n;
-    if (n > 1 && !threads_.empty()) {
+    if (!threads_.empty()) {
       std::lock_guard<std::mutex> g(mu_);
       jobs_.push_back(job);
-      cv_.notify_all();
+      // wake about one worker per 8 items
+      const int wake = std::min<int>((int)threads_.size(), (n + 7) / 8 - 1);
+      for (int k = 0; k < wake; k++) cv_.notify_one();
     }
     work(*job);
     std::unique_lock<std::mutex> lk(job->mu);
@@ -178,6 +185,7 @@ class HostPool {
   }
 
  private:
+  static constexpr int kMinShared = 16;  // fewer items run on the caller
   struct Job {
     const std::function<void(int)> *f = nullptr;
     int n = 0;
@@ -313,6 +321,13 @@ struct wl_ctx {
   static constexpr int kSide = 3;
   cudaStream_t side[kSide] = {};
   cudaEvent_t fork = nullptr, join[kSide] = {};
+  // second half of a large batch: its own stream, started when the first
+  // half's transform has finished (halfT), joined back at the end (halfJ)
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t halfT = nullptr, halfJ = nullptr;
+  cudaStream_t side2[kSide] = {};  // the second half's side streams
+  cudaEvent_t fork2 = nullptr, join2[kSide] = {};
+  int splitMode = 1;  // 1: split large batches into two staggered halves
   float timings[6] = {0, 0, 0, 0, 0, 0};
   bool profiling = false;
   cudaEvent_t pev[10] = {};
@@ -820,6 +835,32 @@ wl_status launch_groups(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t 
 // before anything later in the stream runs.  Small groups -- a few hundred
 // tiles of short rows -- fill the SMs that a lone launch of them would leave
 // idle.
+wl_status launch_phase_on(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b,
+                          cudaStream_t main, cudaStream_t *side, cudaEvent_t fork,
+                          cudaEvent_t *join) {
+  if (b - a <= 1 || !fork) {
+    for (size_t i = a; i < b; i++) TRY(launch_one(ctx, ls[i], main));
+    return WL_OK;
+  }
+  std::vector<size_t> order;
+  for (size_t i = a; i < b; i++) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return ls[x].weight() > ls[y].weight();
+  });
+  const int nStreams = (int)std::min<size_t>(order.size(), wl_ctx::kSide + 1);
+  CU(cudaEventRecord(fork, main));
+  for (int k = 1; k < nStreams; k++) CU(cudaStreamWaitEvent(side[k - 1], fork, 0));
+  for (size_t j = 0; j < order.size(); j++) {
+    const int k = (int)(j % nStreams);
+    TRY(launch_one(ctx, ls[order[j]], k ? side[k - 1] : main));
+  }
+  for (int k = 1; k < nStreams; k++) {
+    CU(cudaEventRecord(join[k - 1], side[k - 1]));
+    CU(cudaStreamWaitEvent(main, join[k - 1], 0));
+  }
+  return WL_OK;
+}
+
 wl_status launch_phase(wl_ctx *ctx, const std::vector<GroupLaunch> &ls, size_t a, size_t b) {
   if (b - a <= 1 || !ctx->fork) return launch_groups(ctx, ls, a, b);
   std::vector<size_t> order;
@@ -1016,17 +1057,47 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     }
   }
 
+  // ---- halves ----
+  // A large batch runs as two halves (cubelets [0, cut) and [cut, n), cut at
+  // half of the padded elements) on two streams: the second half's transform
+  // starts when the first half's has finished, so each half's latency-bound
+  // steps (radix-select resolves, Lloyd solve, zero-run join, Huffman tree
+  // build) run beside the other half's bulk passes.  Each half is a view of
+  // the same buffers (per-cubelet and per-chunk arrays offset to its first
+  // cubelet and chunk), so the results are those of one batch.
+  int cut = n, nh = 1;
+  if (ctx->splitMode && ctx->stream2 && !coefOut && !ctx->profiling && n >= 8 &&
+      coefTotal >= (32LL << 20)) {
+    long long acc = 0;
+    for (int i = 0; i < n; i++) {
+      acc += plans[i].n;
+      if (2 * acc >= coefTotal) { cut = i + 1; break; }
+    }
+    cut = std::max(1, std::min(cut, n - 1));
+    nh = 2;
+  }
+  const int hc0[3] = {0, cut, n};
+  auto half_of = [&](int i) { return i < cut ? 0 : 1; };
+
   // ---- descriptors (host side of the upload block) ----
   CubeletDev *hc = H<CubeletDev>(ctx->hPasses);
   long long *hp = reinterpret_cast<long long *>(H<char>(ctx->hPasses) + cubBytes);
   long long groupTotal = 0;
+  long long chunk0[2] = {0, 0}, group0[2] = {0, 0}, words0[2] = {0, 0};
+  long long wordsAcc = 0;
   for (int i = 0; i < n; i++) {
     const Plan &pl = plans[i];
+    const int h = half_of(i);
+    if (i == hc0[h]) {
+      chunk0[h] = pl.chunkBase;
+      group0[h] = groupTotal;
+      words0[h] = wordsAcc;
+    }
     CubeletDev &c = hc[i];
     memset(&c, 0, sizeof c);
     c.n = pl.n;
     c.coefOff = pl.coefOff;
-    c.chunkBase = pl.chunkBase;
+    c.chunkBase = pl.chunkBase - chunk0[h];
     c.wordsOff = 0;
     c.wordsCap = pl.wordsCap;
     c.nChunks = pl.nChunks;
@@ -1036,9 +1107,10 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     c.frac = pl.p.threshold_fraction;
     c.lloydIters = pl.p.lloyd_iters > 0 ? pl.p.lloyd_iters : 20;
     c.tableOff = pl.tableOff;
-    c.groupBase = (int)groupTotal;
+    c.groupBase = (int)(groupTotal - group0[h]);
     groupTotal += (pl.nChunks + kQuantGroup - 1) / kQuantGroup;
-    hp[i] = pl.chunkBase;
+    wordsAcc += pl.wordsCap;
+    hp[i] = c.chunkBase;
   }
 
   DevBatch b;
@@ -1071,56 +1143,118 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.logHdr = P<int4>(ctx->logHdr);
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
+  constexpr long long kMetaPer = 4LL * kMaxSymbols + 2LL * kMaxBins;  // ints per cubelet
+  DevBatch bh[2] = {b, b};
+  if (nh == 2) {
+    for (int h = 0; h < 2; h++) {
+      DevBatch &v = bh[h];
+      const int c0 = hc0[h];
+      const long long ch = chunk0[h], g = group0[h];
+      v.n = hc0[h + 1] - c0;
+      v.cub += c0;
+      v.state += c0;
+      v.selHist += (size_t)c0 * kSelectBins;
+      v.lloydHist += (size_t)c0 * kLloydBins;
+      v.qlut += (size_t)c0 * kLutStride;
+      v.dqtable += (size_t)c0 * kMaxBins;
+      v.hist += (size_t)c0 * kMaxSymbols;
+      v.codes += (size_t)c0 * kMaxSymbols;
+      v.codeLen += (size_t)c0 * kMaxSymbols;
+      v.decode += (size_t)c0 * 4 * kMaxSymbols;
+      v.logHdr += c0;
+      v.chunkPrefix += c0;
+      v.chunkTok += ch;
+      v.chunkSpan += ch;
+      v.chunkRun += ch;
+      v.chunkRunCtx += 2 * ch;
+      v.chunkBits += ch;
+      v.chunkCub += ch;
+      v.groupCub += g;
+      v.words += words0[h];
+      v.meta += c0 * kMetaPer;
+      v.totalChunks = (h ? chunkTotal : chunk0[1]) - ch;
+      v.totalGroups = (h ? groupTotal : group0[1]) - g;
+    }
+  }
 
-  PassGroups xs, ys, zs;
-  bool pass0 = false;  // some cubelet needs the stand-alone first select pass
+  PassGroups xs[2], ys[2], zs[2];
+  bool pass0[2] = {false, false};  // a cubelet needs the stand-alone first select pass
   for (int i = 0; i < n; i++) {
-    const bool fused = forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs, ys,
-                                      zs, b.selHist + (size_t)i * kSelectBins, b.state + i);
+    const int h = half_of(i);
+    const bool fused = forward_passes(plans[i], dIn[i], hostIn[i] != 0, b.coef, b.coef2, xs[h],
+                                      ys[h], zs[h], b.selHist + (size_t)i * kSelectBins,
+                                      b.state + i);
     hc[i].selFused = fused ? 1 : 0;
-    pass0 |= !fused;
+    pass0[h] |= !fused;
   }
   std::vector<GroupLaunch> gl;
   size_t hoff = cubBytes + prefBytes;
-  TRY(stage_groups(ctx, xs, hoff, kTuneFwdX, WL_F32, false, gl));
-  const size_t gx = gl.size();
-  TRY(stage_groups(ctx, ys, hoff, kTuneFwdY, WL_F32, false, gl));
-  const size_t gy = gl.size();
-  TRY(stage_groups(ctx, zs, hoff, kTuneFwdZ, WL_F32, false, gl));
+  size_t gb[2][4];  // per half: group index bounds of the x, y, z phases
+  for (int h = 0; h < nh; h++) {
+    gb[h][0] = gl.size();
+    TRY(stage_groups(ctx, xs[h], hoff, kTuneFwdX, WL_F32, false, gl));
+    gb[h][1] = gl.size();
+    TRY(stage_groups(ctx, ys[h], hoff, kTuneFwdY, WL_F32, false, gl));
+    gb[h][2] = gl.size();
+    TRY(stage_groups(ctx, zs[h], hoff, kTuneFwdZ, WL_F32, false, gl));
+    gb[h][3] = gl.size();
+  }
   const size_t upBytes = hoff;
+  cudaStream_t s2 = ctx->stream2;
 
   // ---- device work, in one or two segments (a host step between them
   // computes the log quantizer tables); each may run as a CUDA graph ----
   ctx->launches = 0;
+  // everything after the select for half h on stream st
+  auto post = [&](int h, cudaStream_t st) -> wl_status {
+    DevBatch &v = bh[h];
+    const bool first = h == 0;
+    if (first) CU(record(ctx, ctx->ev[2]));
+    launch_quant_params(v, st);
+    ctx->launches += 1;
+    if (anyLloyd) { launch_lloyd(v, v.coef, maxLloyd, st); ctx->launches += 3; }
+    if (first) mark(ctx, 5);
+    launch_quantize(v, v.coef, maxTable, maxS, st);
+    if (first) mark(ctx, 6);
+    launch_runs(v, st);
+    ctx->launches += 2;
+    if (first) mark(ctx, 7);
+    CU(cudaGetLastError());
+    if (first) CU(record(ctx, ctx->ev[3]));
+    launch_huffman_build(v, maxS, st);
+    ctx->launches += 1;
+    if (first) mark(ctx, 8);
+    CU(cudaGetLastError());
+    if (first) CU(record(ctx, ctx->ev[4]));
+    launch_encode(v, maxS, st);
+    launch_pack_meta(v, st);
+    ctx->launches += 6;
+    if (first) mark(ctx, 9);
+    CU(cudaGetLastError());
+    if (first) CU(record(ctx, ctx->ev[5]));
+    return WL_OK;
+  };
+  // the second half's stream joins the context's stream
+  auto join = [&]() -> wl_status {
+    if (nh == 2) {
+      CU(cudaEventRecord(ctx->halfJ, s2));
+      CU(cudaStreamWaitEvent(s, ctx->halfJ, 0));
+    }
+    return WL_OK;
+  };
   auto quantize_to_end = [&]() -> wl_status {
     if (anyLog) {
       CU(cudaMemcpyAsync(ctx->qtable.p, ctx->hTab.p, (size_t)tableTotal * 4,
                          cudaMemcpyHostToDevice, s));
       CU(cudaMemcpyAsync(ctx->logHdr.p, ctx->hLogHdr.p, n * sizeof(int4), cudaMemcpyHostToDevice, s));
+      if (nh == 2) {  // the second half starts once the tables are on the device
+        CU(cudaEventRecord(ctx->halfT, s));
+        CU(cudaStreamWaitEvent(s2, ctx->halfT, 0));
+      }
     }
-    CU(record(ctx, ctx->ev[2]));
-    launch_quant_params(b, s);
-    ctx->launches += 1;
-    if (anyLloyd) { launch_lloyd(b, b.coef, maxLloyd, s); ctx->launches += 3; }
-    mark(ctx, 5);
-    launch_quantize(b, b.coef, maxTable, maxS, s);
-    mark(ctx, 6);
-    launch_runs(b, s);
-    ctx->launches += 2;
-    mark(ctx, 7);
-    CU(cudaGetLastError());
-    CU(record(ctx, ctx->ev[3]));
-    launch_huffman_build(b, maxS, s);
-    ctx->launches += 1;
-    mark(ctx, 8);
-    CU(cudaGetLastError());
-    CU(record(ctx, ctx->ev[4]));
-    launch_encode(b, maxS, s);
-    launch_pack_meta(b, s);
-    ctx->launches += 6;
-    mark(ctx, 9);
-    CU(cudaGetLastError());
-    CU(record(ctx, ctx->ev[5]));
+    TRY(post(0, s));
+    if (nh == 2) TRY(post(1, s2));
+    TRY(join());
     CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
                        cudaMemcpyDeviceToHost, s));
     return WL_OK;
@@ -1133,24 +1267,43 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     if (anyLloyd) CU(cudaMemsetAsync(ctx->lloydHist.p, 0, (size_t)n * kLloydBins * 4, s));
     launch_select_init(b, s);
     ctx->launches += 1;
+    if (nh == 2) {  // the second half starts with the first
+      CU(cudaEventRecord(ctx->halfT, s));
+      CU(cudaStreamWaitEvent(s2, ctx->halfT, 0));
+    }
     mark(ctx, 0);
-    TRY(launch_phase(ctx, gl, 0, gx));
+    TRY(launch_phase(ctx, gl, gb[0][0], gb[0][1]));
     mark(ctx, 1);
-    TRY(launch_phase(ctx, gl, gx, gy));
+    TRY(launch_phase(ctx, gl, gb[0][1], gb[0][2]));
     mark(ctx, 2);
-    TRY(launch_phase(ctx, gl, gy, gl.size()));
+    TRY(launch_phase(ctx, gl, gb[0][2], gb[0][3]));
     mark(ctx, 3);
     CU(record(ctx, ctx->ev[1]));
+    if (nh == 2) {
+      for (int ph = 0; ph < 3; ph++)
+        TRY(launch_phase_on(ctx, gl, gb[1][ph], gb[1][ph + 1], s2, ctx->side2, ctx->fork2,
+                            ctx->join2));
+    }
     if (coefOut) return WL_OK;
-    launch_select(b, b.coef, pass0, s);
-    ctx->launches += pass0 ? 8 : 7;
+    launch_select(bh[0], bh[0].coef, pass0[0], s);
+    ctx->launches += pass0[0] ? 8 : 7;
+    if (nh == 2) {
+      launch_select(bh[1], bh[1].coef, pass0[1], s2);
+      ctx->launches += pass0[1] ? 8 : 7;
+    }
     CU(cudaGetLastError());
     mark(ctx, 4);
-    if (anyLog)
+    if (anyLog) {
+      TRY(join());
       CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
                          cudaMemcpyDeviceToHost, s));
-    else
-      TRY(quantize_to_end());
+    } else {
+      if (nh == 2) TRY(post(1, s2));
+      TRY(post(0, s));
+      TRY(join());
+      CU(cudaMemcpyAsync(ctx->hState.p, ctx->state.p, n * sizeof(CubeletState),
+                         cudaMemcpyDeviceToHost, s));
+    }
     return WL_OK;
   };
 
@@ -1160,7 +1313,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     std::vector<long long> key;
     key.reserve(4 + (size_t)n * 18);
     key.push_back(n);
-    key.push_back(onDevice | (ctx->profiling ? 2 : 0));
+    key.push_back(onDevice | (ctx->profiling ? 2 : 0) | (nh == 2 ? 4 : 0));
     key.push_back((long long)tune_version());
     for (int i = 0; i < n; i++) {
       const Plan &pl = plans[i];
@@ -1222,16 +1375,19 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   // ---- results ----
   CU(cudaStreamSynchronize(s));
   const CubeletState *hs = H<CubeletState>(ctx->hState);
-  long long totalWords = 0;
+  long long hw0[3] = {0, 0, 0};  // words of each half, then their sum
+  size_t hm0[3] = {0, 0, 0};     // packed metadata ints of each half
   for (int i = 0; i < n; i++) {
     if (hs[i].error)
       return fail(ctx, WL_EINVAL, "cubelet %d: device error %d (code too long or output overflow)",
                   i, hs[i].error);
-    totalWords += hs[i].nWords;
+    const int h = half_of(i);
+    hw0[h] += hs[i].nWords;
+    hm0[h] += hs[i].nDecode +
+              (plans[i].p.quant_alg == WL_LLOYD ? hs[i].nBounds + hs[i].nValues : 0);
   }
-  size_t metaInts = 0;
-  for (int i = 0; i < n; i++)
-    metaInts += hs[i].nDecode + (plans[i].p.quant_alg == WL_LLOYD ? hs[i].nBounds + hs[i].nValues : 0);
+  const long long totalWords = hw0[0] + hw0[1];
+  const size_t metaInts = hm0[0] + hm0[1];
   // words, then the packed decode tables and codebooks, straight into the slab
   const size_t wordsBytes = ((size_t)totalWords * 4 + 15) & ~(size_t)15;
   ResultSlab *slab = slab_pool().acquire(wordsBytes + metaInts * 4 + 16);
@@ -1239,18 +1395,26 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
                          wordsBytes + metaInts * 4 + 16);
   uint32_t *hw = reinterpret_cast<uint32_t *>(slab->base);
   int *hd = reinterpret_cast<int *>(slab->base + wordsBytes);
-  if (totalWords) {
-    const cudaError_t e = cudaMemcpyAsync(hw, b.words, (size_t)totalWords * 4, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+  const long long wAt[2] = {0, hw0[0]};
+  const size_t mAt[2] = {0, hm0[0]};
+  for (int h = 0; h < nh; h++) {
+    if (hw0[h]) {
+      const cudaError_t e = cudaMemcpyAsync(hw + wAt[h], bh[h].words, (size_t)hw0[h] * 4,
+                                            cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+    }
+    if (hm0[h]) {
+      const cudaError_t e = cudaMemcpyAsync(hd + mAt[h], bh[h].meta, hm0[h] * 4,
+                                            cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
+    }
   }
-  if (metaInts) {
-    const cudaError_t e = cudaMemcpyAsync(hd, b.meta, metaInts * 4, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) { slab_pool().release(slab); CU(e); }
-  }
-  std::vector<size_t> decOff(n), cbOff(n, 0);
+  std::vector<size_t> decOff(n), cbOff(n, 0), wOff(n);
   for (int i = 0; i < n; i++) {
-    decOff[i] = (size_t)hs[i].metaBase;
-    cbOff[i] = (size_t)hs[i].metaBase + hs[i].nDecode;
+    const int h = half_of(i);
+    decOff[i] = mAt[h] + (size_t)hs[i].metaBase;
+    cbOff[i] = decOff[i] + hs[i].nDecode;
+    wOff[i] = (size_t)(wAt[h] + hs[i].wordsBase);
   }
   {
     cudaError_t e = cudaEventRecord(ctx->ev[6], s);
@@ -1295,7 +1459,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     r.longest_code = st.longest;
     r.owner = slab;
     r.n_words = st.nWords;
-    r.words = hw + st.wordsBase;
+    r.words = hw + wOff[i];
     r.n_decode = st.nDecode;
     r.decode = hd + decOff[i];
     if (pl.p.quant_alg == WL_LLOYD) {
@@ -2094,6 +2258,17 @@ wl_status wl_init(int device, wl_ctx **out) {
     ctx->fork = nullptr;
   }
   for (auto &e : ctx->pev) cudaEventCreate(&e);
+  bool ok2 = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->halfT, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->halfJ, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ctx->fork2, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < wl_ctx::kSide && ok2; k++)
+    ok2 = cudaStreamCreateWithFlags(&ctx->side2[k], cudaStreamNonBlocking) == cudaSuccess &&
+          cudaEventCreateWithFlags(&ctx->join2[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok2) {
+    cudaGetLastError();  // batches then run as one
+    ctx->splitMode = 0;
+  }
   *out = ctx;
   return WL_OK;
 }
@@ -2123,6 +2298,17 @@ void wl_destroy(wl_ctx *ctx) {
     if (ctx->join[k]) cudaEventDestroy(ctx->join[k]);
   }
   if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->stream2) {
+    cudaStreamSynchronize(ctx->stream2);
+    cudaStreamDestroy(ctx->stream2);
+  }
+  if (ctx->halfT) cudaEventDestroy(ctx->halfT);
+  if (ctx->halfJ) cudaEventDestroy(ctx->halfJ);
+  if (ctx->fork2) cudaEventDestroy(ctx->fork2);
+  for (int k = 0; k < wl_ctx::kSide; k++) {
+    if (ctx->side2[k]) cudaStreamDestroy(ctx->side2[k]);
+    if (ctx->join2[k]) cudaEventDestroy(ctx->join2[k]);
+  }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -2372,6 +2558,16 @@ wl_status wl_set_stream_priority(wl_ctx *ctx, int high) {
   CU(cudaStreamSynchronize(ctx->stream));
   cudaStreamDestroy(ctx->stream);
   ctx->stream = ns;
+  if (ctx->stream2) {
+    cudaStream_t n2 = nullptr;
+    if (cudaStreamCreateWithPriority(&n2, cudaStreamNonBlocking, prio) == cudaSuccess) {
+      cudaStreamSynchronize(ctx->stream2);
+      cudaStreamDestroy(ctx->stream2);
+      ctx->stream2 = n2;
+    } else {
+      cudaGetLastError();
+    }
+  }
   for (int k = 0; k < wl_ctx::kSide; k++)
     if (ctx->side[k]) {
       cudaStreamSynchronize(ctx->side[k]);
