@@ -311,7 +311,8 @@ SERVE_CLASSES = ((0, 1 << 20, "<=1MiB"), (1 << 20, 8 << 20, "1-8MiB"),
 
 
 def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30, device=0,
-              express_lanes=1, small_bytes=4 << 20, max_batch_bytes=32 << 20):
+              express_lanes=1, small_bytes=4 << 20, max_batch_bytes=32 << 20,
+              express_priority=False):
     """Poisson stream of requests (80% compress, 20% decompress) against the
     library's serving loop: payloads with axes log-uniform in 16..512 (at most
     256 MiB each), uint8/uint16/float32 in equal parts, CDF 9/7 with 3 steps
@@ -347,7 +348,7 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30
     which = rng.integers(0, 1 << 30, n)
     srv = lib.Server(lanes=lanes, memory_budget=budget, device=device,
                      express_lanes=express_lanes, small_request_bytes=small_bytes,
-                     max_batch_bytes=max_batch_bytes)
+                     max_batch_bytes=max_batch_bytes, express_priority=express_priority)
     # warm the lanes' buffers with one request of every payload
     for ptr, dt, size, _ in reqs:
         srv.wait(srv.submit_compress(ptr=ptr, dtype=dt, size=size, params=prm))
@@ -399,6 +400,13 @@ def serve_run(lib, seconds, rate=2000.0, seed=20261207, lanes=3, budget=16 << 30
     th.join()
     elapsed = max(t_last[0], time.perf_counter()) - t0
     srv.close()
+    # page-locked buffers back to the system now, not whenever Python
+    # collects them
+    del out_views, srcs
+    for bufs in outs:
+        for b_ in bufs:
+            b_.free()
+    pin.free()
     allv = np.array(lat["compress"] + lat["decompress"])
 
     def pct(v, p_):
@@ -551,7 +559,17 @@ def main():
                          "1024^3 split volume) in the default run")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the serving measurement (0: skip)")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving measurement and print its JSON (the default "
+                         "run starts this in a separate process)")
     args = ap.parse_args()
+    if args.serve_only:
+        from wavelets_gb300 import build
+        build.build()
+        from wavelets_gb300 import lib
+        print(json.dumps(serve_run(lib, args.serve_seconds,
+                                   device=int(os.environ.get("LOCAL_RANK", "0")))), flush=True)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -900,7 +918,19 @@ def main():
     # ---- serving: Poisson request stream, p50/p99 latency ----
     serving = None
     if rank == 0 and args.serve_seconds > 0 and args.workload == "mixed":
-        serving = serve_run(lib, args.serve_seconds, device=local)
+        # in a process of its own, as a server runs: consecutive serving runs
+        # in one long-lived process were measured to get slower run after run
+        # (p99 from ~2.6 ms to over 10 ms), which would charge this section
+        # for what the sections before it left behind
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serve-only",
+                            "--serve-seconds", str(args.serve_seconds)],
+                           capture_output=True, text=True,
+                           timeout=args.serve_seconds * 4 + 300,
+                           env=dict(os.environ, LOCAL_RANK=str(local)))
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        serving = json.loads(lines[-1]) if r.returncode == 0 and lines else {
+            "error": (r.stderr or r.stdout)[-400:]}
+        serving["process"] = "separate (fresh) process"
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(items)

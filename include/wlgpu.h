@@ -239,10 +239,11 @@ typedef struct {
                                one batch; a larger request runs alone (0, the
                                default: no cap) */
   int express_lanes;        /* lanes that take only requests of at most
-                               small_request_bytes, on high-priority streams,
-                               so small requests do not wait behind large
-                               ones (default 0) */
+                               small_request_bytes, so small requests do not
+                               wait behind large ones (default 0) */
   size_t small_request_bytes; /* the express lanes' limit (default 4 MiB) */
+  int express_priority;     /* 1: express lanes on the device's highest-priority
+                               streams (wl_set_stream_priority); default 0 */
 } wl_serve_config;
 
 typedef struct {

@@ -312,6 +312,7 @@ void wl_serve_config_default(wl_serve_config *cfg) {
   cfg->max_batch_bytes = 0;
   cfg->express_lanes = 0;
   cfg->small_request_bytes = (size_t)4 << 20;
+  cfg->express_priority = 0;
 }
 
 wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **out) {
@@ -337,7 +338,7 @@ wl_status wl_serve_create(int device, const wl_serve_config *cfg, wl_server **ou
     }
     s->ctxs.push_back(c);
     wl_set_host_input_mode(c, s->cfg.stage_host_inputs ? 1 : 0);
-    if (i < s->cfg.express_lanes) wl_set_stream_priority(c, 1);
+    if (i < s->cfg.express_lanes && s->cfg.express_priority) wl_set_stream_priority(c, 1);
   }
   for (int i = 0; i < s->cfg.lanes; i++) s->workers.emplace_back(worker, s, i);
   *out = s;

@@ -69,7 +69,7 @@ class WlServeConfig(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("memory_budget", ctypes.c_size_t),
                 ("max_batch", ctypes.c_int), ("stage_host_inputs", ctypes.c_int),
                 ("max_batch_bytes", ctypes.c_size_t), ("express_lanes", ctypes.c_int),
-                ("small_request_bytes", ctypes.c_size_t)]
+                ("small_request_bytes", ctypes.c_size_t), ("express_priority", ctypes.c_int)]
 
 
 class WlRequest(ctypes.Structure):
@@ -905,7 +905,8 @@ class Server:
 
     def __init__(self, lanes: int = 2, memory_budget: int = 16 << 30, max_batch: int = 1024,
                  device: int = 0, stage_host_inputs: bool = True, max_batch_bytes: int = 0,
-                 express_lanes: int = 0, small_request_bytes: int = 4 << 20):
+                 express_lanes: int = 0, small_request_bytes: int = 4 << 20,
+                 express_priority: bool = False):
         self.lib = load()
         cfg = WlServeConfig()
         self.lib.wl_serve_config_default(ctypes.byref(cfg))
@@ -914,6 +915,7 @@ class Server:
         cfg.max_batch_bytes = max_batch_bytes
         cfg.express_lanes = express_lanes
         cfg.small_request_bytes = small_request_bytes
+        cfg.express_priority = 1 if express_priority else 0
         h = ctypes.c_void_p()
         st = self.lib.wl_serve_create(device, ctypes.byref(cfg), ctypes.byref(h))
         if st != WL_OK:
