@@ -403,6 +403,13 @@ void wl_tune_reset(void);
  * a failed capture turns graphs off for the context and wl_graph_error
  * names the reason. */
 wl_status wl_set_graph_mode(wl_ctx *ctx, int mode);
+
+/* Bit-packer slices per 4096-element chunk (no reference counterpart): the
+ * Huffman tokens of a chunk are packed by `slices` lanes (1, 2, 4, 8, 16 or
+ * 32) that each take a contiguous share.  0 (default): the smallest count
+ * that gives the launch at least 16 warps per SM.  The packed bits do not
+ * depend on it. */
+wl_status wl_set_encode_slices(wl_ctx *ctx, int slices);
 wl_status wl_graph_stats(const wl_ctx *ctx, long long out[4]);
 const char *wl_graph_error(const wl_ctx *ctx);
 

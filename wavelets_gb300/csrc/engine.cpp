@@ -299,7 +299,7 @@ struct wl_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, codes, codeLen, decode, chunkSpan,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, encCub, codes, codeLen, decode, chunkSpan,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr,
       errIn, errRest, errPart;
   HostBuf hState, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
@@ -328,6 +328,7 @@ struct wl_ctx {
   cudaStream_t side2[kSide] = {};  // the second half's side streams
   cudaEvent_t fork2 = nullptr, join2[kSide] = {};
   int splitMode = 1;  // 1: split large batches into two staggered halves
+  int encSlices = 0;  // bit-packer slices per chunk; 0: from the batch size
   float timings[6] = {0, 0, 0, 0, 0, 0};
   bool profiling = false;
   cudaEvent_t pev[10] = {};
@@ -965,6 +966,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->state, n * sizeof(CubeletState)));
   TRY(ensure(ctx, ctx->chunkCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->groupCub, chunkTotal * sizeof(int)));
+  TRY(ensure(ctx, ctx->encCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
   if (anyLloyd) TRY(ensure(ctx, ctx->lloydHist, (size_t)n * kLloydBins * 4));
   TRY(ensure(ctx, ctx->qtable, (size_t)tableTotal * 4));
@@ -1082,9 +1084,16 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   // ---- descriptors (host side of the upload block) ----
   CubeletDev *hc = H<CubeletDev>(ctx->hPasses);
   long long *hp = reinterpret_cast<long long *>(H<char>(ctx->hPasses) + cubBytes);
-  long long groupTotal = 0;
-  long long chunk0[2] = {0, 0}, group0[2] = {0, 0}, words0[2] = {0, 0};
+  long long groupTotal = 0, encTotal = 0;
+  long long chunk0[2] = {0, 0}, group0[2] = {0, 0}, words0[2] = {0, 0}, enc0[2] = {0, 0};
   long long wordsAcc = 0;
+  // bit-packer slices per chunk, from each half's chunk count
+  int encF[2] = {1, 1};
+  {
+    long long halfChunks[2] = {0, 0};
+    for (int i = 0; i < n; i++) halfChunks[half_of(i)] += plans[i].nChunks;
+    for (int h = 0; h < nh; h++) encF[h] = ctx->encSlices ? ctx->encSlices : enc_slices(halfChunks[h]);
+  }
   for (int i = 0; i < n; i++) {
     const Plan &pl = plans[i];
     const int h = half_of(i);
@@ -1092,6 +1101,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       chunk0[h] = pl.chunkBase;
       group0[h] = groupTotal;
       words0[h] = wordsAcc;
+      enc0[h] = encTotal;
     }
     CubeletDev &c = hc[i];
     memset(&c, 0, sizeof c);
@@ -1109,6 +1119,8 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     c.tableOff = pl.tableOff;
     c.groupBase = (int)(groupTotal - group0[h]);
     groupTotal += (pl.nChunks + kQuantGroup - 1) / kQuantGroup;
+    c.encBase = (int)(encTotal - enc0[h]);
+    encTotal += ((long long)pl.nChunks * encF[h] + 31) / 32;
     wordsAcc += pl.wordsCap;
     hp[i] = c.chunkBase;
   }
@@ -1140,6 +1152,9 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.chunkCub = P<int>(ctx->chunkCub);
   b.groupCub = P<int>(ctx->groupCub);
   b.totalGroups = groupTotal;
+  b.encCub = P<int>(ctx->encCub);
+  b.totalEnc = encTotal;
+  b.encF = encF[0];
   b.logHdr = P<int4>(ctx->logHdr);
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
@@ -1170,6 +1185,9 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       v.chunkBits += ch;
       v.chunkCub += ch;
       v.groupCub += g;
+      v.encCub += enc0[h];
+      v.totalEnc = (h ? encTotal : enc0[1]) - enc0[h];
+      v.encF = encF[h];
       v.words += words0[h];
       v.meta += c0 * kMetaPer;
       v.totalChunks = (h ? chunkTotal : chunk0[1]) - ch;
@@ -1315,6 +1333,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     key.push_back(n);
     key.push_back(onDevice | (ctx->profiling ? 2 : 0) | (nh == 2 ? 4 : 0));
     key.push_back((long long)tune_version());
+    key.push_back(ctx->encSlices);
     for (int i = 0; i < n; i++) {
       const Plan &pl = plans[i];
       const wl_params &q = pl.p;
@@ -2281,6 +2300,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->state,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkCub, &ctx->groupCub,
+                   &ctx->encCub,
                    &ctx->chunkSpan, &ctx->optIn, &ctx->optOut, &ctx->optErr,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,
@@ -2588,6 +2608,12 @@ size_t wl_memory_held(const wl_ctx *ctx) { return ctx ? ctx->devBytes : 0; }
 wl_status wl_set_host_input_mode(wl_ctx *ctx, int mode) {
   if (!ctx || mode < 0 || mode > 1) return WL_EINVAL;
   ctx->stageHost = mode;
+  return WL_OK;
+}
+
+wl_status wl_set_encode_slices(wl_ctx *ctx, int slices) {
+  if (!ctx || slices < 0 || slices > 32 || (slices & (slices - 1))) return WL_EINVAL;
+  ctx->encSlices = slices;
   return WL_OK;
 }
 

@@ -19,9 +19,8 @@
 // bit_stream.h:60-162): every coefficient yields zero or one token -- its own
 // code, a single zero-bin code, or at the first element of a dup chunk the
 // zero-run key code followed by 3 length bits.  Token lengths are summed per
-// 4096-element chunk, chunk offsets are scanned per cubelet, and each chunk
-// ORs its tokens into a shared-memory copy of its words; words wholly inside
-// a chunk are stored directly, the two edge words are ORed into global memory.
+// 4096-element chunk, chunk offsets are scanned per cubelet, and lanes pack
+// slices of a chunk's tokens in registers (the bit packer below).
 #include "wl_internal.h"
 
 namespace wl {
@@ -235,26 +234,6 @@ __device__ __forceinline__ int token_len(uint16_t t, const uint8_t *len, int dup
   return len[sym] + (sym == dupKey ? 3 : 0);
 }
 
-// exclusive block scan (256 threads)
-__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned *sh, unsigned &total) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned inc = v;
-  for (int off = 1; off < 32; off <<= 1) {
-    unsigned t = __shfl_up_sync(0xffffffffu, inc, off);
-    if (lane >= off) inc += t;
-  }
-  if (lane == 31) sh[w] = inc;
-  __syncthreads();
-  unsigned before = 0;
-  total = 0;
-  for (int i = 0; i < kThreads / 32; i++) {
-    if (i < w) before += sh[i];
-    total += sh[i];
-  }
-  __syncthreads();
-  return before + inc - v;
-}
-
 // Bits of a chunk: the code lengths of its tokens, read straight from its slot.
 __global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
   // one CTA per group of kQuantGroup chunks of a cubelet: the code lengths
@@ -395,126 +374,151 @@ __global__ void encode_zero_kernel(DevBatch b) {
   w[(end - 1) >> 5] = 0;
 }
 
-// Chunk words staged in shared memory; a chunk longer than this (only with
-// very long codes) ORs its bits straight into global memory instead.
-constexpr int kWriteWords = 2048;
+// ---- bit packer -------------------------------------------------------------
+// A chunk's tokens are cut into F slices of ceil(n / F) tokens (F from
+// enc_slices, per launch); lane s of the chunk's F lanes packs slice s, and a
+// one-warp CTA takes 32 / F consecutive chunks of one cubelet.  With F = 1 a
+// lane's first bit is its chunk's offset from the scan; with F > 1 each lane
+// sums its slice's code lengths and an F-lane exclusive scan places the
+// slices.  A lane keeps its bits in a 64-bit register and stores whole words:
+// words wholly inside its slice are stored directly, its first and last word
+// (which it may share with neighbouring slices) are OR-ed in.  A word shared
+// by slices of one chunk is zeroed by the lane whose slice starts in it,
+// before any lane of the chunk ORs (the chunk's lanes are one warp); the
+// chunk's first and last words, shared with neighbouring chunks, were zeroed
+// by encode_zero_kernel.  Tokens are read with 16-byte loads: a slot starts
+// at a multiple of 128 bytes and holds kChunk tokens, so the aligned blocks
+// around a slice stay inside its chunk's slot.
 
-__host__ __device__ inline size_t write_smem_bytes(int S) {
-  return (size_t)S * 8 + (((size_t)S + 15) & ~(size_t)15) + (size_t)kWriteWords * 4;
+// code bits (below kMaxCodeBits) and length (above) of one symbol
+constexpr unsigned long long kCodeMask = (1ull << kMaxCodeBits) - 1;
+
+// f(token, table entry) for tokens [a, e) of a slot, in order; the eight
+// table entries of a 16-byte block are read before any of them is used
+template <class Fn>
+__device__ __forceinline__ void for_tokens(const uint16_t *slot, int a, int e,
+                                           const unsigned long long *tab, Fn &&f) {
+  if (a >= e) return;
+  const uint4 *p = reinterpret_cast<const uint4 *>(slot) + (a >> 3);
+  const uint4 *pe = reinterpret_cast<const uint4 *>(slot) + ((e + 7) >> 3);
+  for (int i = a & ~7; p < pe; p++, i += 8) {
+    const uint4 q = *p;
+    const unsigned w[4] = {q.x, q.y, q.z, q.w};
+    unsigned t[8];
+    unsigned long long en[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      t[k] = (w[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+      en[k] = tab[t[k] & 0x1fff];
+    }
+    if (i >= a && i + 8 <= e) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) f(t[k], en[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if (i + k >= a && i + k < e) f(t[k], en[k]);
+    }
+  }
 }
 
-__global__ void __launch_bounds__(kThreads) encode_write_kernel(DevBatch b) {
-  __shared__ uint16_t list[kMaxChunkTokens];
-  __shared__ unsigned shs[kThreads / 32];
-  extern __shared__ unsigned long long wsm[];
-  const int ci = b.groupCub[blockIdx.x];
+__global__ void __launch_bounds__(32, 32) encode_write_kernel(DevBatch b) {
+  extern __shared__ unsigned long long sTab[];  // code | length << kMaxCodeBits
+  const int ci = b.encCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
   const CubeletState *st = b.state + ci;
   if (st->error) return;
-  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
-  const int nc = min(kQuantGroup, cd.nChunks - c0);
-  const int dupKey = cd.binCount;
-  const int S = cd.binCount + 1;
-  // tables sized for this cubelet's alphabet (the launch sizes for the largest)
-  unsigned long long *sCode = wsm;
-  uint8_t *sLen = reinterpret_cast<uint8_t *>(sCode + S);
-  uint32_t *sw = reinterpret_cast<uint32_t *>(sLen + ((S + 15) & ~15));
-  for (int i = threadIdx.x; i < S; i += kThreads) {
-    sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
-    sCode[i] = b.codes[(size_t)ci * kMaxSymbols + i];
+  const int lane = threadIdx.x;
+  const int lgF = __ffs(b.encF) - 1, F = 1 << lgF;
+  const int dupKey = cd.binCount, S = cd.binCount + 1;
+  {
+    const unsigned long long *gc = b.codes + (size_t)ci * kMaxSymbols;
+    const uint8_t *gl = b.codeLen + (size_t)ci * kMaxSymbols;
+    for (int i = lane; i < S; i += 32)
+      sTab[i] = (gc[i] & kCodeMask) | ((unsigned long long)gl[i] << kMaxCodeBits);
   }
-  for (int k = 0; k < nc; k++) {
-    const long long chunk = cd.chunkBase + c0 + k;
-    const unsigned long long chunkOff = b.chunkBits[chunk];
-    const unsigned long long chunkEnd = (chunk + 1 < cd.chunkBase + cd.nChunks)
-                                            ? b.chunkBits[chunk + 1] : st->totalBits;
-    const int shift = (int)(chunkOff & 31);
-    const int nW = (int)((shift + (chunkEnd - chunkOff) + 31) >> 5);
-    uint32_t *gw = b.words + st->wordsBase + (chunkOff >> 5);
-    const bool staged = nW <= kWriteWords;
-    if (staged) {
-      for (int i = threadIdx.x; i < nW; i += kThreads) sw[i] = 0;
-    } else {
-      // interior words belong to this chunk alone; the edge words were zeroed
-      // by encode_zero_kernel and are shared with the neighbours
-      for (int i = 1 + threadIdx.x; i < nW - 1; i += kThreads) gw[i] = 0;
-    }
-    const int2 span = b.chunkSpan[chunk];
-    const uint16_t *src = b.tok + cd.coefOff + (chunk - cd.chunkBase) * (long long)kChunk + span.x;
-    const int n = span.y;
-    for (int i = threadIdx.x; i < n; i += kThreads) list[i] = src[i];
-    __syncthreads();
-    const uint16_t *tl = list;
-    uint32_t *dstw = staged ? sw : gw;
-    // each thread takes a contiguous slice of the tokens
-    const int per = (n + kThreads - 1) / kThreads;
-    const int t0 = min(n, (int)threadIdx.x * per), t1 = min(n, t0 + per);
+  __syncwarp();
+  const int cl = (((int)blockIdx.x - cd.encBase) << (5 - lgF)) + (lane >> lgF);
+  const int sub = lane & (F - 1);
+  const bool okc = cl < cd.nChunks;
+  const long long chunk = cd.chunkBase + cl;
+  unsigned long long off = 0, end = 0;
+  int2 span = make_int2(0, 0);
+  if (okc) {
+    off = b.chunkBits[chunk];
+    end = cl + 1 < cd.nChunks ? b.chunkBits[chunk + 1] : st->totalBits;
+    span = b.chunkSpan[chunk];
+  }
+  const int m = (span.y + F - 1) >> lgF;
+  const int t0 = min(span.y, sub * m), t1 = min(span.y, t0 + m);
+  const uint16_t *slot = b.tok + cd.coefOff + (long long)cl * kChunk;
+  // the slice's bits and first bit
+  unsigned long long sb = end - off, pos = off;
+  if (F > 1) {
     unsigned mine = 0;
-    for (int i = t0; i < t1; i++) mine += token_len(tl[i], sLen, dupKey);
-    unsigned total;
-    const unsigned pos = block_excl_scan(mine, shs, total) + shift;
-    // The slice's bits are packed in a register and leave a word at a time:
-    // words wholly inside the slice are stored, the first and the last
-    // (shared with the neighbouring slices) are OR-ed in.
-    if (mine > 0) {
-      unsigned w = pos >> 5;
-      const unsigned wFirst = w;
-      unsigned long long acc = 0;  // bit 0 = bit 0 of word w
-      int bits = (int)(pos & 31);
-      for (int i = t0; i < t1; i++) {
-        const uint16_t t = tl[i];
-        const int sym = t & 0x1fff;
-        int l = sLen[sym];
-        unsigned long long v = sCode[sym];
-        if (sym == dupKey) {
-          v |= (unsigned long long)(t >> 13) << l;
-          l += 3;
-        }
-        // the common case: at most 32 bits, one OR into the 64-bit
-        // accumulator (bits < 32 here, and a code has no bits above its
-        // length)
-        if (l <= 32) {
-          acc |= v << bits;
-          bits += l;
-          if (bits >= 32) {
-            if (w == wFirst) atomicOr(&dstw[w], (unsigned)acc);
-            else dstw[w] = (unsigned)acc;
-            w++;
-            acc >>= 32;
-            bits -= 32;
-          }
-          continue;
-        }
-        // up to 61 bits, appended at most 32 at a time (bits < 32 here)
-        while (l > 0) {
-          const int take = l < 32 ? l : 32;
-          acc |= (v & ((1ull << take) - 1)) << bits;
-          bits += take;
-          v >>= take;
-          l -= take;
-          if (bits >= 32) {
-            if (w == wFirst) atomicOr(&dstw[w], (unsigned)acc);
-            else dstw[w] = (unsigned)acc;
-            w++;
-            acc >>= 32;
-            bits -= 32;
-          }
-        }
-      }
-      if (bits > 0) atomicOr(&dstw[w], (unsigned)acc);
+    if (okc)
+      for_tokens(slot, span.x + t0, span.x + t1, sTab, [&](unsigned t, unsigned long long en) {
+        mine += (unsigned)(en >> kMaxCodeBits) + ((int)(t & 0x1fff) == dupKey ? 3u : 0u);
+      });
+    unsigned inc = mine;
+    for (int d = 1; d < F; d <<= 1) {
+      const unsigned x = __shfl_up_sync(0xffffffffu, inc, d, F);
+      if (sub >= d) inc += x;
     }
-    __syncthreads();
-    if (staged) {
-      for (int i = threadIdx.x; i < nW; i += kThreads) {
-        if (i == 0 || i == nW - 1) {
-          if (sw[i]) atomicOr(&gw[i], sw[i]);
-        } else {
-          gw[i] = sw[i];
-        }
-      }
-      __syncthreads();  // sw and the token list are reused by the next chunk
-    }
+    sb = mine;
+    pos = off + (inc - mine);
   }
+  uint32_t *gw = b.words + st->wordsBase;
+  const bool any = okc && sb > 0;
+  if (any && F > 1) {
+    const unsigned long long fw = pos >> 5;
+    if (fw > (off >> 5) && fw < ((end - 1) >> 5)) gw[fw] = 0;
+  }
+  __syncwarp();
+  if (!any) return;
+  unsigned long long w = pos >> 5;
+  const unsigned long long wFirst = w;
+  unsigned long long acc = 0;  // bit 0 = bit 0 of word w
+  int bits = (int)(pos & 31);
+  for_tokens(slot, span.x + t0, span.x + t1, sTab, [&](unsigned t, unsigned long long e) {
+    const int sym = t & 0x1fff;
+    int l = (int)(e >> kMaxCodeBits);
+    unsigned long long v = e & kCodeMask;
+    if (sym == dupKey) {
+      v |= (unsigned long long)(t >> 13) << l;
+      l += 3;
+    }
+    // the common case: at most 32 bits, one OR into the accumulator (bits <
+    // 32 here, and a code has no bits above its length)
+    if (l <= 32) {
+      acc |= v << bits;
+      bits += l;
+      if (bits >= 32) {
+        if (w == wFirst) atomicOr(&gw[w], (unsigned)acc);
+        else gw[w] = (unsigned)acc;
+        w++;
+        acc >>= 32;
+        bits -= 32;
+      }
+      return;
+    }
+    // up to 61 bits, appended at most 32 at a time
+    while (l > 0) {
+      const int take = l < 32 ? l : 32;
+      acc |= (v & ((1ull << take) - 1)) << bits;
+      bits += take;
+      v >>= take;
+      l -= take;
+      if (bits >= 32) {
+        if (w == wFirst) atomicOr(&gw[w], (unsigned)acc);
+        else gw[w] = (unsigned)acc;
+        w++;
+        acc >>= 32;
+        bits -= 32;
+      }
+    }
+  });
+  if (bits > 0) atomicOr(&gw[w], (unsigned)acc);
 }
 
 }  // namespace
@@ -533,10 +537,9 @@ void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   encode_scan_kernel<<<b.n, 1024, 0, s>>>(b);
   cubelet_offsets_kernel<<<1, 1024, 0, s>>>(b);
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);
-  const int smem = (int)write_smem_bytes(maxSymbols);
-  // static + dynamic above 48 KB needs the opt-in
+  const int smem = maxSymbols * (int)sizeof(unsigned long long);
   raise_smem_limit(encode_write_kernel, smem);
-  encode_write_kernel<<<(unsigned)b.totalGroups, kThreads, smem, s>>>(b);
+  encode_write_kernel<<<(unsigned)b.totalEnc, 32, smem, s>>>(b);
 }
 
 }  // namespace wl

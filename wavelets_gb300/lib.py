@@ -187,6 +187,7 @@ EXPORTS = {
     "wl_tune_import": (ctypes.c_int, [ctypes.c_char_p]),
     "wl_tune_reset": (None, []),
     "wl_set_graph_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "wl_set_encode_slices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "wl_graph_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "wl_graph_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "wl_error_metrics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WlResult),
@@ -754,6 +755,11 @@ class Context:
 
     def memory_held(self) -> int:
         return self.lib.wl_memory_held(self.h)
+
+    def set_encode_slices(self, slices: int):
+        """Bit-packer lanes per 4096-element chunk (1, 2, 4, 8, 16, 32);
+        0 = chosen from the batch size.  The output does not depend on it."""
+        self._check(self.lib.wl_set_encode_slices(self.h, int(slices)))
 
     def set_graph_mode(self, mode: int):
         """1: capture a batch geometry seen twice in a row as a CUDA graph
