@@ -299,7 +299,7 @@ struct wl_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   DevBuf input, coef, coef2, bins, tokCount, state, selHist, lloydHist, qtable, dqtable, qlut,
-      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, encCub, codes, codeLen, decode, chunkSpan,
+      hist, chunkRun, chunkRunCtx, chunkBits, chunkCub, groupCub, encCub, sliceOff, codes, codeLen, decode, chunkSpan,
       words, passes, logHdr, outbuf, decWords, decTable, decWs, meta, optIn, optOut, optErr,
       errIn, errRest, errPart;
   HostBuf hState, hDecode, hPasses, hTab, hLogHdr, hPrefix, hIn, hVals, hFlags;
@@ -967,6 +967,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   TRY(ensure(ctx, ctx->chunkCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->groupCub, chunkTotal * sizeof(int)));
   TRY(ensure(ctx, ctx->encCub, chunkTotal * sizeof(int)));
+  TRY(ensure(ctx, ctx->sliceOff, chunkTotal * 32 * sizeof(unsigned)));
   TRY(ensure(ctx, ctx->selHist, (size_t)n * kSelectBins * 4));
   if (anyLloyd) TRY(ensure(ctx, ctx->lloydHist, (size_t)n * kLloydBins * 4));
   TRY(ensure(ctx, ctx->qtable, (size_t)tableTotal * 4));
@@ -1120,7 +1121,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
     c.groupBase = (int)(groupTotal - group0[h]);
     groupTotal += (pl.nChunks + kQuantGroup - 1) / kQuantGroup;
     c.encBase = (int)(encTotal - enc0[h]);
-    encTotal += ((long long)pl.nChunks * encF[h] + 31) / 32;
+    encTotal += ((long long)pl.nChunks * encF[h] + kEncThreads - 1) / kEncThreads;
     wordsAcc += pl.wordsCap;
     hp[i] = c.chunkBase;
   }
@@ -1155,6 +1156,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
   b.encCub = P<int>(ctx->encCub);
   b.totalEnc = encTotal;
   b.encF = encF[0];
+  b.sliceOff = P<unsigned>(ctx->sliceOff);
   b.logHdr = P<int4>(ctx->logHdr);
   b.meta = P<int>(ctx->meta);
   b.totalChunks = chunkTotal;
@@ -1188,6 +1190,7 @@ wl_status compress_impl(wl_ctx *ctx, const wl_cubelet *items, int n, int onDevic
       v.encCub += enc0[h];
       v.totalEnc = (h ? encTotal : enc0[1]) - enc0[h];
       v.encF = encF[h];
+      v.sliceOff += ch * 32;
       v.words += words0[h];
       v.meta += c0 * kMetaPer;
       v.totalChunks = (h ? chunkTotal : chunk0[1]) - ch;
@@ -2300,7 +2303,7 @@ void wl_destroy(wl_ctx *ctx) {
                    &ctx->state,
                    &ctx->selHist, &ctx->lloydHist, &ctx->qtable, &ctx->dqtable, &ctx->qlut, &ctx->hist,
                    &ctx->chunkRun, &ctx->chunkRunCtx, &ctx->chunkBits, &ctx->chunkCub, &ctx->groupCub,
-                   &ctx->encCub,
+                   &ctx->encCub, &ctx->sliceOff,
                    &ctx->chunkSpan, &ctx->optIn, &ctx->optOut, &ctx->optErr,
                    &ctx->codes, &ctx->codeLen, &ctx->decode, &ctx->words, &ctx->passes,
                    &ctx->logHdr, &ctx->outbuf, &ctx->decWords, &ctx->decTable, &ctx->decWs,

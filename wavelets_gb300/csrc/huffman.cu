@@ -227,43 +227,114 @@ __global__ void __launch_bounds__(kBuildThreads) huffman_build_kernel(DevBatch b
 // A chunk's tokens, in stream order, are slots [span.x, span.x + span.y) of
 // its token slot: the zero-run tokens entering it, its stored tokens and the
 // zero-run tokens leaving it (quantize_kernel and runs_kernel put them there).
-constexpr int kMaxChunkTokens = kChunk;
 
-__device__ __forceinline__ int token_len(uint16_t t, const uint8_t *len, int dupKey) {
-  const int sym = t & 0x1fff;
-  return len[sym] + (sym == dupKey ? 3 : 0);
+// ---- bit packer -------------------------------------------------------------
+// A chunk's tokens are cut into F slices of ceil(n / F) tokens (F from
+// enc_slices, per launch); lane s of the chunk's F lanes packs slice s, and a
+// CTA of kEncThreads lanes takes kEncThreads / F consecutive chunks of one
+// cubelet.  The bit
+// counter sums each slice's code lengths and places the slices inside their
+// chunk with an F-lane exclusive scan; the packer starts each slice at its
+// chunk's offset (from the per-cubelet scan) plus that place.  A lane keeps
+// its bits in a 64-bit register and stores whole words: words wholly inside
+// its slice are stored directly, its first and last word (which it may share
+// with neighbouring slices) are OR-ed in.  A word shared
+// by slices of one chunk is zeroed by the lane whose slice starts in it,
+// before any lane of the chunk ORs (the chunk's lanes are one warp); the
+// chunk's first and last words, shared with neighbouring chunks, were zeroed
+// by encode_zero_kernel.  Tokens are read with 16-byte loads: a slot starts
+// at a multiple of 128 bytes and holds kChunk tokens, so the aligned blocks
+// around a slice stay inside its chunk's slot.
+
+// code bits (below kMaxCodeBits) and length (above) of one symbol
+constexpr unsigned long long kCodeMask = (1ull << kMaxCodeBits) - 1;
+
+// f(token, table entry) for tokens [a, e) of a slot, in order.  In a block
+// of eight tokens that all lie in [a, e) the table entries are read before
+// any is used; in the blocks at the ends only the tokens inside [a, e) are
+// looked up (the other slots hold other slices' tokens or stale values).
+template <class T, class Fn>
+__device__ __forceinline__ void for_tokens(const uint16_t *slot, int a, int e, const T *tab,
+                                           Fn &&f) {
+  if (a >= e) return;
+  const uint4 *p = reinterpret_cast<const uint4 *>(slot) + (a >> 3);
+  const uint4 *pe = reinterpret_cast<const uint4 *>(slot) + ((e + 7) >> 3);
+  for (int i = a & ~7; p < pe; p++, i += 8) {
+    const uint4 q = *p;
+    const unsigned w[4] = {q.x, q.y, q.z, q.w};
+    if (i >= a && i + 8 <= e) {
+      unsigned t[8];
+      T en[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        t[k] = (w[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+        en[k] = tab[t[k] & 0x1fff];
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) f(t[k], en[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        if (i + k >= a && i + k < e) {
+          const unsigned t = (w[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+          f(t, tab[t & 0x1fff]);
+        }
+      }
+    }
+  }
 }
 
-// Bits of a chunk: the code lengths of its tokens, read straight from its slot.
-__global__ void __launch_bounds__(kThreads) encode_count_kernel(DevBatch b) {
-  // one CTA per group of kQuantGroup chunks of a cubelet: the code lengths
-  // are loaded once, and each chunk's tokens are summed by kWpc warps
-  constexpr int kWpc = (kThreads / 32) / kQuantGroup;
-  static_assert(kWpc >= 1 && kWpc * kQuantGroup * 32 == kThreads, "warps per chunk");
-  __shared__ uint8_t sLen[kMaxSymbols + 3];
-  __shared__ unsigned sBits[kQuantGroup];
-  const int ci = b.groupCub[blockIdx.x];
+// Slice geometry shared by the bit counter and the packer: chunk `cl` of the
+// cubelet (within its CTA's run), slice `sub` of it, tokens [t0, t1) of the
+// chunk's token list.
+struct SliceAt {
+  int cl, sub, t0, t1;
+  bool ok;        // the chunk exists
+  long long chunk;
+  int2 span;      // first token slot, token count
+};
+__device__ __forceinline__ SliceAt slice_at(const DevBatch &b, const CubeletDev &cd, int lgF) {
+  SliceAt r;
+  const int lane = threadIdx.x;
+  r.cl = (((int)blockIdx.x - cd.encBase) << (7 - lgF)) + (lane >> lgF);
+  r.sub = lane & ((1 << lgF) - 1);
+  r.ok = r.cl < cd.nChunks;
+  r.chunk = cd.chunkBase + r.cl;
+  r.span = r.ok ? b.chunkSpan[r.chunk] : make_int2(0, 0);
+  const int m = (r.span.y + (1 << lgF) - 1) >> lgF;
+  r.t0 = min(r.span.y, r.sub * m);
+  r.t1 = min(r.span.y, r.t0 + m);
+  return r;
+}
+
+// Bits of every slice: lane s of a chunk's F lanes sums its tokens' code
+// lengths, an F-lane exclusive scan places the slice inside the chunk
+// (sliceOff), and the chunk's last lane writes the chunk's bit count.
+__global__ void __launch_bounds__(kEncThreads) encode_count_kernel(DevBatch b) {
+  extern __shared__ uint8_t sLen[];
+  const int ci = b.encCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
-  const int c0 = ((int)blockIdx.x - cd.groupBase) * kQuantGroup;
-  const int nc = min(kQuantGroup, cd.nChunks - c0);
-  const int dupKey = cd.binCount;
-  const int S = cd.binCount + 1;
-  for (int i = threadIdx.x; i < S; i += kThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
-  if ((int)threadIdx.x < kQuantGroup) sBits[threadIdx.x] = 0;
+  const int lgF = __ffs(b.encF) - 1, F = 1 << lgF;
+  const int dupKey = cd.binCount, S = cd.binCount + 1;
+  for (int i = threadIdx.x; i < S; i += kEncThreads) sLen[i] = b.codeLen[(size_t)ci * kMaxSymbols + i];
   __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = w / kWpc, part = w % kWpc;
-  if (k < nc) {
-    const long long chunk = cd.chunkBase + c0 + k;
-    const int2 span = b.chunkSpan[chunk];
-    const uint16_t *src = b.tok + cd.coefOff + (long long)(c0 + k) * kChunk + span.x;
-    unsigned s = 0;  // at most kChunk tokens of at most 64 bits
-    for (int i = part * 32 + lane; i < span.y; i += kWpc * 32) s += token_len(src[i], sLen, dupKey);
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if (lane == 0 && s) atomicAdd(&sBits[k], s);
+  const SliceAt sl = slice_at(b, cd, lgF);
+  unsigned mine = 0;  // at most kChunk tokens of at most 61 bits
+  if (sl.ok) {
+    const uint16_t *slot = b.tok + cd.coefOff + (long long)sl.cl * kChunk;
+    for_tokens(slot, sl.span.x + sl.t0, sl.span.x + sl.t1, sLen, [&](unsigned t, uint8_t l) {
+      mine += l + ((int)(t & 0x1fff) == dupKey ? 3u : 0u);
+    });
   }
-  __syncthreads();
-  if ((int)threadIdx.x < nc) b.chunkBits[cd.chunkBase + c0 + threadIdx.x] = sBits[threadIdx.x];
+  unsigned inc = mine;
+  for (int d = 1; d < F; d <<= 1) {
+    const unsigned x = __shfl_up_sync(0xffffffffu, inc, d, F);
+    if (sl.sub >= d) inc += x;
+  }
+  if (sl.ok) {
+    b.sliceOff[sl.chunk * 32 + sl.sub] = inc - mine;
+    if (sl.sub == F - 1) b.chunkBits[sl.chunk] = inc;
+  }
 }
 
 // per cubelet: exclusive scan of the chunk bit counts
@@ -374,55 +445,7 @@ __global__ void encode_zero_kernel(DevBatch b) {
   w[(end - 1) >> 5] = 0;
 }
 
-// ---- bit packer -------------------------------------------------------------
-// A chunk's tokens are cut into F slices of ceil(n / F) tokens (F from
-// enc_slices, per launch); lane s of the chunk's F lanes packs slice s, and a
-// one-warp CTA takes 32 / F consecutive chunks of one cubelet.  With F = 1 a
-// lane's first bit is its chunk's offset from the scan; with F > 1 each lane
-// sums its slice's code lengths and an F-lane exclusive scan places the
-// slices.  A lane keeps its bits in a 64-bit register and stores whole words:
-// words wholly inside its slice are stored directly, its first and last word
-// (which it may share with neighbouring slices) are OR-ed in.  A word shared
-// by slices of one chunk is zeroed by the lane whose slice starts in it,
-// before any lane of the chunk ORs (the chunk's lanes are one warp); the
-// chunk's first and last words, shared with neighbouring chunks, were zeroed
-// by encode_zero_kernel.  Tokens are read with 16-byte loads: a slot starts
-// at a multiple of 128 bytes and holds kChunk tokens, so the aligned blocks
-// around a slice stay inside its chunk's slot.
-
-// code bits (below kMaxCodeBits) and length (above) of one symbol
-constexpr unsigned long long kCodeMask = (1ull << kMaxCodeBits) - 1;
-
-// f(token, table entry) for tokens [a, e) of a slot, in order; the eight
-// table entries of a 16-byte block are read before any of them is used
-template <class Fn>
-__device__ __forceinline__ void for_tokens(const uint16_t *slot, int a, int e,
-                                           const unsigned long long *tab, Fn &&f) {
-  if (a >= e) return;
-  const uint4 *p = reinterpret_cast<const uint4 *>(slot) + (a >> 3);
-  const uint4 *pe = reinterpret_cast<const uint4 *>(slot) + ((e + 7) >> 3);
-  for (int i = a & ~7; p < pe; p++, i += 8) {
-    const uint4 q = *p;
-    const unsigned w[4] = {q.x, q.y, q.z, q.w};
-    unsigned t[8];
-    unsigned long long en[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      t[k] = (w[k >> 1] >> (16 * (k & 1))) & 0xffffu;
-      en[k] = tab[t[k] & 0x1fff];
-    }
-    if (i >= a && i + 8 <= e) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) f(t[k], en[k]);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 8; k++)
-        if (i + k >= a && i + k < e) f(t[k], en[k]);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(32, 32) encode_write_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kEncThreads, 8) encode_write_kernel(DevBatch b) {
   extern __shared__ unsigned long long sTab[];  // code | length << kMaxCodeBits
   const int ci = b.encCub[blockIdx.x];
   const CubeletDev cd = b.cub[ci];
@@ -434,42 +457,24 @@ __global__ void __launch_bounds__(32, 32) encode_write_kernel(DevBatch b) {
   {
     const unsigned long long *gc = b.codes + (size_t)ci * kMaxSymbols;
     const uint8_t *gl = b.codeLen + (size_t)ci * kMaxSymbols;
-    for (int i = lane; i < S; i += 32)
+    for (int i = lane; i < S; i += kEncThreads)
       sTab[i] = (gc[i] & kCodeMask) | ((unsigned long long)gl[i] << kMaxCodeBits);
   }
-  __syncwarp();
-  const int cl = (((int)blockIdx.x - cd.encBase) << (5 - lgF)) + (lane >> lgF);
-  const int sub = lane & (F - 1);
-  const bool okc = cl < cd.nChunks;
-  const long long chunk = cd.chunkBase + cl;
+  __syncthreads();
+  const SliceAt sl = slice_at(b, cd, lgF);
   unsigned long long off = 0, end = 0;
-  int2 span = make_int2(0, 0);
-  if (okc) {
-    off = b.chunkBits[chunk];
-    end = cl + 1 < cd.nChunks ? b.chunkBits[chunk + 1] : st->totalBits;
-    span = b.chunkSpan[chunk];
+  if (sl.ok) {
+    off = b.chunkBits[sl.chunk];
+    end = sl.cl + 1 < cd.nChunks ? b.chunkBits[sl.chunk + 1] : st->totalBits;
   }
-  const int m = (span.y + F - 1) >> lgF;
-  const int t0 = min(span.y, sub * m), t1 = min(span.y, t0 + m);
-  const uint16_t *slot = b.tok + cd.coefOff + (long long)cl * kChunk;
-  // the slice's bits and first bit
-  unsigned long long sb = end - off, pos = off;
-  if (F > 1) {
-    unsigned mine = 0;
-    if (okc)
-      for_tokens(slot, span.x + t0, span.x + t1, sTab, [&](unsigned t, unsigned long long en) {
-        mine += (unsigned)(en >> kMaxCodeBits) + ((int)(t & 0x1fff) == dupKey ? 3u : 0u);
-      });
-    unsigned inc = mine;
-    for (int d = 1; d < F; d <<= 1) {
-      const unsigned x = __shfl_up_sync(0xffffffffu, inc, d, F);
-      if (sub >= d) inc += x;
-    }
-    sb = mine;
-    pos = off + (inc - mine);
-  }
+  // the slice's first bit and bit count
+  const unsigned rel = sl.ok ? b.sliceOff[sl.chunk * 32 + sl.sub] : 0u;
+  unsigned nxt = __shfl_down_sync(0xffffffffu, rel, 1, F);
+  if (sl.sub == F - 1) nxt = (unsigned)(end - off);
+  const unsigned long long sb = nxt - rel, pos = off + rel;
+  const uint16_t *slot = b.tok + cd.coefOff + (long long)sl.cl * kChunk;
   uint32_t *gw = b.words + st->wordsBase;
-  const bool any = okc && sb > 0;
+  const bool any = sl.ok && sb > 0;
   if (any && F > 1) {
     const unsigned long long fw = pos >> 5;
     if (fw > (off >> 5) && fw < ((end - 1) >> 5)) gw[fw] = 0;
@@ -480,7 +485,8 @@ __global__ void __launch_bounds__(32, 32) encode_write_kernel(DevBatch b) {
   const unsigned long long wFirst = w;
   unsigned long long acc = 0;  // bit 0 = bit 0 of word w
   int bits = (int)(pos & 31);
-  for_tokens(slot, span.x + t0, span.x + t1, sTab, [&](unsigned t, unsigned long long e) {
+  for_tokens(slot, sl.span.x + sl.t0, sl.span.x + sl.t1, sTab,
+             [&](unsigned t, unsigned long long e) {
     const int sym = t & 0x1fff;
     int l = (int)(e >> kMaxCodeBits);
     unsigned long long v = e & kCodeMask;
@@ -533,13 +539,13 @@ void launch_pack_meta(DevBatch &b, cudaStream_t s) { pack_meta_kernel<<<b.n, 256
 
 void launch_encode(DevBatch &b, int maxSymbols, cudaStream_t s) {
   const unsigned chunks = (unsigned)b.totalChunks;
-  encode_count_kernel<<<(unsigned)b.totalGroups, kThreads, 0, s>>>(b);
+  encode_count_kernel<<<(unsigned)b.totalEnc, kEncThreads, (maxSymbols + 15) & ~15, s>>>(b);
   encode_scan_kernel<<<b.n, 1024, 0, s>>>(b);
   cubelet_offsets_kernel<<<1, 1024, 0, s>>>(b);
   encode_zero_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(b);
   const int smem = maxSymbols * (int)sizeof(unsigned long long);
   raise_smem_limit(encode_write_kernel, smem);
-  encode_write_kernel<<<(unsigned)b.totalEnc, 32, smem, s>>>(b);
+  encode_write_kernel<<<(unsigned)b.totalEnc, kEncThreads, smem, s>>>(b);
 }
 
 }  // namespace wl

@@ -295,7 +295,7 @@ __global__ void chunk_map_kernel(DevBatch b) {
   const int groups = (cd.nChunks + kQuantGroup - 1) / kQuantGroup;
   for (int j = threadIdx.x; j < groups; j += blockDim.x)
     b.groupCub[cd.groupBase + j] = (int)blockIdx.x;
-  const int enc = (int)(((long long)cd.nChunks * b.encF + 31) / 32);
+  const int enc = (int)(((long long)cd.nChunks * b.encF + kEncThreads - 1) / kEncThreads);
   for (int j = threadIdx.x; j < enc; j += blockDim.x) b.encCub[cd.encBase + j] = (int)blockIdx.x;
 }
 

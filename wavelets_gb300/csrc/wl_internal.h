@@ -30,13 +30,15 @@ constexpr int kLutCells = 4096;         // Lloyd bin lookup: cells of the float 
 constexpr int kLutStride = kLutCells + 8;  // per-cubelet table stride (16-byte rows)
 constexpr int kQuantGroup = 8;          // chunks per select / quantize / encode CTA
 // Bit packer: a chunk's tokens are split into F slices (F a power of two,
-// 1..32), one lane each; a one-warp CTA packs 32 / F consecutive chunks of
-// one cubelet.  Short slices keep many warps in flight (a lane's tokens are a
+// 1..32), one lane each; a CTA of kEncThreads lanes packs kEncThreads / F
+// consecutive chunks of one cubelet (four warps: few CTAs, so kernels of
+// another stream still find CTA slots on the SMs).  Short slices keep many warps in flight (a lane's tokens are a
 // serial chain): measured on a 512-cubelet batch (92 K chunks), the encode
 // stage (bit counts, scans, packer) takes 0.70, 0.85, 0.69, 0.59, 0.57 and
 // 0.59 ms for F = 1, 2, 4, 8, 16, 32.
 // F = 16 unless the launch would then have fewer lanes than one full wave of
 // a 152-SM GB300 (2048 per SM); small batches take 32.
+constexpr int kEncThreads = 128;
 constexpr long long kEncFullWave = 152LL * 2048;
 inline int enc_slices(long long chunks) { return chunks * 16 >= kEncFullWave ? 16 : 32; }
 constexpr int kTileBudget = 16384;      // floats of shared memory per DWT tile
@@ -175,7 +177,7 @@ struct CubeletDev {
   int tableOff;           // offset into per-cubelet quantizer tables (floats)
   int nTable;             // entries in the table (log: boundaries; lloyd: boundaries)
   int groupBase;          // first quantize group (kQuantGroup chunks per group)
-  int encBase;            // first bit-packer CTA (32 / F chunks per CTA)
+  int encBase;            // first bit-packer CTA (kEncThreads / F chunks per CTA)
   int selFused;           // 1: the last transform pass gathered the first select
                           // digit and the extremes (no stand-alone first pass)
 };
@@ -211,6 +213,7 @@ struct DevBatch {
   int *encCub;                    // [totalEnc] cubelet of every bit-packer CTA
   long long totalEnc;
   int encF;                       // bit-packer slices per chunk
+  unsigned *sliceOff;             // [totalChunks][32] bit offset of each slice in its chunk
   int4 *logHdr;                   // [n] log table layout from the host
   int *meta;                      // packed decode tables and Lloyd codebooks
   long long totalChunks;
