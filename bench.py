@@ -825,15 +825,22 @@ def main():
             srv.wait_batch(pending.pop(0)).release()
         return time.perf_counter() - t0
 
+    windows = []
     if args.no_stream:
         streamed_ms = e2e_ms
     else:
         stream(4)
-        barrier()
+        # The host-link copy rate varies between windows on these boxes (the
+        # same build measured 4.75 ms per batch in most windows of 20 and 5.6
+        # to 6.4 ms in some; one lane alone shows the same +2 ms windows), so
+        # three windows are timed and the median is reported beside all three.
         nb = max(8, args.steps)  # amortise the window's fill and drain
-        st_s = gmax(stream(nb))
-        barrier()
-        streamed_ms = st_s * 1e3 / nb
+        windows = []
+        for _ in range(3):
+            barrier()
+            windows.append(gmax(stream(nb)) * 1e3 / nb)
+            barrier()
+        streamed_ms = statistics.median(windows)
     srv.close()
     # the same through the Python API (list of Compressed objects per call)
     py_t = []
@@ -874,20 +881,23 @@ def main():
     # Algorithmic HBM bytes of each kernel group per step: the coefficient
     # reads and writes the algorithm cannot avoid (N padded voxels, 4-byte
     # coefficients).  x pass: input + coefficients out; y, z passes: 4N in and
-    # out; select: the first digit pass and the bucket compaction each read
-    # the coefficients (the last two digits work on the few candidates);
+    # out; select: the bucket compaction reads the coefficients (the first
+    # digit is gathered by the z pass while it stores them, and the last two
+    # digits work on the few candidates);
     # quantize: one read of the coefficients; encode: the compressed output.
     group_bytes = {
         "dwt_x": in_bytes + 4 * n_pad, "dwt_y": 8 * n_pad, "dwt_z": 8 * n_pad_z,
-        "select": 2 * 4 * n_pad, "quantize": 4 * n_pad, "encode": comp_bytes,
+        "select": 4 * n_pad, "quantize": 4 * n_pad, "encode": comp_bytes,
         "huffman_build": 0, "runs": 0, "quant_setup": 0}
     per_step = {k: v / n_prof for k, v in kt.items()}
     # the dominant kernel group among those that move bulk data
     dom = max((k for k in per_step if group_bytes.get(k, 0) > 0), key=lambda k: per_step[k])
     dom_gbs = group_bytes[dom] / (per_step[dom] / 1e3) / 1e9 if per_step[dom] > 0 else 0.0
-    # measured DRAM bytes (read + write) per padded voxel of the mixed batch,
-    # from the ncu capture summarised in profiles/step_metrics_mixed128.md
-    traffic_per_voxel = {"quantize": 4.76, "select": 4.44} if args.workload == "mixed" else {}
+    # measured DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per
+    # padded voxel of the mixed batch, from one ncu capture of a batched call
+    # of its first 128 cubelets (select: compaction, candidate histograms and
+    # resolves)
+    traffic_per_voxel = {"quantize": 4.59, "select": 4.40} if args.workload == "mixed" else {}
     traffic = traffic_per_voxel[dom] * n_pad if dom in traffic_per_voxel else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": dom_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": dom_gbs / hbm, "traffic": traffic,
@@ -956,7 +966,9 @@ def main():
                     "how": ("one synchronous wl_compress_batch per step (--no-stream)"
                             if args.no_stream else
                             "wl_serve_submit_batch / wl_serve_wait_batch, two lanes, "
-                            "two batches in flight, inputs copied by the copy engine"),
+                            "two batches in flight, inputs copied by the copy engine; "
+                            "median of three windows of batches"),
+                    "window_ms": windows,
                     "single_call": {"value": world * in_bytes / (e2e_ms / 1e3) / 1e9,
                                     "ms_per_step": e2e_ms,
                                     "how": "one synchronous wl_compress_batch per step, "
