@@ -13,6 +13,11 @@
 // decoding started.  Rounds: a subsequence whose start differs from its
 // predecessor's exit is decoded again from that exit; rounds repeat until no
 // start changes (each round fixes at least the first wrong subsequence).
+// The first kSync token boundaries of every speculative decode are kept, so a
+// later round stops as soon as it lands on one of them: from there on its
+// tokens are the speculative ones, and the exit and element count follow
+// from the record (without it every subsequence would be decoded again,
+// since a speculative start is almost never a token boundary).
 // Then an exclusive scan of the element counts gives every subsequence its
 // output offset, and a last pass decodes again and writes the elements (the
 // bins, or for batched decompression their dequantized values, where zero-bin
@@ -28,6 +33,7 @@ namespace wl {
 namespace {
 
 constexpr int kSubBits = 1024;
+constexpr int kSync = 8;  // token boundaries kept per speculative decode
 constexpr int kLutBits = 12;
 constexpr int kThreads = 256;
 
@@ -170,33 +176,112 @@ __device__ long long decode_span(const DecCub &c, const unsigned *L, long long s
   return p;
 }
 
+// Speculative decode of subsequence i from its first bit, keeping the first
+// kSync token boundaries: rec[k * totalSub + i] = (boundary - start) | (elements
+// before it << 16), all ones where the subsequence ends first (a boundary is at
+// most kSync * 61 bits and 8192 elements past the start).
+__device__ long long decode_span_rec(const DecCub &c, const unsigned *L, long long start,
+                                     long long limit, long long &elems, bool &bad,
+                                     unsigned *rec, long long stride) {
+  long long p = start, e = 0;
+  const long long total = c.nWords * 32;
+  Window win;
+  win.init(c.words, c.nWords, p);
+#pragma unroll
+  for (int k = 0; k < kSync; k++) {
+    unsigned r = ~0u;
+    if (!bad && p < limit && p < total) {
+      int cnt, val;
+      const int used = decode_token(c, L, win, p, cnt, val);
+      if (used <= 0) {
+        bad = true;
+      } else {
+        p += used;
+        e += cnt;
+        r = (unsigned)(p - start) | ((unsigned)e << 16);
+      }
+    }
+    rec[k * stride] = r;
+  }
+  while (!bad && p < limit && p < total) {
+    int cnt, val;
+    const int used = decode_token(c, L, win, p, cnt, val);
+    if (used <= 0) { bad = true; break; }
+    p += used;
+    e += cnt;
+  }
+  elems = e;
+  return p;
+}
+
+// Decode from a true token boundary s (s >= s0, the speculative start) until
+// the position meets a boundary of the speculative decode (then its exit x0
+// and element count e0 hold, less the elements it produced before that
+// boundary) or the subsequence ends.
+__device__ long long decode_span_sync(const DecCub &c, const unsigned *L, long long s,
+                                      long long limit, long long s0, long long x0, long long e0,
+                                      const unsigned *rec, long long stride, long long &elems,
+                                      bool &bad) {
+  long long p = s, e = 0;
+  const long long total = c.nWords * 32;
+  int k = -1;                 // speculative boundary below or at p: k = -1 is s0
+  long long bk = s0, ck = 0;  // its position and the elements before it
+  Window win;
+  win.init(c.words, c.nWords, p);
+  for (;;) {
+    while (bk < p && k + 1 < kSync) {
+      const unsigned r = rec[(k + 1) * stride];
+      if (r == ~0u) break;
+      k++;
+      bk = s0 + (r & 0xffffu);
+      ck = r >> 16;
+    }
+    if (bk == p) {  // on the speculative path from here
+      elems = e + (e0 - ck);
+      return x0;
+    }
+    if (!(p < limit && p < total)) break;
+    int cnt, val;
+    const int used = decode_token(c, L, win, p, cnt, val);
+    if (used <= 0) { bad = true; break; }
+    p += used;
+    e += cnt;
+  }
+  elems = e;
+  return p;
+}
+
 __global__ void spec_kernel(const DecCub *cubs, int nCub, const unsigned *lut, long long totalSub,
                             long long *start, long long *exitPos, long long *elems, int *flags,
-                            int round) {
+                            int round, unsigned *rec, long long *spec0) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= totalSub) return;
   const int ci = find_cub(cubs, nCub, i);
   const DecCub c = cubs[ci];
   const long long local = i - c.subBase;
-  long long s;
+  const long long s0 = local * kSubBits, limit = (local + 1) * kSubBits;
+  bool bad = false;
+  long long e, x;
   if (round == 0) {
-    s = local * kSubBits;
+    start[i] = s0;
+    x = decode_span_rec(c, lut + c.lutOff, s0, limit, e, bad, rec + i, totalSub);
+    spec0[2 * i] = x;
+    spec0[2 * i + 1] = e;
   } else {
     if (local == 0) {  // always starts right; carry its exit to this round's buffer
       exitPos[2 * i + (round & 1)] = exitPos[2 * i + ((round - 1) & 1)];
       return;
     }
-    s = exitPos[2 * (i - 1) + ((round - 1) & 1)];
+    const long long s = exitPos[2 * (i - 1) + ((round - 1) & 1)];
     if (s == start[i]) {
       exitPos[2 * i + (round & 1)] = exitPos[2 * i + ((round - 1) & 1)];
       return;
     }
     atomicAdd(&flags[0], 1);
+    start[i] = s;
+    x = decode_span_sync(c, lut + c.lutOff, s, limit, s0, spec0[2 * i], spec0[2 * i + 1],
+                         rec + i, totalSub, e, bad);
   }
-  start[i] = s;
-  bool bad = false;
-  long long e;
-  const long long x = decode_span(c, lut + c.lutOff, s, (local + 1) * kSubBits, e, bad);
   exitPos[2 * i + (round & 1)] = x;
   elems[i] = e;
   if (bad) atomicAdd(&flags[1], 1);
@@ -302,8 +387,12 @@ __global__ void fill_kernel(int *out, long long n, int v) {
 // (items whose table is one node are filled by the caller).  Returns 0 on
 // success, 1 when a stream is malformed or holds fewer elements than its
 // cubelet, -1 on a CUDA error; bad[i] (host, may be NULL) marks the items.
+// per subsequence: start, two exits, element count (32 bytes), the
+// speculative exit and count (16) and its kSync boundaries (4 each)
+constexpr size_t kSubBytes = 48 + 4 * kSync;
+
 size_t decode_batch_workspace_bytes(int n, long long totalSub) {
-  return (size_t)n * sizeof(DecCub) + 256 + (size_t)n * 4096 * 4 + (size_t)totalSub * 8 * 4 +
+  return (size_t)n * sizeof(DecCub) + 256 + (size_t)n * 4096 * 4 + (size_t)totalSub * kSubBytes +
          (size_t)n * 8 + 64 + 256;
 }
 
@@ -330,6 +419,8 @@ int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags,
   long long *start = reinterpret_cast<long long *>(p); p += totalSub * 8;
   long long *exitPos = reinterpret_cast<long long *>(p); p += totalSub * 16;
   long long *elems = reinterpret_cast<long long *>(p); p += totalSub * 8;
+  long long *spec0 = reinterpret_cast<long long *>(p); p += totalSub * 16;
+  unsigned *rec = reinterpret_cast<unsigned *>(p); p += totalSub * 4 * kSync;
   long long *total = reinterpret_cast<long long *>(p); p += (size_t)n * 8;
   int *flags = reinterpret_cast<int *>(p);
   if (cudaMemcpyAsync(dc, cs.data(), (size_t)n * sizeof(DecCub), cudaMemcpyHostToDevice, s) !=
@@ -340,12 +431,13 @@ int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags,
   constexpr int kRounds = 6;
   int round = 0;
   cudaMemsetAsync(flags, 0, 8, s);
-  spec_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, flags, 0);
+  spec_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, flags, 0,
+                                        rec, spec0);
   bool converged = false;
   for (round = 1; round <= kRounds; round++) {
     cudaMemsetAsync(flags, 0, 4, s);
     spec_kernel<<<grid, kThreads, 0, s>>>(dc, n, lut, totalSub, start, exitPos, elems, flags,
-                                          round);
+                                          round, rec, spec0);
     cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
     if (hostFlags[0] == 0) { converged = true; break; }
@@ -373,7 +465,7 @@ int decode_streams(const DecodeItem *items, int n, void *ws, int *hostFlags,
 // with zero bits: fill_value() handles that case.
 size_t decode_workspace_bytes(long long nWords) {
   const long long nSub = (nWords * 32 + kSubBits - 1) / kSubBits + 1;
-  return (size_t)nSub * 8 * 4 + 4096 * 4 + 256 + 64;
+  return (size_t)nSub * kSubBytes + 4096 * 4 + 256 + 64;
 }
 
 int decode_stream(const uint32_t *words, long long nWords, const int *table, int nTable,
@@ -387,6 +479,8 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
   long long *start = reinterpret_cast<long long *>(p); p += nSub * 8;
   long long *exitPos = reinterpret_cast<long long *>(p); p += nSub * 16;
   long long *elems = reinterpret_cast<long long *>(p); p += nSub * 8;
+  long long *spec0 = reinterpret_cast<long long *>(p); p += nSub * 16;
+  unsigned *rec = reinterpret_cast<unsigned *>(p); p += nSub * 4 * kSync;
   long long *total = reinterpret_cast<long long *>(p); p += 8;
   int *flags = reinterpret_cast<int *>(p);
   DecCub c{};  // bins out (fout stays null)
@@ -399,11 +493,13 @@ int decode_stream(const uint32_t *words, long long nWords, const int *table, int
   constexpr int kRounds = 6;
   int round = 0;
   cudaMemsetAsync(flags, 0, 8, s);
-  spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, 0);
+  spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, 0, rec,
+                                        spec0);
   bool converged = false;
   for (round = 1; round <= kRounds; round++) {
     cudaMemsetAsync(flags, 0, 4, s);
-    spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, round);
+    spec_kernel<<<grid, kThreads, 0, s>>>(dc, 1, lut, nSub, start, exitPos, elems, flags, round,
+                                          rec, spec0);
     cudaMemcpyAsync(hostFlags, flags, 8, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
     if (hostFlags[0] == 0) { converged = true; break; }
