@@ -599,18 +599,17 @@ quantize_kernel(DevBatch b, const float *__restrict__ coef, int histOff) {
       }
       if (v) {
         int t = nStaged + inc - cnt;
-        if (gap > 8) {  // dup tokens, in the order of run_tokens_short
-          for (int j = gap >> 10; j > 0; j--) stage[t++] = make_token(B, 7);
-          int rr = gap & 1023;
-          while (rr > 8) {
-            const int lg = 31 - __clz(rr);
-            stage[t++] = make_token(B, lg - 3);
-            rr -= 1 << lg;
-          }
-          t += rr;
-        } else {
-          t += gap;
-        }
+        // dup tokens in the order of run_tokens_short: runs of 1024, then
+        // one per set bit of the remainder from 512 down to 16, then 8 when
+        // more than 8 remain; the rest are single (prefilled) tokens
+        for (int j = gap >> 10; j > 0; j--) stage[t++] = make_token(B, 7);
+        const int rr = gap & 1023;
+#pragma unroll
+        for (int lg = 9; lg >= 4; lg--)
+          if ((rr >> lg) & 1) stage[t++] = make_token(B, lg - 3);
+        const bool eight = (rr & 8) && (rr & 7);
+        if (eight) stage[t++] = make_token(B, 0);
+        t += (rr & 8) && !eight ? 8 : (rr & 7);
         stage[t] = make_token(bin, 0);
         atomicAdd(&hist[bin], 1u);
       }
