@@ -331,16 +331,25 @@ __global__ void write_kernel(const DecCub *cubs, int nCub, const unsigned *lut, 
     // zero bin's value everywhere (launch_fill_batch), so only the other
     // values are written; runs and single zero-bin tokens just move on.
     float *F = c.fout;
-    const bool prefilled = c.dupValue >= 0;
+    if (c.dupValue >= 0) {
+      // prefilled: a zero-run token or a single zero-bin token only moves on,
+      // every other token is one value (only the zero-run key counts more
+      // than one element)
+      while (p < limit && p < total && o < c.n) {
+        int cnt, val;
+        const int used = decode_token(c, L, win, p, cnt, val);
+        if (used <= 0) break;
+        p += used;
+        if (val != c.dupValue) F[o] = c.dq[min(max(val, 0), c.binCount - 1)];
+        o = min(o + cnt, c.n);
+      }
+      return;
+    }
     while (p < limit && p < total && o < c.n) {
       int cnt, val;
       const int used = decode_token(c, L, win, p, cnt, val);
       if (used <= 0) break;
       p += used;
-      if (prefilled && val == c.dupValue) {
-        o = min(o + cnt, c.n);
-        continue;
-      }
       const float fv = c.dq[min(max(val, 0), c.binCount - 1)];
       const long long e = min(o + cnt, c.n);
       for (; o < e; o++) F[o] = fv;
