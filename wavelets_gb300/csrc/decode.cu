@@ -125,7 +125,8 @@ struct Window {
 
 __device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, Window &win,
                                             long long p, int &count, int &value) {
-  unsigned long long bits = win.peek(p);
+  const unsigned long long b0 = win.peek(p);  // bits p .. p + 63
+  unsigned long long bits = b0;
   const unsigned e = L[bits & ((1u << kLutBits) - 1)];
   int len, sym;
   if (e & 0x80000000u) {
@@ -147,7 +148,8 @@ __device__ __forceinline__ int decode_token(const DecCub &c, const unsigned *L, 
     sym = c.table[node + 1];
   }
   if (sym == c.dupKey && c.dupKey >= 0) {
-    const unsigned v = (unsigned)(win.peek(p + len) & 7u);
+    // the 3 length bits follow the code; len <= 60, so they are in b0
+    const unsigned v = (unsigned)((b0 >> len) & 7u);
     count = 1 << (v + 3);
     value = c.dupValue;
     return len + 3;
