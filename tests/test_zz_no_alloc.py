@@ -73,3 +73,51 @@ def test_noalloc_rejects_oversize():
     st = L.wl_select_threshold_noalloc(ctypes.c_void_p(1), (64 << 20) + 1, ctypes.c_float(0.5),
                                        None, ctypes.c_void_p(1))
     assert st == lib.WL_EINVAL
+
+
+def test_noalloc_inside_stream_capture():
+    """The use the entry point exists for: after one call outside capture
+    (which looks up the scratch address), a call captured into a CUDA graph
+    on a non-blocking stream, replayed on two different inputs in the same
+    buffer, gives what direct calls give."""
+    torch = pytest.importorskip("torch")
+    from wavelets_gb300 import build
+    build.build()
+    L = lib.load()
+    rng = np.random.default_rng(31)
+    n = 3 * 4096 + 777  # a ragged last chunk
+    data = [rng.standard_normal(n).astype(np.float32) * s for s in (1.0, 40.0)]
+    frac = ctypes.c_float(0.9)
+    dbuf = lib.DeviceBuffer(n * 4)
+    dout = lib.DeviceBuffer(64)
+
+    def read():
+        got = np.zeros(5, np.float32)
+        assert L.wl_copy_to_host(ctypes.c_void_p(got.ctypes.data),
+                                 ctypes.c_void_p(dout.ptr), 20) == lib.WL_OK
+        return got
+
+    try:
+        want = []
+        for d in data:  # direct calls (the first also looks up the scratch)
+            dbuf.upload(d)
+            assert L.wl_select_threshold_noalloc(ctypes.c_void_p(dbuf.ptr), n, frac, None,
+                                                 ctypes.c_void_p(dout.ptr)) == lib.WL_OK
+            torch.cuda.synchronize()
+            want.append(read())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            s = torch.cuda.current_stream().cuda_stream
+            st = L.wl_select_threshold_noalloc(ctypes.c_void_p(dbuf.ptr), n, frac,
+                                               ctypes.c_void_p(s), ctypes.c_void_p(dout.ptr))
+        assert st == lib.WL_OK
+        for d, w in zip(data, want):
+            dbuf.upload(d)
+            torch.cuda.synchronize()
+            g.replay()
+            torch.cuda.synchronize()
+            assert np.array_equal(read(), w)
+        del g
+    finally:
+        dbuf.free()
+        dout.free()
