@@ -26,7 +26,6 @@
 namespace wl {
 namespace {
 
-constexpr int kThreads = kChunkThreads;
 constexpr int kMaxCodeBits = 58;  // + 3 dup bits fits 61 bits -> at most 3 words
 
 // ---- tree -------------------------------------------------------------------
