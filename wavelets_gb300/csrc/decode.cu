@@ -117,9 +117,10 @@ struct Window {
       c = ld(i + 3);
       i++;
     }
-    const int o = (int)(p & 31);
-    const unsigned long long lo = a | ((unsigned long long)b << 32);
-    return o ? ((lo >> o) | ((unsigned long long)c << (64 - o))) : lo;
+    // bits o .. o + 63 of c:b:a, as two 32-bit funnel shifts (o = 0 included)
+    const unsigned o = (unsigned)(p & 31);
+    const unsigned lo = __funnelshift_r(a, b, o), hi = __funnelshift_r(b, c, o);
+    return lo | ((unsigned long long)hi << 32);
   }
 };
 
