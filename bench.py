@@ -273,6 +273,31 @@ def cpu_baseline(items, budget_s=12.0):
                       "oracle/port CPU restatement of the reference path"}
 
 
+# ------------------------------------------------------------------ ranks
+# N GPUs run N independent replicas (cubelets are independent: no exchange),
+# one process each under torchrun; the ranks meet only to start and stop the
+# timed region together and to take the slowest rank's time.
+def rank_barrier(dist):
+    if dist:
+        dist.barrier()
+
+
+def rank_max(dist, x):
+    """The largest x over the ranks (x itself on one rank)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_gbs(world, nbytes_per_rank, max_ms):
+    """Whole-job GB/s of `world` replicas that each processed nbytes_per_rank
+    in the slowest rank's max_ms."""
+    return world * nbytes_per_rank / (max_ms / 1e3) / 1e9
+
+
 def run_reference(args, items, desc, rank, world):
     """--impl reference: the reference algorithm on all host cores; each step
     compresses cubelets (seeded shuffled order) for a bounded time."""
@@ -635,16 +660,10 @@ def main():
                       for (a, p), o in zip(items, offs)]
 
     def barrier():
-        if dist:
-            dist.barrier()
+        rank_barrier(dist)
 
     def gmax(x):
-        if not dist:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(dist, x)
 
     # ---- device-resident batched path (value) ----
     # Results are released as in steady use (the previous batch's results
@@ -706,7 +725,7 @@ def main():
     ctx.set_graph_mode(1)
     comp_bytes = sum(c.compressed_bytes for c in out)
     same = all(np.array_equal(a.words, b) for a, b in zip(out, ref_words))
-    value = world * in_bytes / (step_ms / 1e3) / 1e9
+    value = replica_gbs(world, in_bytes, step_ms)
 
     # ---- batched decompression of the step's results into device memory ----
     decomp = None
@@ -960,7 +979,7 @@ def main():
             "psnr_db_mean": float(np.mean(psnrs)) if psnrs else None,
             "psnr_sample": len(psnrs),
             "deterministic": bool(same and same_h),
-            "e2e": {"value": world * in_bytes / (streamed_ms / 1e3) / 1e9, "unit": UNIT,
+            "e2e": {"value": replica_gbs(world, in_bytes, streamed_ms), "unit": UNIT,
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
                     "ms_per_step": streamed_ms,
                     "how": ("one synchronous wl_compress_batch per step (--no-stream)"
@@ -969,7 +988,7 @@ def main():
                             "two batches in flight, inputs copied by the copy engine; "
                             "median of three windows of batches"),
                     "window_ms": windows,
-                    "single_call": {"value": world * in_bytes / (e2e_ms / 1e3) / 1e9,
+                    "single_call": {"value": replica_gbs(world, in_bytes, e2e_ms),
                                     "ms_per_step": e2e_ms,
                                     "how": "one synchronous wl_compress_batch per step, "
                                            "inputs read in place over the host link",
