@@ -15,13 +15,19 @@ Printed JSON line (rank 0):
               host buffers (wl_serve_submit_batch / wl_serve_wait_batch on
               two lanes, two batches in flight): every step's host->device
               transfer of its inputs (copy engine) and device->host copy of
-              its compressed streams inside the timed region (wall clock);
-              e2e.single_call = one synchronous wl_compress_batch per step
+              its compressed streams inside the timed region (wall clock;
+              the median of three windows of batches, all three in
+              e2e.window_ms); e2e.single_call = one synchronous
+              wl_compress_batch per step
   plain_value the same 512 cubelets compressed one cubelet per call
   serving     a Poisson stream of 2,000 requests/s (80% compress, 20%
               decompress; axes log-uniform 16..512, CDF 9/7 3,3,3, log 256)
-              through the serving loop for --serve-seconds: p50/p99 latency
-              and served GB/s
+              through the serving loop for --serve-seconds, in a process of
+              its own: p50/p99 latency (also per request-size class) and
+              served GB/s
+  workloads   the 2048^2 u8 image, the 256^3 f32 volume and the 1024^3 u16
+              split volume: GB/s, e2e, round-trip PSNR
+  decompress  batched decompression of the step's results
   roofline    the dominant kernel group: its compulsory bytes / its time
   pipeline_roofline  (input + compressed bytes) / whole-step device time
   cpu_baseline the oracle (CPU restatement of the reference path) on a
