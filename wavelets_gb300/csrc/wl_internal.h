@@ -34,8 +34,8 @@ constexpr int kQuantGroup = 8;          // chunks per select / quantize / encode
 // consecutive chunks of one cubelet (four warps: few CTAs, so kernels of
 // another stream still find CTA slots on the SMs).  Short slices keep many warps in flight (a lane's tokens are a
 // serial chain): measured on a 512-cubelet batch (92 K chunks), the encode
-// stage (bit counts, scans, packer) takes 0.70, 0.85, 0.69, 0.59, 0.57 and
-// 0.59 ms for F = 1, 2, 4, 8, 16, 32.
+// stage (per-slice bit counts, scans, packer) took 0.79, 0.76, 0.60, 0.52,
+// 0.50 and 0.52 ms for F = 1, 2, 4, 8, 16, 32.
 // F = 16 unless the launch would then have fewer lanes than one full wave of
 // a 152-SM GB300 (2048 per SM); small batches take 32.
 constexpr int kEncThreads = 128;
